@@ -1,0 +1,454 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 Winograd 3x3 conv2d operator.
+
+Default workload: N=32, C=256, H=W=56, K=256, 3x3, pad 1, stride 1, fp16
+NCHW input ~U[-1,1] and fp16 filter ~N(0, std 1/sqrt(9C)) from a fixed seed,
+run through the operator's C ABI with the reference's algorithm selection
+(F(2x3) fused for this shape) unless --algo says otherwise.
+
+One step = one conv2d call over one batch.  `value` is effective TFLOP/s
+(direct-convolution FLOPs 2*N*K*OH*OW*C*9 / time) with inputs resident in
+HBM; `e2e` is the same metric through the host-buffer C entry point
+(conv2d_fp16_host: pinned input copied in, output copied out, every step).
+Buffer sets rotate so the bytes touched between two uses of one set exceed
+the 129 MB L2.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload cfg2|cfg1|cfg3|...] [--algo ref|fused|2x3|4x3]
+"""
+from __future__ import annotations
+
+import argparse
+import importlib.util
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+METRIC = "3x3 conv eff. TFLOP/s, p50/p99 latency: served vs per-call at fixed rel err"
+L2_BYTES = 129 * 1024 * 1024
+
+# (n, c, h, w, k, input distribution, filter distribution, description)
+WORKLOADS = {
+    "cfg2": (32, 256, 56, 56, 256, "uniform", "normal",
+             "single-shape F(2x3) workload: N=32 C=256 H=W=56 K=256, 3x3 pad 1 stride 1, fp16 NCHW"),
+    "cfg1": (1, 64, 56, 56, 64, "uniform", "uniform",
+             "small workload: N=1 C=64 H=W=56 K=64, 3x3 pad 1 stride 1, fp16 NCHW"),
+    "cfg3": (32, 512, 28, 28, 512, "normal", "normal",
+             "precision-study shape: N=32 C=512 H=W=28 K=512, 3x3 pad 1 stride 1, fp16 NCHW"),
+    "final1": (16, 128, 64, 64, 27, "uniform", "uniform", "contest shape 16x128x64x64 -> 27"),
+    "final2": (16, 256, 32, 32, 256, "uniform", "uniform", "contest shape 16x256x32x32 -> 256"),
+    "final3": (16, 64, 128, 128, 64, "uniform", "uniform", "contest shape 16x64x128x128 -> 64"),
+    "final4": (2, 1920, 32, 32, 640, "uniform", "uniform", "contest shape 2x1920x32x32 -> 640"),
+    "final5": (2, 640, 64, 64, 640, "uniform", "uniform", "contest shape 2x640x64x64 -> 640"),
+    "final6": (2, 320, 64, 64, 4, "uniform", "uniform", "contest shape 2x320x64x64 -> 4"),
+}
+ALGO_ARG = {"ref": -1, "4x3": 0, "2x3": 1, "fused": 2, "auto": 3}
+FALLBACK_PEAKS = {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}
+
+
+def load_pkg():
+    if "wgconv" in sys.modules:
+        return sys.modules["wgconv"]
+    spec = importlib.util.spec_from_file_location("wgconv", os.path.join(ROOT, "dcu-winograd-conv2d_gb300",
+                                                                         "__init__.py"))
+    mod = importlib.util.module_from_spec(spec)
+    sys.modules["wgconv"] = mod
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def load_oracle():
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle  # noqa: E402
+    return oracle
+
+
+def direct_flops(n, c, h, w, k, p=1, q=1):
+    return 2.0 * n * k * (h + 2 * p - 2) * (w + 2 * q - 2) * c * 9
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return d, "measured"
+    except (OSError, ValueError):
+        return dict(FALLBACK_PEAKS), "fallback"
+
+
+def env_dist():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+# ---- clocks sampler ------------------------------------------------------------
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index):
+        self.proc = None
+        self.path = None
+        self.dev = device_index
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(prefix="clocks_", suffix=".csv")
+            os.close(fd)
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.dev), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.fh, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.fh.close()
+        rows = []
+        with open(self.path) as f:
+            for line in f:
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            for nm, val in zip(names, r[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(rows)}
+
+
+# ---- CPU baseline (the reference verifier or its port) -------------------------
+
+def cpu_sample(O, x16, w16, n_img, threads):
+    """Direct conv of `n_img` images on `threads` host threads.  Uses the
+    reference's own conv2dcpu (oracle/_ref) when that build loads here, else
+    the oracle's C port of it.  Returns (seconds, flops, kind)."""
+    import concurrent.futures as cf
+    import numpy as np
+    xs = np.ascontiguousarray(x16[:n_img])
+    n, c, h, w = xs.shape
+    k = w16.shape[0]
+    flops = direct_flops(n, c, h, w, k)
+    if O.ref_lib() is not None:
+        # split output channels across threads; each call is the unmodified function
+        ksplit = max(1, min(threads, k))
+        bounds = [(k * i // ksplit, k * (i + 1) // ksplit) for i in range(ksplit)]
+        parts = [np.ascontiguousarray(w16[a:b]) for a, b in bounds]
+        t0 = time.perf_counter()
+        with cf.ThreadPoolExecutor(max_workers=ksplit) as ex:
+            list(ex.map(lambda wt: O.ref_conv2dcpu(xs, wt), parts))
+        return time.perf_counter() - t0, flops, "reference", ksplit
+    t0 = time.perf_counter()
+    O.conv2d_direct(xs, w16, nthreads=threads, want64=False)
+    return time.perf_counter() - t0, flops, "port", threads
+
+
+def reference_arm(args):
+    """--impl reference: the reference's CPU implementation of the path on the
+    host cores, same workload/metric; each step is a bounded sample."""
+    import numpy as np
+    rank, world, _ = env_dist()
+    if rank != 0:
+        return 0
+    O = load_oracle()
+    if not os.path.exists(O.LIB_PATH):
+        O.build()
+    n, c, h, w, k, xdist, wdist, desc = WORKLOADS[args.workload]
+    rng_x, rng_w = sample_host_inputs(O, args.workload, n_img=1)
+    threads = os.cpu_count() or 1
+    times = []
+    kind = None
+    used = threads
+    for i in range(args.warmup + args.steps):
+        dt, fl, kind, used = cpu_sample(O, rng_x, rng_w, 1, threads)
+        if i >= args.warmup:
+            times.append(dt)
+    mean = sum(times) / len(times)
+    val = fl / mean / 1e12
+    sample = f"1 of {n} images ({fl / 1e9:.2f} GFLOP) per step, all {k} output channels"
+    line = {
+        "impl": "reference", "metric": METRIC, "value": val, "unit": "TFLOP/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": mean * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f16", "data": "synthetic (seeded)",
+        "config": {"workload": desc, "n": n, "c": c, "h": h, "w": w, "k": k, "pad": 1, "stride": 1},
+        "cpu_baseline": {"value": val, "unit": "TFLOP/s", "cores": used, "kind": kind, "sample": sample},
+        "e2e": {"value": val, "unit": "TFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def sample_host_inputs(O, workload, n_img):
+    """Seeded host copy of the first `n_img` images of the workload (and the filter)."""
+    n, c, h, w, k, xdist, wdist, _ = WORKLOADS[workload]
+    import numpy as np
+    rng = np.random.default_rng(20261203)
+    if xdist == "normal":
+        x = rng.standard_normal((n_img, c, h, w)).astype(np.float16)
+    else:
+        x = rng.uniform(-1, 1, size=(n_img, c, h, w)).astype(np.float16)
+    if wdist == "normal":
+        wt = (rng.standard_normal((k, c, 3, 3)) / math.sqrt(9 * c)).astype(np.float16)
+    else:
+        wt = rng.uniform(-1, 1, size=(k, c, 3, 3)).astype(np.float16)
+    return x, wt
+
+
+# ---- our arm ---------------------------------------------------------------------
+
+def make_inputs(torch, workload, device, seed):
+    n, c, h, w, k, xdist, wdist, _ = WORKLOADS[workload]
+    g = torch.Generator(device=device)
+    g.manual_seed(seed)
+    if xdist == "normal":
+        x = torch.randn((n, c, h, w), generator=g, device=device, dtype=torch.float32).half()
+    else:
+        x = (torch.rand((n, c, h, w), generator=g, device=device, dtype=torch.float32) * 2 - 1).half()
+    if wdist == "normal":
+        wt = (torch.randn((k, c, 3, 3), generator=g, device=device) / math.sqrt(9 * c)).half()
+    else:
+        wt = (torch.rand((k, c, 3, 3), generator=g, device=device) * 2 - 1).half()
+    return x, wt
+
+
+def roofline_for(name, wg, geo, ms, pk, pk_kind):
+    n, c, h, w, k, m = geo
+    oh, ow = h, w  # pad 1
+    tiles = n * math.ceil(oh / m) * math.ceil(ow / m)
+    E = (m + 2) ** 2
+    if name in ("fused2x3", "gemm_tcgen05"):
+        flops = 2.0 * E * tiles * c * k
+        ach = flops / (ms * 1e-3) / 1e12
+        peak = pk["bf16_tflops"]
+        return {"kernel": name, "bound": "tensor", "achieved": ach, "peak": peak, "unit": "TFLOP/s",
+                "frac": ach / peak, "peak_source": f"{pk_kind} bf16 dense (burst)",
+                "algorithmic_per_launch": f"{flops / 1e9:.2f} GFLOP (2*{E}*P*C*K)"}
+    if name == "input_transform":
+        byts = 2.0 * n * c * h * w + 2.0 * E * tiles * c
+    else:
+        byts = (4.0 if m == 4 else 2.0) * E * tiles * k + 2.0 * n * k * oh * ow
+    ach = byts / (ms * 1e-3) / 1e9
+    peak = pk["hbm_gbs"]
+    return {"kernel": name, "bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
+            "peak_source": f"{pk_kind} HBM copy", "algorithmic_per_launch": f"{byts / 1e6:.1f} MB"}
+
+
+def committed_traffic(kernel, workload):
+    """DRAM bytes per launch recorded from an ncu capture in profiles/ (a line
+    `traffic <kernel> <workload> <bytes>` in profiles/traffic.txt), else None."""
+    path = os.path.join(ROOT, "profiles", "traffic.txt")
+    try:
+        with open(path) as f:
+            for line in f:
+                parts = line.split()
+                if len(parts) >= 4 and parts[0] == "traffic" and parts[1] == kernel and parts[2] == workload:
+                    return float(parts[3])
+    except OSError:
+        pass
+    return None
+
+
+def our_arm(args):
+    import numpy as np
+    import torch
+
+    rank, world, local = env_dist()
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", init_method="env://")
+    torch.cuda.set_device(local)
+    device = torch.device("cuda", local)
+    wg = load_pkg()
+    wg.lib()  # the CUDA library must load; there is no fallback
+    n, c, h, w, k, xdist, wdist, desc = WORKLOADS[args.workload]
+    flops = direct_flops(n, c, h, w, k)
+
+    opts = wg.default_options(algo=ALGO_ARG[args.algo])
+    if args.gemm_bn:
+        opts.gemm_bn = args.gemm_bn
+    if args.l2_chunk is not None:
+        opts.l2_chunk_bytes = args.l2_chunk
+    in_bytes = 2 * n * c * h * w
+    out_bytes = 2 * n * k * h * w
+    nsets = max(2, math.ceil(3 * L2_BYTES / (in_bytes + out_bytes)))
+    nsets = min(nsets, 16)
+    xs, ys, ops = [], [], []
+    x0, wt = make_inputs(torch, args.workload, device, seed=1234 + rank)
+    for i in range(nsets):
+        x = x0 if i == 0 else x0.roll(i, dims=0).contiguous()
+        y = torch.empty((n, k, h, w), dtype=torch.float16, device=device)
+        prob = wg.make_problem(x.data_ptr(), wt.data_ptr(), y.data_ptr(), n, c, h, w, k)
+        xs.append(x)
+        ys.append(y)
+        ops.append(wg.Conv2d(prob, opts))
+    stream = torch.cuda.current_stream(device)
+    sptr = stream.cuda_stream
+    algo = ops[0].algo
+
+    for i in range(args.warmup):
+        ops[i % nsets](sptr)
+    torch.cuda.synchronize(device)
+    st, site = ops[0].check_device()
+    if st != wg.OK:
+        raise RuntimeError(f"device wait gave up at site {site}")
+
+    sampler = ClockSampler(local)
+    sampler.start()
+    time.sleep(0.3)
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize(device)
+    t_start = torch.cuda.Event(enable_timing=True)
+    t_end = torch.cuda.Event(enable_timing=True)
+    t_start.record(stream)
+    for i in range(args.steps):
+        evs[i][0].record(stream)
+        ops[i % nsets](sptr)
+        evs[i][1].record(stream)
+    t_end.record(stream)
+    torch.cuda.synchronize(device)
+    if dist:
+        dist.barrier()
+    clocks = sampler.stop()
+    total_ms = t_start.elapsed_time(t_end)
+    if dist:
+        tt = torch.tensor([total_ms], device=device)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        total_ms = float(tt.item())
+    per_step = [a.elapsed_time(b) for a, b in evs]
+    ms_per_step = total_ms / args.steps
+    value = world * flops * args.steps / (total_ms * 1e-3) / 1e12
+
+    # per-kernel durations (CUDA events between the launches of one call)
+    names = ops[0].kernel_names()
+    kt = {}
+    reps = min(args.steps, 20)
+    for i in range(reps):
+        d = ops[i % nsets].timed(sptr)
+        for nm, ms in zip(names, d):
+            kt.setdefault(nm, []).append(ms)
+    tot = {nm: sum(v) for nm, v in kt.items()}
+    dominant = max(tot, key=tot.get)
+    launches_of_dom = len(kt[dominant])
+    dom_ms = tot[dominant] / launches_of_dom
+    m = 4 if algo == wg.ALGO_4X3 else 2
+    pk, pk_kind = peaks()
+    roof = roofline_for(dominant, wg, (n, c, h, w, k, m), dom_ms, pk, pk_kind)
+    traffic = committed_traffic(dominant, args.workload)
+    roof["traffic"] = traffic
+    roof["share_of_step"] = tot[dominant] / max(1e-9, sum(tot.values()))
+    kernel_ms = {nm: sum(v) / len(v) * (len(v) / reps) for nm, v in kt.items()}
+
+    # end to end through the host-buffer entry point
+    e2e = None
+    if not args.no_e2e:
+        hin = torch.empty((n, c, h, w), dtype=torch.float16).pin_memory()
+        hin.copy_(x0.cpu())
+        hout = torch.empty((n, k, h, w), dtype=torch.float16).pin_memory()
+        e_steps = max(3, min(args.steps, 20))
+        for i in range(2):
+            ops[0].host(hin.data_ptr(), hout.data_ptr(), sptr)
+        torch.cuda.synchronize(device)
+        if dist:
+            dist.barrier()
+        t0 = time.perf_counter()
+        for i in range(e_steps):
+            ops[0].host(hin.data_ptr(), hout.data_ptr(), sptr)
+        el = time.perf_counter() - t0
+        if dist:
+            tt = torch.tensor([el], device=device)
+            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+            el = float(tt.item())
+        e2e = {"value": world * flops * e_steps / el / 1e12, "unit": "TFLOP/s", "h2d_bytes_per_step": in_bytes,
+               "d2h_bytes_per_step": out_bytes, "ms_per_step": el / e_steps * 1e3, "steps": e_steps,
+               "path": "conv2d_fp16_host (pinned host in/out, stream sync per call)"}
+
+    # CPU baseline on the host cores (rank 0 of a 1-GPU run only)
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        O = load_oracle()
+        if not os.path.exists(O.LIB_PATH):
+            O.build()
+        hx, hw = sample_host_inputs(O, args.workload, n_img=1)
+        threads = os.cpu_count() or 1
+        dt, fl, kind, used = cpu_sample(O, hx, hw, 1, threads)
+        cpu = {"value": fl / dt / 1e12, "unit": "TFLOP/s", "cores": used, "kind": kind,
+               "sample": f"1 of {n} images ({fl / 1e9:.2f} GFLOP), all {k} output channels, {dt:.2f} s"}
+
+    lat = sorted(per_step)
+    line = {
+        "metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f16", "data": "synthetic (seeded torch RNG)",
+        "config": {"workload": desc, "n": n, "c": c, "h": h, "w": w, "k": k, "pad": 1, "stride": 1,
+                   "algo": wg.ALGO_NAMES[algo], "selection": args.algo, "accumulate": "fp32",
+                   "input": f"{xdist}, filter {wdist}",
+                   "l2": f"{nsets} rotating input/output sets ({nsets * (in_bytes + out_bytes) / 2**20:.0f} MiB) > L2",
+                   "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
+        "latency_us": {"p50": lat[len(lat) // 2] * 1e3, "p99": lat[min(len(lat) - 1, int(0.99 * len(lat)))] * 1e3},
+        "kernel_ms": kernel_ms,
+        "roofline": roof,
+        "e2e": e2e,
+        "cpu_baseline": cpu,
+        "clocks": clocks,
+        "gpu_launches": args.steps * ops[0].launches_per_call,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    for op in ops:
+        op.destroy()
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="cfg2")
+    ap.add_argument("--algo", choices=sorted(ALGO_ARG), default="ref")
+    ap.add_argument("--gemm-bn", type=int, default=0)
+    ap.add_argument("--l2-chunk", type=int, default=None)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return reference_arm(args)
+    return our_arm(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,226 @@
+"""Python mirror of the operator's C ABI (include/conv2d.h), over ctypes.
+
+The operator itself is C++/CUDA in ``csrc/`` built into ``_build/libwgconv.so``;
+this module only binds that library so tests and the benchmark can call it the
+way the reference's harness does (reference ``src/main.cpp:58-105``:
+``getParamsize`` -> ``getkernelInfo`` -> ``conv2d_fp16``).  There is no
+compute here and no fallback: if the library is missing, loading fails.
+
+Device memory in the helpers comes from PyTorch tensors (plumbing only).
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libwgconv.so")
+
+# status codes and algorithms (include/conv2d.h)
+OK, ERR_INVALID, ERR_UNSUPPORTED, ERR_NOMEM, ERR_CUDA, ERR_TIMEOUT, ERR_BUSY = range(7)
+ALGO_REFERENCE, ALGO_4X3, ALGO_2X3, ALGO_2X3_FUSED, ALGO_AUTO = -1, 0, 1, 2, 3
+ALGO_NAMES = {ALGO_4X3: "F(4x3) non-fused", ALGO_2X3: "F(2x3) non-fused", ALGO_2X3_FUSED: "F(2x3) fused"}
+
+
+class Problem(ctypes.Structure):
+    """problem_t (reference include/conv2d.h:8-24)."""
+    _fields_ = [("in_", ctypes.c_void_p), ("weight", ctypes.c_void_p), ("out", ctypes.c_void_p)] + [
+        (f, ctypes.c_uint) for f in ("n", "c", "h", "w", "k", "r", "s", "u", "v", "p", "q")]
+
+
+class KernelInfo(ctypes.Structure):
+    """kernelInfo_t (reference include/conv2d.h:26-36)."""
+    _fields_ = [(f, ctypes.c_uint) for f in ("blockx", "blocky", "blockz", "threadx", "thready", "threadz",
+                                              "dynmicLdsSize")] + [("kernelPtr", ctypes.c_void_p)]
+
+
+class Options(ctypes.Structure):
+    """conv2d_options_t."""
+    _fields_ = [("algo", ctypes.c_int), ("operand_bf16", ctypes.c_int), ("tile_scaling", ctypes.c_int),
+                ("f4_points", ctypes.c_int), ("filter_policy", ctypes.c_int), ("gemm_bn", ctypes.c_int),
+                ("l2_chunk_bytes", ctypes.c_longlong), ("reserved", ctypes.c_int * 4)]
+
+
+# every symbol include/conv2d.h declares
+EXPORTS = [
+    "getParamsize", "getkernelInfo", "conv2d_fp16", "wg_getParamsize", "wg_getkernelInfo",
+    "conv2d_options_default", "getkernelInfo_ex", "conv2d_fp16_ex", "conv2d_fp16_host",
+    "conv2d_refresh_filter", "conv2d_destroy", "conv2d_get_algo", "conv2d_workspace_bytes",
+    "conv2d_launches_per_call", "conv2d_check_device", "conv2d_last_error", "conv2d_last_error_message",
+    "conv2d_status_string", "conv2d_select_reference", "conv2d_copy_to_host", "conv2d_fp16_timed",
+]
+
+_lib = None
+
+
+class Conv2dError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__(f"status {status}: {msg}")
+        self.status = status
+
+
+def build(verbose: bool = False) -> str:
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("_wg_build", os.path.join(HERE, "build.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod.build(verbose=verbose)
+
+
+def lib():
+    """The operator library.  Raises if it was not built: there is no fallback."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"operator library not built: {LIB_PATH} (run build.py)")
+        L = ctypes.CDLL(LIB_PATH)
+        vp, ip = ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)
+        L.getParamsize.argtypes = [ctypes.POINTER(Problem), ip]
+        L.getkernelInfo.argtypes = [ctypes.POINTER(Problem), ctypes.POINTER(KernelInfo), vp]
+        L.getkernelInfo_ex.argtypes = [ctypes.POINTER(Problem), ctypes.POINTER(KernelInfo), vp,
+                                       ctypes.POINTER(Options)]
+        L.conv2d_fp16.argtypes = [vp]
+        L.conv2d_fp16.restype = None
+        L.conv2d_fp16_ex.argtypes = [vp, vp]
+        L.conv2d_fp16_host.argtypes = [vp, vp, vp, vp]
+        L.conv2d_refresh_filter.argtypes = [vp, vp]
+        L.conv2d_destroy.argtypes = [vp]
+        L.conv2d_get_algo.argtypes = [vp]
+        L.conv2d_workspace_bytes.argtypes = [vp]
+        L.conv2d_workspace_bytes.restype = ctypes.c_longlong
+        L.conv2d_launches_per_call.argtypes = [vp]
+        L.conv2d_check_device.argtypes = [vp, ip]
+        L.conv2d_last_error_message.restype = ctypes.c_char_p
+        L.conv2d_status_string.restype = ctypes.c_char_p
+        L.conv2d_options_default.argtypes = [ctypes.POINTER(Options)]
+        L.conv2d_select_reference.argtypes = [ctypes.POINTER(Problem)]
+        L.conv2d_copy_to_host.argtypes = [vp, vp, ctypes.c_size_t]
+        L.conv2d_fp16_timed.argtypes = [vp, vp, ctypes.POINTER(ctypes.c_float), ctypes.c_int]
+        _lib = L
+    return _lib
+
+
+def _check(status):
+    if status != OK:
+        raise Conv2dError(status, lib().conv2d_last_error_message().decode())
+    return status
+
+
+def default_options(**kw) -> Options:
+    o = Options()
+    _check(lib().conv2d_options_default(ctypes.byref(o)))
+    for k, v in kw.items():
+        setattr(o, k, v)
+    return o
+
+
+def make_problem(x_ptr, w_ptr, y_ptr, n, c, h, w, k, p=1, q=1, r=3, s=3, u=1, v=1) -> Problem:
+    return Problem(x_ptr, w_ptr, y_ptr, n, c, h, w, k, r, s, u, v, p, q)
+
+
+class Conv2d:
+    """One configured convolution: the param blob of getkernelInfo plus its calls."""
+
+    def __init__(self, problem: Problem, options: Options | None = None):
+        L = lib()
+        self.problem = problem
+        size = ctypes.c_int(0)
+        _check(L.getParamsize(ctypes.byref(problem), ctypes.byref(size)))
+        self.param = (ctypes.c_ubyte * size.value)()
+        self.info = KernelInfo()
+        if options is None:
+            _check(L.getkernelInfo(ctypes.byref(problem), ctypes.byref(self.info), self.param))
+        else:
+            _check(L.getkernelInfo_ex(ctypes.byref(problem), ctypes.byref(self.info), self.param,
+                                      ctypes.byref(options)))
+        self._alive = True
+        opts = options if options is not None else default_options()
+        self.scaling = bool(opts.tile_scaling) and self.algo == ALGO_4X3
+
+    @property
+    def ptr(self):
+        return ctypes.cast(self.param, ctypes.c_void_p)
+
+    def __call__(self, stream: int | None = None):
+        _check(lib().conv2d_fp16_ex(self.ptr, ctypes.c_void_p(stream or 0)))
+
+    def host(self, host_in: int, host_out: int, stream: int | None = None):
+        _check(lib().conv2d_fp16_host(self.ptr, ctypes.c_void_p(host_in), ctypes.c_void_p(host_out),
+                                      ctypes.c_void_p(stream or 0)))
+
+    def timed(self, stream: int | None = None, max_kernels: int = 64):
+        """One call; per-kernel durations in ms (CUDA events on the stream)."""
+        buf = (ctypes.c_float * max_kernels)()
+        n = lib().conv2d_fp16_timed(self.ptr, ctypes.c_void_p(stream or 0), buf, max_kernels)
+        if n < 0:
+            _check(-n)
+        return list(buf[:n])
+
+    def kernel_names(self):
+        """Kernels launched by one call, in launch order."""
+        if self.algo == ALGO_2X3_FUSED:
+            return ["fused2x3"]
+        per = (["tile_scale"] if self.scaling else []) + ["input_transform", "gemm_tcgen05", "output_transform"]
+        return per * (self.launches_per_call // len(per))
+
+    def refresh_filter(self, stream: int | None = None):
+        _check(lib().conv2d_refresh_filter(self.ptr, ctypes.c_void_p(stream or 0)))
+
+    def check_device(self):
+        site = ctypes.c_int(0)
+        st = lib().conv2d_check_device(self.ptr, ctypes.byref(site))
+        return st, site.value
+
+    @property
+    def algo(self):
+        return lib().conv2d_get_algo(self.ptr)
+
+    @property
+    def workspace_bytes(self):
+        return lib().conv2d_workspace_bytes(self.ptr)
+
+    @property
+    def launches_per_call(self):
+        return lib().conv2d_launches_per_call(self.ptr)
+
+    def blob_pointers(self):
+        """(U_d, V_d, M_d) device pointers recorded in the param blob."""
+        vals = (ctypes.c_void_p * 7).from_buffer(self.param)
+        return vals[3], vals[4], vals[5]
+
+    def destroy(self):
+        if self._alive:
+            _check(lib().conv2d_destroy(self.ptr))
+            self._alive = False
+
+    def __del__(self):
+        try:
+            if self._alive and _lib is not None:
+                _lib.conv2d_destroy(self.ptr)
+        except Exception:
+            pass
+
+
+def copy_to_host(host_ptr: int, dev_ptr: int, nbytes: int):
+    _check(lib().conv2d_copy_to_host(ctypes.c_void_p(host_ptr), ctypes.c_void_p(dev_ptr), nbytes))
+
+
+# ---- torch convenience (tests / benchmark) ------------------------------------
+
+def conv2d_torch(x, w, p=1, q=1, options: Options | None = None, stream=None):
+    """Run the operator on CUDA fp16 tensors x [N,C,H,W], w [K,C,3,3]; returns
+    (output tensor, Conv2d handle)."""
+    import torch
+    assert x.is_cuda and w.is_cuda and x.dtype == torch.float16 and w.dtype == torch.float16
+    x = x.contiguous()
+    w = w.contiguous()
+    n, c, h, wd = x.shape
+    k = w.shape[0]
+    oh, ow = h + 2 * p - 2, wd + 2 * q - 2
+    y = torch.empty((n, k, oh, ow), dtype=torch.float16, device=x.device)
+    prob = make_problem(x.data_ptr(), w.data_ptr(), y.data_ptr(), n, c, h, wd, k, p, q)
+    op = Conv2d(prob, options)
+    op._keep = (x, w, y)
+    s = stream if stream is not None else torch.cuda.current_stream().cuda_stream
+    op(s)
+    return y, op

@@ -1,0 +1,501 @@
+// C ABI of the operator: descriptor -> plan -> launches.
+//
+// Mirrors the reference's operator API (include/conv2d.h:8-42,
+// src/conv2d.cpp:1-133): getParamsize returns the size of the opaque param
+// blob, getkernelInfo fills it (selection + device workspace, as
+// src/conv2d.cpp:66-157 does), conv2d_fp16 runs the selected algorithm
+// (src/conv2d.cpp:160-175).  Differences, each deliberate:
+//   * sizes are computed in 64-bit arithmetic (the reference's unsigned 32-bit
+//     products overflow for large batches);
+//   * no file-static state is mutated (the reference rewrites its tile
+//     constants on the F(2x3)-non-fused branch, src/conv2d.cpp:131-134);
+//   * unsupported descriptors return a status code;
+//   * the filter transform runs once per weight set (first call) instead of
+//     on every call, and the workspace can be released (conv2d_destroy).
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+
+#include "../../include/conv2d.h"
+#include "wg_kernels.h"
+#include "wg_plan.h"
+
+namespace wg {
+
+namespace {
+
+thread_local int t_last_status = CONV2D_OK;
+thread_local std::string t_last_msg;
+
+int fail(int status, const std::string& msg) {
+    t_last_status = status;
+    t_last_msg = msg;
+    return status;
+}
+
+int cuda_fail(cudaError_t e, const char* what) {
+    return fail(CONV2D_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+int env_int(const char* name, int dflt) {
+    const char* v = std::getenv(name);
+    if (!v || !*v) return dflt;
+    return std::atoi(v);
+}
+
+int env_algo(int dflt) {
+    const char* v = std::getenv("WG_CONV2D_ALGO");
+    if (!v || !*v) return dflt;
+    std::string s(v);
+    if (s == "ref" || s == "reference") return CONV2D_ALGO_REFERENCE;
+    if (s == "4x3") return CONV2D_ALGO_4X3_NON_FUSED;
+    if (s == "2x3") return CONV2D_ALGO_2X3_NON_FUSED;
+    if (s == "fused" || s == "2x3_fused") return CONV2D_ALGO_2X3_FUSED;
+    if (s == "auto") return CONV2D_ALGO_AUTO;
+    return dflt;
+}
+
+}  // namespace
+
+int select_reference64(unsigned long long n, unsigned long long c, unsigned long long h, unsigned long long w,
+                       unsigned long long k, unsigned long long r, unsigned long long s, unsigned long long oh,
+                       unsigned long long ow) {
+    // src/conv2d.cpp:118-156 with the tile constants of a first call:
+    // fused F(2x3) when the image is at least 10x the filter, F(2x3)
+    // non-fused when the F(4x3) filter workspace exceeds 4x the input one,
+    // else F(4x3).
+    const unsigned long long image = n * c * h * w;
+    const unsigned long long filter = k * c * r * s;
+    const unsigned long long tiles4 = n * ((oh + 3) / 4) * ((ow + 3) / 4);
+    const unsigned long long U = 36ull * k * c;
+    const unsigned long long V = 36ull * tiles4 * c;
+    if (image >= 10ull * filter) return CONV2D_ALGO_2X3_FUSED;
+    if (U > 4ull * V) return CONV2D_ALGO_2X3_NON_FUSED;
+    return CONV2D_ALGO_4X3_NON_FUSED;
+}
+
+int validate_problem(const problem_t* pr) {
+    if (!pr) return fail(CONV2D_ERR_INVALID, "null problem");
+    if (!pr->in || !pr->weight || !pr->out) return fail(CONV2D_ERR_INVALID, "null tensor pointer");
+    if (!pr->n || !pr->c || !pr->h || !pr->w || !pr->k) return fail(CONV2D_ERR_INVALID, "zero dimension");
+    if (pr->r != 3 || pr->s != 3) return fail(CONV2D_ERR_UNSUPPORTED, "only 3x3 filters are supported");
+    if (pr->u != 1 || pr->v != 1) return fail(CONV2D_ERR_UNSUPPORTED, "only stride 1 is supported");
+    if (pr->p > 64 || pr->q > 64) return fail(CONV2D_ERR_UNSUPPORTED, "padding above 64");
+    const long long oh = static_cast<long long>(pr->h) + 2LL * pr->p - 2;
+    const long long ow = static_cast<long long>(pr->w) + 2LL * pr->q - 2;
+    if (oh <= 0 || ow <= 0) return fail(CONV2D_ERR_INVALID, "empty output");
+    if (pr->c > 65535 || pr->k > 65535 || pr->h > 65535 || pr->w > 65535)
+        return fail(CONV2D_ERR_UNSUPPORTED, "dimension above 65535");
+    const long long tiles = static_cast<long long>(pr->n) * ((oh + 1) / 2) * ((ow + 1) / 2);
+    if (tiles > 0x7fffffffLL) return fail(CONV2D_ERR_UNSUPPORTED, "more than 2^31 tiles");
+    return CONV2D_OK;
+}
+
+int options_default(conv2d_options_t* o) {
+    std::memset(o, 0, sizeof(*o));
+    o->algo = env_algo(CONV2D_ALGO_REFERENCE);
+    o->operand_bf16 = env_int("WG_CONV2D_BF16", 0) ? 1 : 0;
+    o->tile_scaling = env_int("WG_CONV2D_TILE_SCALING", 0) ? 1 : 0;
+    o->f4_points = env_int("WG_CONV2D_F4_REFERENCE_POINTS", 0) ? 1 : 0;
+    o->filter_policy = env_int("WG_CONV2D_FILTER_EVERY_CALL", 0) ? 1 : 0;
+    o->gemm_bn = env_int("WG_CONV2D_GEMM_BN", 0);
+    const char* l2 = std::getenv("WG_CONV2D_L2_CHUNK_BYTES");
+    o->l2_chunk_bytes = (l2 && *l2) ? std::atoll(l2) : 0;
+    return CONV2D_OK;
+}
+
+int default_bn(int K) {
+    if (K <= 32) return 32;
+    if (K <= 64) return 64;
+    if (K <= 128) return 128;
+    // prefer the tile with the least padding waste; ties go to the wider tile
+    const int w256 = ((K + 255) / 256) * 256 - K;
+    const int w128 = ((K + 127) / 128) * 128 - K;
+    return w256 <= w128 ? 256 : 128;
+}
+
+Plan::~Plan() { release(); }
+
+void Plan::release() {
+    if (ws) cudaFree(ws);
+    ws = nullptr;
+    U = V = Mw = nullptr;
+    scale = nullptr;
+    err = nullptr;
+}
+
+int Plan::build(const problem_t* pr, const conv2d_options_t* opt_in) {
+    int st = validate_problem(pr);
+    if (st) return st;
+    prob = *pr;
+    if (opt_in)
+        opt = *opt_in;
+    else
+        options_default(&opt);
+    if (cudaGetDevice(&device) != cudaSuccess) return fail(CONV2D_ERR_CUDA, "no CUDA device");
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    num_sms = sms > 0 ? sms : 1;
+
+    const unsigned oh = pr->h + 2 * pr->p - 2, ow = pr->w + 2 * pr->q - 2;
+    algo = opt.algo;
+    if (algo == CONV2D_ALGO_REFERENCE || algo == CONV2D_ALGO_AUTO)
+        algo = select_reference64(pr->n, pr->c, pr->h, pr->w, pr->k, pr->r, pr->s, oh, ow);
+    if (opt.algo == CONV2D_ALGO_AUTO) algo = autotune_pick(*pr, opt, algo);
+    if (algo < 0 || algo > 2) return fail(CONV2D_ERR_INVALID, "bad algorithm");
+
+    op = opt.operand_bf16 ? OpType::BF16 : OpType::F16;
+    const int m = algo == CONV2D_ALGO_4X3_NON_FUSED ? 4 : 2;
+    xf = m == 2 ? Xform::F2 : (opt.f4_points ? Xform::F4Ref : Xform::F4);
+    m_fp32 = (m == 4);
+    scaling = (m == 4) && opt.tile_scaling;
+    g = make_geom(pr->n, pr->c, pr->h, pr->w, pr->k, pr->p, pr->q, m);
+    const int E = g.alpha * g.alpha;
+    const long long op_bytes = 2;
+
+    // image chunking keeps V and M of one chunk L2-resident between kernels
+    chunk_n = static_cast<int>(pr->n);
+    if (algo != CONV2D_ALGO_2X3_FUSED && opt.l2_chunk_bytes > 0) {
+        const long long per_img = static_cast<long long>(E) * g.tiles_h * g.tiles_w *
+                                  (g.cp * op_bytes + g.kp * (m_fp32 ? 4LL : 2LL));
+        chunk_n = static_cast<int>(std::max(1LL, std::min<long long>(pr->n, opt.l2_chunk_bytes / std::max(1LL, per_img))));
+    }
+    const long long Pc = static_cast<long long>(chunk_n) * g.tiles_h * g.tiles_w;
+
+    // one workspace: U | V | M | scale | device error word (256-byte aligned parts)
+    auto al = [](long long b) { return (b + 255) / 256 * 256; };
+    const long long bU = al(static_cast<long long>(E) * g.k * g.cp * op_bytes);
+    long long bV = 0, bM = 0, bS = 0;
+    if (algo != CONV2D_ALGO_2X3_FUSED) {
+        bV = al(static_cast<long long>(E) * Pc * g.cp * op_bytes);
+        bM = al(static_cast<long long>(E) * Pc * g.kp * (m_fp32 ? 4 : 2));
+        if (scaling) bS = al(Pc * 4);
+    }
+    const long long bE = 256;
+    ws_bytes = bU + bV + bM + bS + bE;
+    cudaError_t ce = cudaMalloc(&ws, static_cast<size_t>(ws_bytes));
+    if (ce != cudaSuccess) {
+        ws = nullptr;
+        cudaGetLastError();
+        return fail(CONV2D_ERR_NOMEM, "workspace cudaMalloc failed");
+    }
+    char* b = static_cast<char*>(ws);
+    U = b;
+    V = bV ? b + bU : nullptr;
+    Mw = bM ? b + bU + bV : nullptr;
+    scale = bS ? reinterpret_cast<float*>(b + bU + bV + bM) : nullptr;
+    err = reinterpret_cast<DevErr*>(b + bU + bV + bM + bS);
+    ce = cudaMemset(err, 0, sizeof(DevErr));
+    if (ce != cudaSuccess) return cuda_fail(ce, "cudaMemset");
+
+    if (algo == CONV2D_ALGO_2X3_FUSED) {
+        ce = plan_fused2x3(fused, op, g, U);
+        if (ce != cudaSuccess) return cuda_fail(ce, "fused plan");
+        launches = 1;
+        info_grid = static_cast<unsigned>(fused.m_blocks * fused.n_blocks);
+        info_threads = 288;
+        info_smem = fused.smem_bytes;
+    } else {
+        const int bn = opt.gemm_bn ? opt.gemm_bn : default_bn(g.k);
+        ce = plan_gemm(gemm_full, op, E, Pc, g.k, g.kp, g.cp, V, U, m_fp32, bn, num_sms);
+        if (ce != cudaSuccess) return cuda_fail(ce, "GEMM plan (tensor maps)");
+        n_chunks = (static_cast<int>(pr->n) + chunk_n - 1) / chunk_n;
+        const int tail_n = static_cast<int>(pr->n) - (n_chunks - 1) * chunk_n;
+        has_tail = tail_n != chunk_n;
+        if (has_tail) {
+            const long long Pt = static_cast<long long>(tail_n) * g.tiles_h * g.tiles_w;
+            ce = plan_gemm(gemm_tail, op, E, Pt, g.k, g.kp, g.cp, V, U, m_fp32, bn, num_sms);
+            if (ce != cudaSuccess) return cuda_fail(ce, "GEMM plan (tail)");
+        }
+        launches = n_chunks * (3 + (scaling ? 1 : 0));
+        info_grid = static_cast<unsigned>(gemm_full.grid);
+        info_threads = 192;
+        info_smem = gemm_full.smem_bytes;
+    }
+    filter_ready = false;
+    return CONV2D_OK;
+}
+
+int Plan::filter(cudaStream_t s) {
+    cudaError_t ce = launch_filter_transform(xf, op, prob.weight, U, g.k, g.c, g.cp, s);
+    if (ce != cudaSuccess) return cuda_fail(ce, "filter transform launch");
+    filter_ready = true;
+    return CONV2D_OK;
+}
+
+void Plan::mark(cudaStream_t s) {
+    if (marks && n_marks < max_marks) cudaEventRecord(marks[n_marks++], s);
+}
+
+int Plan::run(cudaStream_t s) {
+    int cur = -1;
+    if (cudaGetDevice(&cur) == cudaSuccess && cur != device) cudaSetDevice(device);
+    if (!filter_ready || opt.filter_policy == 1) {
+        int st = filter(s);
+        if (st) return st;
+    }
+    cudaError_t ce;
+    if (algo == CONV2D_ALGO_2X3_FUSED) {
+        ce = launch_fused2x3(fused, g, prob.in, prob.out, err, s);
+        if (ce != cudaSuccess) return cuda_fail(ce, "fused F(2x3) launch");
+        mark(s);
+        return CONV2D_OK;
+    }
+    const long long in_img = static_cast<long long>(g.c) * g.h * g.w;
+    const long long out_img = static_cast<long long>(g.k) * g.oh * g.ow;
+    for (int ci = 0; ci < n_chunks; ++ci) {
+        const int n0 = ci * chunk_n;
+        const int nc = std::min<int>(chunk_n, static_cast<int>(prob.n) - n0);
+        Geom gc = make_geom(nc, g.c, g.h, g.w, g.k, g.pad_h, g.pad_w, g.m);
+        const uint16_t* xin = static_cast<const uint16_t*>(prob.in) + n0 * in_img;
+        uint16_t* yout = static_cast<uint16_t*>(prob.out) + n0 * out_img;
+        if (scaling) {
+            ce = launch_tile_scale(gc, xin, scale, s);
+            if (ce != cudaSuccess) return cuda_fail(ce, "tile scale launch");
+            mark(s);
+        }
+        ce = launch_input_transform(xf, op, gc, xin, V, scale, s);
+        if (ce != cudaSuccess) return cuda_fail(ce, "input transform launch");
+        mark(s);
+        const GemmPlan& gp = (has_tail && ci == n_chunks - 1) ? gemm_tail : gemm_full;
+        ce = launch_gemm(gp, Mw, err, s);
+        if (ce != cudaSuccess) return cuda_fail(ce, "GEMM launch");
+        mark(s);
+        ce = launch_output_transform(xf, m_fp32, gc, Mw, yout, scale, s);
+        if (ce != cudaSuccess) return cuda_fail(ce, "output transform launch");
+        mark(s);
+    }
+    return CONV2D_OK;
+}
+
+Plan* plan_of(const void* param) {
+    if (!param) return nullptr;
+    const ParamBlob* pb = static_cast<const ParamBlob*>(param);
+    if (pb->magic != kParamMagic || !pb->plan) return nullptr;
+    return static_cast<Plan*>(pb->plan);
+}
+
+void fill_blob(ParamBlob* pb, Plan* pl) {
+    const problem_t& pr = pl->prob;
+    pb->pin = pr.in;
+    pb->pweight = pr.weight;
+    pb->pout = pr.out;
+    pb->U_d = pl->U;
+    pb->V_d = pl->V;
+    pb->M_d = pl->Mw;
+    pb->Y_d = nullptr;
+    pb->n = pr.n; pb->c = pr.c; pb->h = pr.h; pb->w = pr.w; pb->k = pr.k;
+    pb->r = pr.r; pb->s = pr.s; pb->u = pr.u; pb->v = pr.v; pb->p = pr.p; pb->q = pr.q;
+    pb->Oh = static_cast<unsigned>(pl->g.oh);
+    pb->Ow = static_cast<unsigned>(pl->g.ow);
+    pb->kernel = pl->algo;
+    pb->magic = kParamMagic;
+    pb->plan = pl;
+}
+
+}  // namespace wg
+
+using namespace wg;
+
+extern "C" {
+
+int wg_getParamsize(problem_t* problem, int* paramSize) {
+    (void)problem;
+    if (!paramSize) return fail(CONV2D_ERR_INVALID, "null paramSize");
+    *paramSize = static_cast<int>(sizeof(ParamBlob));
+    return CONV2D_OK;
+}
+
+int getParamsize(problem_t* problem, int* paramSize) { return wg_getParamsize(problem, paramSize); }
+
+int conv2d_options_default(conv2d_options_t* opt) {
+    if (!opt) return fail(CONV2D_ERR_INVALID, "null options");
+    return options_default(opt);
+}
+
+int getkernelInfo_ex(problem_t* problem, kernelInfo_t* kernelInfo, void* param, const conv2d_options_t* opt) {
+    if (!param) return fail(CONV2D_ERR_INVALID, "null param");
+    ParamBlob* pb = static_cast<ParamBlob*>(param);
+    std::memset(pb, 0, sizeof(*pb));
+    Plan* pl = new Plan();
+    int st = pl->build(problem, opt);
+    if (st) {
+        delete pl;
+        return st;
+    }
+    fill_blob(pb, pl);
+    if (kernelInfo) {
+        kernelInfo->blockx = pl->info_grid;
+        kernelInfo->blocky = 1;
+        kernelInfo->blockz = 1;
+        kernelInfo->threadx = pl->info_threads;
+        kernelInfo->thready = 1;
+        kernelInfo->threadz = 1;
+        kernelInfo->dynmicLdsSize = static_cast<unsigned>(pl->info_smem);
+        kernelInfo->kernelPtr = nullptr;
+    }
+    return CONV2D_OK;
+}
+
+int wg_getkernelInfo(problem_t* problem, kernelInfo_t* kernelInfo, void* param) {
+    return getkernelInfo_ex(problem, kernelInfo, param, nullptr);
+}
+
+int getkernelInfo(problem_t* problem, kernelInfo_t* kernelInfo, void* param) {
+    return wg_getkernelInfo(problem, kernelInfo, param);
+}
+
+int conv2d_fp16_ex(const void* param_ptr, void* stream) {
+    Plan* pl = plan_of(param_ptr);
+    if (!pl) return fail(CONV2D_ERR_INVALID, "param blob not set up by getkernelInfo");
+    return pl->run(static_cast<cudaStream_t>(stream));
+}
+
+// Same behaviour as the reference on a failed launch (include/error.h:18-27):
+// message on stderr and process exit.
+void conv2d_fp16(const void* param_ptr) {
+    const int st = conv2d_fp16_ex(param_ptr, nullptr);
+    if (st == CONV2D_ERR_INVALID) {
+        std::fprintf(stderr, "conv2d_fp16: %s\n", t_last_msg.c_str());
+        return;
+    }
+    if (st != CONV2D_OK) {
+        std::fprintf(stderr, "Kernel panic!!!: %s\n", t_last_msg.c_str());
+        std::exit(-1);
+    }
+}
+
+int conv2d_fp16_host(const void* param_ptr, const void* host_in, void* host_out, void* stream) {
+    Plan* pl = plan_of(param_ptr);
+    if (!pl) return fail(CONV2D_ERR_INVALID, "param blob not set up by getkernelInfo");
+    if (!host_in || !host_out) return fail(CONV2D_ERR_INVALID, "null host buffer");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const size_t in_bytes = static_cast<size_t>(pl->prob.n) * pl->g.c * pl->g.h * pl->g.w * 2;
+    const size_t out_bytes = static_cast<size_t>(pl->prob.n) * pl->g.k * pl->g.oh * pl->g.ow * 2;
+    cudaError_t ce = cudaMemcpyAsync(pl->prob.in, host_in, in_bytes, cudaMemcpyHostToDevice, s);
+    if (ce != cudaSuccess) return cuda_fail(ce, "input copy");
+    int st = pl->run(s);
+    if (st) return st;
+    ce = cudaMemcpyAsync(host_out, pl->prob.out, out_bytes, cudaMemcpyDeviceToHost, s);
+    if (ce != cudaSuccess) return cuda_fail(ce, "output copy");
+    ce = cudaStreamSynchronize(s);
+    if (ce != cudaSuccess) return cuda_fail(ce, "stream sync");
+    return CONV2D_OK;
+}
+
+int conv2d_refresh_filter(const void* param_ptr, void* stream) {
+    Plan* pl = plan_of(param_ptr);
+    if (!pl) return fail(CONV2D_ERR_INVALID, "param blob not set up by getkernelInfo");
+    return pl->filter(static_cast<cudaStream_t>(stream));
+}
+
+int conv2d_destroy(void* param_ptr) {
+    Plan* pl = plan_of(param_ptr);
+    if (!pl) return fail(CONV2D_ERR_INVALID, "param blob not set up by getkernelInfo");
+    cudaDeviceSynchronize();
+    delete pl;
+    std::memset(param_ptr, 0, sizeof(ParamBlob));
+    return CONV2D_OK;
+}
+
+int conv2d_get_algo(const void* param_ptr) {
+    Plan* pl = plan_of(param_ptr);
+    return pl ? pl->algo : -1;
+}
+
+long long conv2d_workspace_bytes(const void* param_ptr) {
+    Plan* pl = plan_of(param_ptr);
+    return pl ? pl->ws_bytes : -1;
+}
+
+int conv2d_launches_per_call(const void* param_ptr) {
+    Plan* pl = plan_of(param_ptr);
+    return pl ? pl->launches : -1;
+}
+
+int conv2d_check_device(const void* param_ptr, int* site) {
+    Plan* pl = plan_of(param_ptr);
+    if (!pl) return fail(CONV2D_ERR_INVALID, "param blob not set up by getkernelInfo");
+    cudaError_t ce = cudaDeviceSynchronize();
+    if (ce != cudaSuccess) return cuda_fail(ce, "device synchronize");
+    DevErr h{};
+    ce = cudaMemcpy(&h, pl->err, sizeof(h), cudaMemcpyDeviceToHost);
+    if (ce != cudaSuccess) return cuda_fail(ce, "error word copy");
+    if (site) *site = static_cast<int>(h.code);
+    if (h.code) {
+        cudaMemset(pl->err, 0, sizeof(DevErr));
+        return fail(CONV2D_ERR_TIMEOUT, "a kernel gave up a bounded wait");
+    }
+    return CONV2D_OK;
+}
+
+int conv2d_last_error(void) { return t_last_status; }
+
+const char* conv2d_last_error_message(void) { return t_last_msg.c_str(); }
+
+const char* conv2d_status_string(int status) {
+    switch (status) {
+        case CONV2D_OK: return "ok";
+        case CONV2D_ERR_INVALID: return "invalid argument";
+        case CONV2D_ERR_UNSUPPORTED: return "unsupported descriptor";
+        case CONV2D_ERR_NOMEM: return "out of device memory";
+        case CONV2D_ERR_CUDA: return "CUDA error";
+        case CONV2D_ERR_TIMEOUT: return "device wait timed out";
+        case CONV2D_ERR_BUSY: return "busy";
+    }
+    return "unknown status";
+}
+
+int conv2d_select_reference(const problem_t* pr) {
+    if (!pr) return -1;
+    const unsigned long long oh = pr->h + 2ull * pr->p - pr->r + 1;
+    const unsigned long long ow = pr->w + 2ull * pr->q - pr->s + 1;
+    return select_reference64(pr->n, pr->c, pr->h, pr->w, pr->k, pr->r, pr->s, oh, ow);
+}
+
+int conv2d_fp16_timed(const void* param_ptr, void* stream, float* kernel_ms, int max_kernels) {
+    Plan* pl = plan_of(param_ptr);
+    if (!pl) return fail(CONV2D_ERR_INVALID, "param blob not set up by getkernelInfo");
+    if (!kernel_ms || max_kernels <= 0) return fail(CONV2D_ERR_INVALID, "null output array");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    if (!pl->filter_ready) {
+        int st = pl->filter(s);
+        if (st) return -st;
+    }
+    const int n = std::min(max_kernels, pl->launches) + 1;
+    cudaEvent_t ev[64];
+    const int ne = std::min(n, 64);
+    for (int i = 0; i < ne; ++i) cudaEventCreate(&ev[i]);
+    cudaEventRecord(ev[0], s);
+    pl->marks = ev + 1;
+    pl->n_marks = 0;
+    pl->max_marks = ne - 1;
+    int st = pl->run(s);
+    const int got = pl->n_marks;
+    pl->marks = nullptr;
+    pl->n_marks = pl->max_marks = 0;
+    cudaError_t ce = cudaStreamSynchronize(s);
+    for (int i = 0; i < got; ++i) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, ev[i], ev[i + 1]);
+        kernel_ms[i] = ms;
+    }
+    for (int i = 0; i < ne; ++i) cudaEventDestroy(ev[i]);
+    if (st) return -st;
+    if (ce != cudaSuccess) return -cuda_fail(ce, "stream sync");
+    return got;
+}
+
+int conv2d_copy_to_host(void* host_dst, const void* device_src, size_t bytes) {
+    if (!host_dst || !device_src) return fail(CONV2D_ERR_INVALID, "null pointer");
+    cudaError_t ce = cudaMemcpy(host_dst, device_src, bytes, cudaMemcpyDeviceToHost);
+    if (ce != cudaSuccess) return cuda_fail(ce, "cudaMemcpy");
+    return CONV2D_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,327 @@
+// Winograd-domain batched GEMM on the 5th-generation tensor cores.
+//
+// For every Winograd element e (16 for F(2x3), 36 for F(4x3)):
+//     M_e[P][K] = V_e[P][Cp] * U_e[K][Cp]^T      (fp32 accumulation)
+// which is the reference's hep_sgemm call (src/winograd_2x3_non_fused.cpp:403-413,
+// src/winograd_4x3_non_fused.cpp:587-597; kernels in include/hep_sgemm.h) with
+// the operands stored K-major.
+//
+// Design (one persistent CTA per SM, 192 threads):
+//   warp 0      TMA producer: 128x64 V tile + BNx64 U tile per stage
+//               (128-byte swizzle), S-stage mbarrier ring;
+//   warp 1      allocates TMEM and issues tcgen05.mma (M=128, N=BN, K=16)
+//               from one thread; accumulators double-buffered in TMEM so the
+//               epilogue of one output tile overlaps the main loop of the next;
+//   warps 2-5   epilogue: tcgen05.ld 32 lanes x 16 columns, convert, 16-byte
+//               stores of M rows (fp16 or fp32).
+// Output tiles are (e, 128-tile block, BN-channel block), handed out round
+// robin; channel blocks of one (e, tile block) are adjacent so the V tile is
+// reused from L2.
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+#include <cudaTypedefs.h>
+
+#include <algorithm>
+
+#include "wg_kernels.h"
+#include "wg_ptx.cuh"
+
+namespace wg {
+
+namespace {
+
+constexpr int kBM = 128;
+constexpr int kBK = 64;                 // 64 fp16 = one 128-byte swizzle row
+constexpr int kTileABytes = kBM * kBK * 2;
+
+template <int BN>
+struct GemmCfg {
+    static constexpr int kTileB = BN * kBK * 2;
+    static constexpr int kStageBytes = kTileABytes + kTileB;
+    static constexpr int kStages = std::min(8, (200 * 1024) / kStageBytes);
+    static constexpr int kTmemCols = (2 * BN < 32) ? 32 : 2 * BN;  // two accumulators
+    static constexpr int kSmem = kStages * kStageBytes + 1024 /*align*/ + 256 /*barriers*/;
+};
+
+template <class MT>
+__device__ __forceinline__ void store16(MT* dst, const uint32_t (&r)[16], int valid8);
+
+// fp16 M: 16 values = two 16-byte stores; `valid8` = number of 8-wide groups inside Kp.
+template <>
+__device__ __forceinline__ void store16<__half>(__half* dst, const uint32_t (&r)[16], int valid8) {
+    uint32_t h[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+        __half2 v = __floats2half2_rn(__uint_as_float(r[2 * i]), __uint_as_float(r[2 * i + 1]));
+        h[i] = *reinterpret_cast<uint32_t*>(&v);
+    }
+    if (valid8 > 0) *reinterpret_cast<uint4*>(dst) = make_uint4(h[0], h[1], h[2], h[3]);
+    if (valid8 > 1) *reinterpret_cast<uint4*>(dst + 8) = make_uint4(h[4], h[5], h[6], h[7]);
+}
+
+template <>
+__device__ __forceinline__ void store16<float>(float* dst, const uint32_t (&r)[16], int valid8) {
+    if (valid8 > 0) {
+        *reinterpret_cast<uint4*>(dst) = make_uint4(r[0], r[1], r[2], r[3]);
+        *reinterpret_cast<uint4*>(dst + 4) = make_uint4(r[4], r[5], r[6], r[7]);
+    }
+    if (valid8 > 1) {
+        *reinterpret_cast<uint4*>(dst + 8) = make_uint4(r[8], r[9], r[10], r[11]);
+        *reinterpret_cast<uint4*>(dst + 12) = make_uint4(r[12], r[13], r[14], r[15]);
+    }
+}
+
+template <int BN, bool BF16, class MT>
+__global__ void __launch_bounds__(192, 1)
+    wino_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+                     MT* __restrict__ Mw, int P, int Kp, int m_blocks, int n_blocks, int k_blocks, int total_tiles,
+                     DevErr* err) {
+    using Cfg = GemmCfg<BN>;
+    constexpr int S = Cfg::kStages;
+    constexpr uint32_t kIdesc = make_idesc_f16(kBM, BN, BF16);
+
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    // 1024-byte alignment for the 128-byte swizzle atoms
+    unsigned char* smem = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    unsigned char* sA = smem;
+    unsigned char* sB = smem + S * kTileABytes;
+    uint64_t* bars = reinterpret_cast<uint64_t*>(smem + S * Cfg::kStageBytes);
+    uint64_t* full = bars;
+    uint64_t* empty = bars + S;
+    uint64_t* tfull = bars + 2 * S;
+    uint64_t* tempty = bars + 2 * S + 2;
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * S + 4);
+    volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < S; ++i) {
+            mbar_init(&full[i], 1);
+            mbar_init(&empty[i], 1);
+        }
+        for (int i = 0; i < 2; ++i) {
+            mbar_init(&tfull[i], 1);
+            mbar_init(&tempty[i], 128);
+        }
+        *abort_flag = 0;
+        fence_barrier_init();
+        tma_prefetch_desc(&tmA);
+        tma_prefetch_desc(&tmB);
+    }
+    if (warp == 1) tmem_alloc(tmem_slot, Cfg::kTmemCols);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem_base = *tmem_slot;
+
+    if (warp == 0) {
+        if (lane == 0) {
+            int stage = 0;
+            uint32_t phase = 0;
+            for (int t = blockIdx.x; t < total_tiles; t += gridDim.x) {
+                const int nb = t % n_blocks;
+                const int rest = t / n_blocks;
+                const int mb = rest % m_blocks;
+                const int e = rest / m_blocks;
+                bool ok = true;
+                for (int kb = 0; kb < k_blocks; ++kb) {
+                    if (!mbar_wait(&empty[stage], phase ^ 1u, abort_flag, err, ERR_SITE_EMPTY)) {
+                        ok = false;
+                        break;
+                    }
+                    mbar_arrive_expect_tx(&full[stage], Cfg::kStageBytes);
+                    tma_load_3d(sA + stage * kTileABytes, &tmA, &full[stage], kb * kBK, mb * kBM, e);
+                    tma_load_3d(sB + stage * Cfg::kTileB, &tmB, &full[stage], kb * kBK, nb * BN, e);
+                    if (++stage == S) {
+                        stage = 0;
+                        phase ^= 1u;
+                    }
+                }
+                if (!ok) break;
+            }
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {
+            int stage = 0;
+            uint32_t phase = 0;
+            int acc = 0;
+            uint32_t acc_phase = 0;
+            for (int t = blockIdx.x; t < total_tiles; t += gridDim.x) {
+                if (!mbar_wait(&tempty[acc], acc_phase ^ 1u, abort_flag, err, ERR_SITE_TMEM_EMPTY)) break;
+                tc_fence_after();
+                const uint32_t d_tmem = tmem_base + static_cast<uint32_t>(acc * BN);
+                bool ok = true;
+                for (int kb = 0; kb < k_blocks; ++kb) {
+                    if (!mbar_wait(&full[stage], phase, abort_flag, err, ERR_SITE_FULL)) {
+                        ok = false;
+                        break;
+                    }
+                    tc_fence_after();
+                    const uint32_t a_base = smem_u32(sA + stage * kTileABytes);
+                    const uint32_t b_base = smem_u32(sB + stage * Cfg::kTileB);
+#pragma unroll
+                    for (int k = 0; k < kBK / 16; ++k) {
+                        const uint64_t ad = make_smem_desc(a_base + k * 32, 16, 1024, Swz::B128);
+                        const uint64_t bd = make_smem_desc(b_base + k * 32, 16, 1024, Swz::B128);
+                        tc_mma_f16(d_tmem, ad, bd, kIdesc, (kb | k) != 0 ? 1u : 0u);
+                    }
+                    tc_commit(&empty[stage]);
+                    if (++stage == S) {
+                        stage = 0;
+                        phase ^= 1u;
+                    }
+                }
+                if (!ok) break;
+                tc_commit(&tfull[acc]);
+                if (++acc == 2) {
+                    acc = 0;
+                    acc_phase ^= 1u;
+                }
+            }
+        }
+    } else {
+        // epilogue warps 2..5: TMEM lane quarter = warp % 4
+        const int quarter = warp & 3;
+        const int row = quarter * 32 + lane;
+        int acc = 0;
+        uint32_t acc_phase = 0;
+        for (int t = blockIdx.x; t < total_tiles; t += gridDim.x) {
+            const int nb = t % n_blocks;
+            const int rest = t / n_blocks;
+            const int mb = rest % m_blocks;
+            const int e = rest / m_blocks;
+            if (!mbar_wait(&tfull[acc], acc_phase, abort_flag, err, ERR_SITE_TMEM_FULL)) break;
+            tc_fence_after();
+            const int p = mb * kBM + row;
+            MT* dst_row = Mw + (static_cast<long long>(e) * P + p) * Kp;
+            const uint32_t taddr = tmem_base + (static_cast<uint32_t>(quarter * 32) << 16) + static_cast<uint32_t>(acc * BN);
+#pragma unroll 1
+            for (int c0 = 0; c0 < BN; c0 += 16) {
+                uint32_t r[16];
+                tmem_ld_x16(taddr + c0, r);
+                tc_wait_ld();
+                const int k0 = nb * BN + c0;
+                if (p < P && k0 < Kp) {
+                    const int valid8 = (Kp - k0) >= 16 ? 2 : 1;
+                    store16<MT>(dst_row + k0, r, valid8);
+                }
+            }
+            tc_fence_before();
+            mbar_arrive(&tempty[acc]);
+            if (++acc == 2) {
+                acc = 0;
+                acc_phase ^= 1u;
+            }
+        }
+    }
+
+    __syncthreads();
+    if (*abort_flag) {
+        // let any copy or MMA still in flight land before the CTA retires
+        const unsigned long long t0 = globaltimer_ns();
+        while (globaltimer_ns() - t0 < 2000000ull) {
+        }
+    }
+    if (warp == 1) {
+        tc_fence_after();
+        tmem_dealloc(tmem_base, Cfg::kTmemCols);
+    }
+}
+
+template <int BN, bool BF16, class MT>
+cudaError_t gemm_launch(const GemmPlan& gp, void* Mw, DevErr* err, cudaStream_t s) {
+    auto kern = wino_gemm_kernel<BN, BF16, MT>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, GemmCfg<BN>::kSmem);
+    if (e != cudaSuccess) return e;
+    const int total = gp.E * gp.m_blocks * gp.n_blocks;
+    kern<<<gp.grid, 192, GemmCfg<BN>::kSmem, s>>>(gp.tmA, gp.tmB, static_cast<MT*>(Mw), gp.P, gp.Kp, gp.m_blocks,
+                                                  gp.n_blocks, gp.k_blocks, total, err);
+    return cudaGetLastError();
+}
+
+template <int BN>
+cudaError_t gemm_dispatch_bn(const GemmPlan& gp, void* Mw, DevErr* err, cudaStream_t s) {
+    const bool bf = gp.op == OpType::BF16;
+    if (gp.m_fp32)
+        return bf ? gemm_launch<BN, true, float>(gp, Mw, err, s) : gemm_launch<BN, false, float>(gp, Mw, err, s);
+    return bf ? gemm_launch<BN, true, __half>(gp, Mw, err, s) : gemm_launch<BN, false, __half>(gp, Mw, err, s);
+}
+
+}  // namespace
+
+CUresult encode_tiled(CUtensorMap* map, CUtensorMapDataType dt, cuuint32_t rank, void* addr, const cuuint64_t* dims,
+                      const cuuint64_t* strides_bytes, const cuuint32_t* box, CUtensorMapSwizzle swz) {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    if (!fn) {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess || !p)
+            return CUDA_ERROR_NOT_FOUND;
+        fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    }
+    cuuint32_t elem_strides[5] = {1, 1, 1, 1, 1};
+    return fn(map, dt, rank, addr, dims, strides_bytes, box, elem_strides, CU_TENSOR_MAP_INTERLEAVE_NONE, swz,
+              CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+}
+
+static int gemm_smem(int bn) {
+    switch (bn) {
+        case 32: return GemmCfg<32>::kSmem;
+        case 64: return GemmCfg<64>::kSmem;
+        case 128: return GemmCfg<128>::kSmem;
+        default: return GemmCfg<256>::kSmem;
+    }
+}
+
+cudaError_t plan_gemm(GemmPlan& gp, OpType op, int E, long long P, int K, int Kp, int Cp, const void* V,
+                      const void* U, bool m_fp32, int bn, int num_sms) {
+    if (bn != 32 && bn != 64 && bn != 128 && bn != 256) return cudaErrorInvalidValue;
+    if (P <= 0 || P > 0x7fffffffLL || Cp % 8 != 0 || Kp % 8 != 0) return cudaErrorInvalidValue;
+    gp.op = op;
+    gp.bn = bn;
+    gp.E = E;
+    gp.P = static_cast<int>(P);
+    gp.K = K;
+    gp.Kp = Kp;
+    gp.Cp = Cp;
+    gp.m_fp32 = m_fp32;
+    gp.m_blocks = static_cast<int>((P + kBM - 1) / kBM);
+    gp.n_blocks = (K + bn - 1) / bn;
+    gp.k_blocks = (Cp + kBK - 1) / kBK;
+    const long long total = static_cast<long long>(E) * gp.m_blocks * gp.n_blocks;
+    gp.grid = static_cast<int>(std::min<long long>(total, num_sms));
+    gp.smem_bytes = gemm_smem(bn);
+    const CUtensorMapDataType dt = op == OpType::BF16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT16;
+    {
+        cuuint64_t dims[3] = {static_cast<cuuint64_t>(Cp), static_cast<cuuint64_t>(P), static_cast<cuuint64_t>(E)};
+        cuuint64_t strides[2] = {static_cast<cuuint64_t>(Cp) * 2, static_cast<cuuint64_t>(P) * Cp * 2};
+        cuuint32_t box[3] = {kBK, kBM, 1};
+        if (encode_tiled(&gp.tmA, dt, 3, const_cast<void*>(V), dims, strides, box, CU_TENSOR_MAP_SWIZZLE_128B) !=
+            CUDA_SUCCESS)
+            return cudaErrorInvalidValue;
+    }
+    {
+        cuuint64_t dims[3] = {static_cast<cuuint64_t>(Cp), static_cast<cuuint64_t>(K), static_cast<cuuint64_t>(E)};
+        cuuint64_t strides[2] = {static_cast<cuuint64_t>(Cp) * 2, static_cast<cuuint64_t>(K) * Cp * 2};
+        cuuint32_t box[3] = {kBK, static_cast<cuuint32_t>(bn), 1};
+        if (encode_tiled(&gp.tmB, dt, 3, const_cast<void*>(U), dims, strides, box, CU_TENSOR_MAP_SWIZZLE_128B) !=
+            CUDA_SUCCESS)
+            return cudaErrorInvalidValue;
+    }
+    return cudaSuccess;
+}
+
+cudaError_t launch_gemm(const GemmPlan& gp, void* Mw, DevErr* err, cudaStream_t stream) {
+    switch (gp.bn) {
+        case 32: return gemm_dispatch_bn<32>(gp, Mw, err, stream);
+        case 64: return gemm_dispatch_bn<64>(gp, Mw, err, stream);
+        case 128: return gemm_dispatch_bn<128>(gp, Mw, err, stream);
+        case 256: return gemm_dispatch_bn<256>(gp, Mw, err, stream);
+    }
+    return cudaErrorInvalidValue;
+}
+
+}  // namespace wg

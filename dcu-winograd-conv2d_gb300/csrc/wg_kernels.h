@@ -1,0 +1,93 @@
+// Host-side launchers of the operator's CUDA kernels.  All pointers are
+// device pointers; every launcher enqueues work on `stream` and returns the
+// cudaError_t of the launch.
+#pragma once
+#include <cstddef>
+#include <cstdint>
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+namespace wg {
+
+// Device error word written by kernels whose bounded waits give up.
+struct DevErr {
+    unsigned int code;   // first failing wait site (0 = none)
+    unsigned int count;  // number of failures
+};
+
+// Transform family: which interpolation points F(4x3) uses.
+enum class Xform : int { F2 = 0, F4 = 1, F4Ref = 2 };
+
+inline int xform_m(Xform x) { return x == Xform::F2 ? 2 : 4; }
+inline int xform_alpha(Xform x) { return xform_m(x) + 2; }
+
+enum class OpType : int { F16 = 0, BF16 = 1 };
+
+// Geometry of one convolution as the Winograd path sees it.
+struct Geom {
+    int n, c, h, w, k;   // NCHW input, K output channels
+    int pad_h, pad_w;    // 3x3 filter, stride 1
+    int oh, ow;          // output size
+    int m, alpha;        // output tile size and input tile size
+    int tiles_h, tiles_w;
+    long long P;         // tiles in the batch = n * tiles_h * tiles_w
+    int cp;              // C padded to a multiple of 8 (U and V row length)
+    int kp;              // K padded to a multiple of 8 (M row length)
+};
+
+Geom make_geom(int n, int c, int h, int w, int k, int pad_h, int pad_w, int m);
+
+// U[e][K][Cp] = G g G^T, from KCRS fp16 weights; fp32 arithmetic, result in
+// the operand type; zero for c >= C.
+cudaError_t launch_filter_transform(Xform xf, OpType op, const void* weight, void* U, int K, int C, int Cp,
+                                    cudaStream_t stream);
+
+// Per-tile power-of-two scale (F(4x3) scaling option): scale[p] = 2^-floor(log2 max|d|)
+// over the tile's input patch in every channel; 1 for an all-zero patch.
+cudaError_t launch_tile_scale(const Geom& g, const void* x, float* scale, cudaStream_t stream);
+
+// V[e][P][Cp] = B^T d B for images [n0, n0 + g.n) of the input; tile p is
+// counted from image n0 (the caller offsets V).  scale may be null.
+cudaError_t launch_input_transform(Xform xf, OpType op, const Geom& g, const void* x, void* V, const float* scale,
+                                   cudaStream_t stream);
+
+// out[N][K][OH][OW] = A^T M A from M[e][P][Kp] (fp16 when m_fp32 is false,
+// else fp32); divides by scale[p] when scale is not null.
+cudaError_t launch_output_transform(Xform xf, bool m_fp32, const Geom& g, const void* Mw, void* out,
+                                    const float* scale, cudaStream_t stream);
+
+// ---- tcgen05 batched GEMM: M_e[P][K] = V_e[P][Cp] * U_e[K][Cp]^T -----------
+struct GemmPlan {
+    CUtensorMap tmA;     // V
+    CUtensorMap tmB;     // U
+    int bn;              // 32, 64, 128 or 256
+    int E, P, K, Kp, Cp;
+    int m_blocks, n_blocks, k_blocks;
+    int grid;
+    int smem_bytes;
+    bool m_fp32;
+    OpType op;
+};
+
+// Builds the tensor maps; V, U, M must stay at these addresses.
+cudaError_t plan_gemm(GemmPlan& gp, OpType op, int E, long long P, int K, int Kp, int Cp, const void* V,
+                      const void* U, bool m_fp32, int bn, int num_sms);
+cudaError_t launch_gemm(const GemmPlan& gp, void* Mw, DevErr* err, cudaStream_t stream);
+
+// ---- fused F(2x3): input transform + tcgen05 GEMM + output transform ------
+struct FusedPlan {
+    CUtensorMap tmU;
+    int m_blocks, n_blocks, c_chunks;
+    int smem_bytes;
+    OpType op;
+};
+
+cudaError_t plan_fused2x3(FusedPlan& fp, OpType op, const Geom& g, const void* U);
+cudaError_t launch_fused2x3(const FusedPlan& fp, const Geom& g, const void* x, void* out, DevErr* err,
+                            cudaStream_t stream);
+
+// Tensor-map encoder from the driver (resolved once through the runtime).
+CUresult encode_tiled(CUtensorMap* map, CUtensorMapDataType dt, cuuint32_t rank, void* addr, const cuuint64_t* dims,
+                      const cuuint64_t* strides_bytes, const cuuint32_t* box, CUtensorMapSwizzle swz);
+
+}  // namespace wg

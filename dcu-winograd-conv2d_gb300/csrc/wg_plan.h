@@ -1,0 +1,79 @@
+// Plan object behind the opaque param blob of the C ABI.
+#pragma once
+#include <cstdint>
+
+#include "../../include/conv2d.h"
+#include "wg_kernels.h"
+
+namespace wg {
+
+constexpr uint32_t kParamMagic = 0x57474233u;  // "WGB3"
+
+// The param blob the caller allocates with getParamsize's size.  Its leading
+// fields mirror the reference's mykernelParamType (include/common.h:146-175)
+// so a debugger shows the familiar values; `plan` holds everything else.
+struct ParamBlob {
+    void* pin;
+    void* pweight;
+    void* pout;
+    void* U_d;
+    void* V_d;
+    void* M_d;
+    void* Y_d;
+    unsigned int n, c, h, w, k, r, s, u, v, p, q, Oh, Ow;
+    int kernel;  // selected algorithm (enum winograd_select order)
+    uint32_t magic;
+    void* plan;
+};
+
+struct Plan {
+    problem_t prob{};
+    conv2d_options_t opt{};
+    int device = 0;
+    int num_sms = 1;
+    int algo = 0;
+    Xform xf = Xform::F2;
+    OpType op = OpType::F16;
+    bool m_fp32 = false;
+    bool scaling = false;
+    Geom g{};
+    int chunk_n = 1, n_chunks = 1;
+    bool has_tail = false;
+    void* ws = nullptr;
+    long long ws_bytes = 0;
+    void* U = nullptr;
+    void* V = nullptr;
+    void* Mw = nullptr;
+    float* scale = nullptr;
+    DevErr* err = nullptr;
+    GemmPlan gemm_full{}, gemm_tail{};
+    FusedPlan fused{};
+    bool filter_ready = false;
+    int launches = 0;
+    unsigned info_grid = 0, info_threads = 0;
+    int info_smem = 0;
+
+    // when set, run() records an event on the stream after every launch
+    cudaEvent_t* marks = nullptr;
+    int n_marks = 0, max_marks = 0;
+
+    ~Plan();
+    int build(const problem_t* pr, const conv2d_options_t* opt);
+    int filter(cudaStream_t s);
+    int run(cudaStream_t s);
+    void mark(cudaStream_t s);
+    void release();
+};
+
+int validate_problem(const problem_t* pr);
+int options_default(conv2d_options_t* o);
+int default_bn(int K);
+int select_reference64(unsigned long long n, unsigned long long c, unsigned long long h, unsigned long long w,
+                       unsigned long long k, unsigned long long r, unsigned long long s, unsigned long long oh,
+                       unsigned long long ow);
+Plan* plan_of(const void* param);
+
+// Per-shape algorithm choice for CONV2D_ALGO_AUTO (autotune.cpp).
+int autotune_pick(const problem_t& pr, const conv2d_options_t& opt, int fallback);
+
+}  // namespace wg

@@ -1,0 +1,170 @@
+/*
+ * GB300 (sm_103a) Winograd 3x3 conv2d operator -- C ABI.
+ *
+ * Drop-in for the reference operator interface (reference include/conv2d.h:8-42):
+ * the same descriptor structs with the same field order and meaning, and the
+ * same three entry points called in the same order (src/main.cpp:58-105):
+ *
+ *     problem_t prob = {in, weight, out, n, c, h, w, k, r, s, u, v, p, q};
+ *     int size;  getParamsize(&prob, &size);
+ *     void* param = malloc(size);
+ *     kernelInfo_t info;  getkernelInfo(&prob, &info, param);
+ *     conv2d_fp16(param);            // as often as wanted
+ *     conv2d_destroy(param); free(param);   // extension: frees the workspace
+ *
+ * All tensor pointers are DEVICE pointers to IEEE binary16 data (the
+ * reference's _Float16*, ABI-identical to void*).  Input NCHW, weights KCRS,
+ * output N K Oh Ow.  Supported: r = s = 3, u = v = 1, any p, q with a
+ * positive output size.  Unsupported descriptors are rejected with a status
+ * code (the reference computes garbage for them).
+ *
+ * The reference exports getParamsize/getkernelInfo with C++ linkage; this
+ * library exports them both with C linkage (declared here) and with the
+ * reference's C++-mangled names, so code compiled against either header links.
+ */
+#ifndef GB300_WINOGRAD_CONV2D_H
+#define GB300_WINOGRAD_CONV2D_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* reference include/conv2d.h:8-24 */
+typedef struct
+{
+    void*        in;       /* input  [n][c][h][w]  fp16, device */
+    void*        weight;   /* filter [k][c][r][s]  fp16, device */
+    void*        out;      /* output [n][k][Oh][Ow] fp16, device */
+    unsigned int n;        /* batch */
+    unsigned int c;        /* input channels */
+    unsigned int h;        /* input height */
+    unsigned int w;        /* input width */
+    unsigned int k;        /* output channels */
+    unsigned int r;        /* filter height (must be 3) */
+    unsigned int s;        /* filter width  (must be 3) */
+    unsigned int u;        /* stride, height (must be 1) */
+    unsigned int v;        /* stride, width  (must be 1) */
+    unsigned int p;        /* padding, height */
+    unsigned int q;        /* padding, width */
+} problem_t;
+
+/* reference include/conv2d.h:26-36.  Filled with the launch shape of the
+ * main kernel of the selected algorithm (the reference leaves it unset). */
+typedef struct
+{
+    unsigned int blockx;
+    unsigned int blocky;
+    unsigned int blockz;
+    unsigned int threadx;
+    unsigned int thready;
+    unsigned int threadz;
+    unsigned int dynmicLdsSize;
+    void*        kernelPtr;
+} kernelInfo_t;
+
+/* Status codes (the reference always returns 0). */
+enum {
+    CONV2D_OK = 0,
+    CONV2D_ERR_INVALID = 1,      /* null pointer, zero size, or param blob not set up */
+    CONV2D_ERR_UNSUPPORTED = 2,  /* r,s != 3, u,v != 1, sizes beyond 32-bit tile counts */
+    CONV2D_ERR_NOMEM = 3,        /* device workspace allocation failed */
+    CONV2D_ERR_CUDA = 4,         /* a CUDA call or kernel launch failed */
+    CONV2D_ERR_TIMEOUT = 5,      /* a kernel gave up a bounded wait (device error word set) */
+    CONV2D_ERR_BUSY = 6          /* resource limit reached (server admission, queue full) */
+};
+
+/* Algorithms; values 0..2 are the reference's enum winograd_select
+ * (include/common.h:140-144). */
+enum {
+    CONV2D_ALGO_REFERENCE = -1,  /* the reference's selection rule (src/conv2d.cpp:125-156) */
+    CONV2D_ALGO_4X3_NON_FUSED = 0,
+    CONV2D_ALGO_2X3_NON_FUSED = 1,
+    CONV2D_ALGO_2X3_FUSED = 2,
+    CONV2D_ALGO_AUTO = 3         /* per-shape autotuner (measures candidates once per shape) */
+};
+
+/* Options for getkernelInfo_ex.  conv2d_options_default() gives the values
+ * getkernelInfo uses, after applying the WG_CONV2D_* environment overrides. */
+typedef struct
+{
+    int algo;            /* CONV2D_ALGO_* */
+    int operand_bf16;    /* 0: fp16 Winograd-domain operands, 1: bf16 */
+    int tile_scaling;    /* F(4x3): per-tile power-of-two scaling of the input transform */
+    int f4_points;       /* F(4x3) interpolation points: 0 = {0,+-1,2,-1/2}, 1 = reference {0,+-1,+-2} */
+    int filter_policy;   /* 0: transform the filter on the first call, then reuse; 1: every call */
+    int gemm_bn;         /* GEMM output-channel tile: 0 = automatic, else 32/64/128/256 */
+    long long l2_chunk_bytes; /* non-fused: process images in chunks whose V+M fit this many bytes (0 = one pass) */
+    int reserved[4];
+} conv2d_options_t;
+
+/* reference include/conv2d.h:39-42 */
+int getParamsize(problem_t* problem, int* paramSize);
+int getkernelInfo(problem_t* problem, kernelInfo_t* kernelInfo, void* param);
+void conv2d_fp16(const void* param_ptr);
+
+/* ---- extensions (no counterpart in the reference unless noted) ---------- */
+
+/* Same entry points under distinct names (used by the C++-linkage shims). */
+int wg_getParamsize(problem_t* problem, int* paramSize);
+int wg_getkernelInfo(problem_t* problem, kernelInfo_t* kernelInfo, void* param);
+
+int conv2d_options_default(conv2d_options_t* opt);
+
+/* getkernelInfo with explicit options (opt may be NULL = defaults). */
+int getkernelInfo_ex(problem_t* problem, kernelInfo_t* kernelInfo, void* param, const conv2d_options_t* opt);
+
+/* conv2d_fp16 on a caller stream (cudaStream_t passed as void*; NULL = legacy
+ * default stream), returning a status instead of exiting the process. */
+int conv2d_fp16_ex(const void* param_ptr, void* stream);
+
+/* End-to-end call with HOST buffers: copies host_in (n*c*h*w fp16) to the
+ * problem's device input, runs, copies the output to host_out and waits for
+ * the stream.  Pinned host memory makes the copies asynchronous. */
+int conv2d_fp16_host(const void* param_ptr, const void* host_in, void* host_out, void* stream);
+
+/* Re-run the filter transform (after the caller changed the weights in place). */
+int conv2d_refresh_filter(const void* param_ptr, void* stream);
+
+/* Frees the device workspace that getkernelInfo allocated (the reference has no
+ * release path: include/common.h:174 never runs).  The blob is unusable after. */
+int conv2d_destroy(void* param_ptr);
+
+/* Selected algorithm (CONV2D_ALGO_4X3_NON_FUSED .. CONV2D_ALGO_2X3_FUSED), or -1. */
+int conv2d_get_algo(const void* param_ptr);
+
+/* Device workspace bytes held by the blob. */
+long long conv2d_workspace_bytes(const void* param_ptr);
+
+/* Kernel launches one conv2d_fp16 call makes (with the filter already transformed). */
+int conv2d_launches_per_call(const void* param_ptr);
+
+/* Waits for the device, then reports (and clears) the device error word of the
+ * blob's kernels: CONV2D_OK or CONV2D_ERR_TIMEOUT; `site` receives the first
+ * failing wait site (may be NULL). */
+int conv2d_check_device(const void* param_ptr, int* site);
+
+/* Status and message of the last failing call on this thread. */
+int conv2d_last_error(void);
+const char* conv2d_last_error_message(void);
+const char* conv2d_status_string(int status);
+
+/* The reference selection rule evaluated in 64-bit arithmetic (0..2). */
+int conv2d_select_reference(const problem_t* problem);
+
+/* One call with a CUDA event recorded on the stream after every kernel
+ * launch; waits, writes each launch's duration (ms, launch order) to
+ * kernel_ms and returns the number of launches (negative status on error). */
+int conv2d_fp16_timed(const void* param_ptr, void* stream, float* kernel_ms, int max_kernels);
+
+/* Copies `bytes` from device memory to host memory and waits (used by tests
+ * to read the Winograd-domain workspaces U_d/V_d/M_d of the param blob). */
+int conv2d_copy_to_host(void* host_dst, const void* device_src, size_t bytes);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GB300_WINOGRAD_CONV2D_H */

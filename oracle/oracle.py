@@ -238,6 +238,23 @@ AT = {
     4: _mat([[1, 1, 1, 1, 1, 0], [0, 1, -1, 2, -2, 0], [0, 1, 1, 4, 4, 0], [0, 1, -1, 8, -8, 1]]),
 }
 
+# F(4x3) with interpolation points 0, +-1, 2, -1/2 (the operator's default
+# F(4x3) transform; the reference's points are 0, +-1, +-2 above).  Same
+# Cook-Toom construction: A^T columns are the points' powers, G rows are the
+# Lagrange weights, B^T solves A^T((G g) . (B^T d)) = correlation(d, g).
+BT_F4S = _mat([[1, "3/2", -2, "-3/2", 1, 0], [0, -1, "-5/2", "-1/2", 1, 0], [0, 1, "1/2", "-5/2", 1, 0],
+               [0, "-1/2", -1, "1/2", 1, 0], [0, 2, -1, -2, 1, 0], [0, 1, "3/2", -2, "-3/2", 1]])
+G_F4S = _mat([[1, 0, 0], ["-1/3", "-1/3", "-1/3"], ["1/3", "-1/3", "1/3"], ["1/15", "2/15", "4/15"],
+              ["-16/15", "8/15", "-4/15"], [0, 0, 1]])
+AT_F4S = _mat([[1, 1, 1, 1, 1, 0], [0, 1, -1, 2, "-1/2", 0], [0, 1, 1, 4, "1/4", 0], [0, 1, -1, 8, "-1/8", 1]])
+
+# transform sets by name: "F2", "F4" (points 0,+-1,2,-1/2), "F4Ref" (0,+-1,+-2)
+XFORMS = {
+    "F2": (2, BT[2], G[2], AT[2]),
+    "F4": (4, BT_F4S, G_F4S, AT_F4S),
+    "F4Ref": (4, BT[4], G[4], AT[4]),
+}
+
 
 def tile_grid(n, h, w, m, p=1, q=1):
     oh, ow = out_hw(h, w, 3, 3, 1, 1, p, q)
@@ -263,46 +280,52 @@ def input_tiles(x, m, p=1, q=1):
     return d.reshape(P, c, a, a)
 
 
-def input_transform(x, m, p=1, q=1):
+def _xf(m, variant):
+    if variant is None:
+        return m, BT[m], G[m], AT[m]
+    return XFORMS[variant]
+
+
+def input_transform(x, m, p=1, q=1, variant=None):
     """V[e][P][C] = (B^T d B)[e // alpha][e % alpha]."""
+    m, B, _, _ = _xf(m, variant)
     d = input_tiles(x, m, p, q)
-    B = BT[m]
     v = np.einsum("ir,pcrs,js->ijpc", B, d, B)
     a = m + 2
     return v.reshape(a * a, d.shape[0], d.shape[1])
 
 
-def filter_transform(wt, m):
+def filter_transform(wt, m, variant=None):
     """U[e][K][C] = (G g G^T)[e // alpha][e % alpha]."""
+    m, _, Gm, _ = _xf(m, variant)
     g = np.asarray(wt, dtype=np.float64)
-    Gm = G[m]
     u = np.einsum("ir,kcrs,js->ijkc", Gm, g, Gm)
     a = m + 2
     return u.reshape(a * a, g.shape[0], g.shape[1])
 
 
-def output_transform(Mw, m, n, k, oh, ow):
+def output_transform(Mw, m, n, k, oh, ow, variant=None):
     """Mw[e][P][K] -> out [N][K][OH][OW] via A^T M A, clipped to the image."""
+    m, _, _, A = _xf(m, variant)
     a = m + 2
     P = Mw.shape[1]
     th, tw = -(-oh // m), -(-ow // m)
     Mm = Mw.reshape(a, a, P, k)
-    A = AT[m]
     y = np.einsum("ir,rspk,js->pkij", A, Mm, A)  # [P][K][m][m]
     y = y.reshape(n, th, tw, k, m, m).transpose(0, 3, 1, 4, 2, 5).reshape(n, k, th * m, tw * m)
     return y[:, :, :oh, :ow]
 
 
-def winograd_conv(x, wt, m, p=1, q=1):
+def winograd_conv(x, wt, m, p=1, q=1, variant=None):
     """Whole Winograd convolution in float64 (equals the direct conv up to
     float64 rounding)."""
     n, c, h, w = x.shape
     k = wt.shape[0]
     oh, ow = out_hw(h, w, 3, 3, 1, 1, p, q)
-    V = input_transform(x, m, p, q)
-    U = filter_transform(wt, m)
+    V = input_transform(x, m, p, q, variant)
+    U = filter_transform(wt, m, variant)
     Mw = np.einsum("epc,ekc->epk", V, U)
-    return output_transform(Mw, m, n, k, oh, ow)
+    return output_transform(Mw, m, n, k, oh, ow, variant)
 
 
 def direct_flops(n, c, h, w, k, p=1, q=1):

@@ -1,0 +1,236 @@
+"""GPU parity tests: the CUDA operator, called through its C ABI, against the
+oracle (the reference verifier restated, pinned to the reference build) and
+the golden vectors made by the reference's own verifier.
+
+Tolerances (max over elements of |y - ref| / max(|ref|, rms(ref))):
+F(2x3) 1e-2, F(4x3) 2e-2 for fp16 operands; bf16 operands are a precision
+study with looser bounds written at each test.
+"""
+import os
+
+import numpy as np
+import pytest
+
+import oracle as O
+
+torch = pytest.importorskip("torch")
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = np.load(os.path.join(os.path.dirname(__file__), "golden", "conv_golden.npz"))
+GOLDEN_CASES = sorted({k.split("__")[0] for k in GOLDEN.files})
+TOL = {2: 1e-2, 4: 2e-2}
+ALGOS = [-1, 0, 1, 2]  # reference selection, F(4x3), F(2x3), F(2x3) fused
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _cuda():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+
+
+def algo_m(algo):
+    return 4 if algo == 0 else 2
+
+
+def run(wg, x16, w16, p=1, q=1, opts=None, stream=None):
+    x = torch.from_numpy(np.ascontiguousarray(x16)).cuda()
+    w = torch.from_numpy(np.ascontiguousarray(w16)).cuda()
+    y, op = wg.conv2d_torch(x, w, p, q, opts, stream=stream)
+    torch.cuda.synchronize()
+    st, site = op.check_device()
+    assert st == wg.OK, f"device wait gave up at site {site}"
+    return y.cpu().numpy(), op
+
+
+def opts_for(wg, algo, **kw):
+    return wg.default_options(algo=algo, **kw)
+
+
+def golden_case(name):
+    seed, n, c, h, w, k, p, q = (int(v) for v in GOLDEN[name + "__meta"])
+    kind = str(GOLDEN[name + "__kind"])
+    if kind == "refstyle":
+        x, wt = O.reference_style_inputs(n, c, h, w, k)
+    else:
+        x, wt = O.uniform_inputs(seed, n, c, h, w, k)
+    return kind, x, wt, p, q, GOLDEN[name + "__out"].view(np.float16)
+
+
+@pytest.mark.parametrize("algo", ALGOS)
+@pytest.mark.parametrize("name", GOLDEN_CASES)
+def test_golden_vectors(wg, name, algo):
+    kind, x, wt, p, q, ref = golden_case(name)
+    y, op = run(wg, x, wt, p, q, opts_for(wg, algo))
+    m = algo_m(op.algo)
+    mx, mean, _ = O.rel_errors(y, ref)
+    assert mx <= TOL[m], (name, op.algo, mx, mean)
+    if kind == "refstyle":
+        # the reference benchmark's own acceptance check (src/main.cpp:123-132)
+        assert O.reference_criterion_failures(y, ref) == 0
+
+
+@pytest.mark.parametrize("algo", [0, 1, 2])
+@pytest.mark.parametrize("shape", [
+    (1, 3, 7, 7, 5), (2, 5, 14, 14, 27), (1, 16, 28, 28, 4), (3, 8, 13, 9, 12), (1, 70, 10, 10, 33),
+    (1, 130, 9, 9, 130), (2, 64, 20, 20, 64), (1, 200, 8, 8, 300), (1, 24, 112, 112, 16), (4, 40, 7, 7, 260),
+])
+@pytest.mark.parametrize("pad", [(1, 1), (0, 0), (2, 1)])
+def test_ragged_against_fp64(wg, algo, shape, pad):
+    n, c, h, w, k = shape
+    if h + 2 * pad[0] < 3 or w + 2 * pad[1] < 3:
+        pytest.skip("no output")
+    x, wt = O.uniform_inputs(hash((shape, pad)) % 1000, n, c, h, w, k, filt="normal")
+    y, op = run(wg, x, wt, pad[0], pad[1], opts_for(wg, algo))
+    _, r64 = O.conv2d_direct(x, wt, p=pad[0], q=pad[1], nthreads=8)
+    mx, mean, _ = O.rel_errors(y, r64)
+    assert op.algo == algo
+    assert mx <= TOL[algo_m(algo)], (shape, pad, algo, mx, mean)
+
+
+def _dev_array(wg, ptr, count, dtype):
+    out = np.empty(count, dtype=dtype)
+    wg.copy_to_host(out.ctypes.data, ptr, out.nbytes)
+    return out
+
+
+@pytest.mark.parametrize("algo,variant", [(1, "F2"), (0, "F4"), (0, "F4Ref")])
+def test_transform_kernels_elementwise(wg, algo, variant):
+    """U, V and M read back from the workspace, each against its restatement."""
+    n, c, h, w, k = 2, 20, 11, 13, 24
+    x, wt = O.uniform_inputs(31, n, c, h, w, k)
+    opts = opts_for(wg, algo, f4_points=1 if variant == "F4Ref" else 0)
+    y, op = run(wg, x, wt, 1, 1, opts)
+    m = O.XFORMS[variant][0]
+    E = (m + 2) ** 2
+    cp, kp = (c + 7) // 8 * 8, (k + 7) // 8 * 8
+    oh, ow = O.out_hw(h, w)
+    P = n * (-(-oh // m)) * (-(-ow // m))
+    Up, Vp, Mp = op.blob_pointers()
+    U = _dev_array(wg, Up, E * k * cp, np.float16).reshape(E, k, cp).astype(np.float64)
+    V = _dev_array(wg, Vp, E * P * cp, np.float16).reshape(E, P, cp).astype(np.float64)
+    mdt = np.float32 if m == 4 else np.float16
+    Mw = _dev_array(wg, Mp, E * P * kp, mdt).reshape(E, P, kp).astype(np.float64)
+
+    U_ref = O.filter_transform(wt.astype(np.float64), m, variant)
+    V_ref = O.input_transform(x.astype(np.float64), m, 1, 1, variant)
+    _, B, Gm, _ = O.XFORMS[variant]
+    d = O.input_tiles(x.astype(np.float64), m, 1, 1)
+    V_abs = np.einsum("ir,pcrs,js->ijpc", np.abs(B), np.abs(d), np.abs(B)).reshape(E, P, c)
+    U_abs = np.einsum("ir,kcrs,js->ijkc", np.abs(Gm), np.abs(wt.astype(np.float64)), np.abs(Gm)).reshape(E, k, c)
+    assert np.all(U[:, :, c:] == 0) and np.all(V[:, :, c:] == 0)
+    # one fp16 rounding of an fp32 result (fp32 error bounded by the sum of |terms|)
+    assert np.all(np.abs(U[:, :, :c] - U_ref) <= np.abs(U_ref) * 2.0 ** -10 + U_abs * 2.0 ** -20)
+    assert np.all(np.abs(V[:, :, :c] - V_ref) <= np.abs(V_ref) * 2.0 ** -10 + V_abs * 2.0 ** -20)
+    # GEMM of exactly the stored operands, fp32 accumulation
+    M_ref = np.einsum("epc,ekc->epk", V, U)
+    scale = np.einsum("epc,ekc->epk", np.abs(V), np.abs(U)) + 1e-30
+    tol = 2.0 ** -10 if mdt == np.float16 else 1e-5
+    assert np.all(np.abs(Mw[:, :, :k] - M_ref) <= scale * tol)
+    # output transform of exactly the stored M
+    y_ref = O.output_transform(Mw[:, :, :k], m, n, k, oh, ow, variant)
+    yscale = np.abs(y_ref).max()
+    assert np.abs(y.astype(np.float64) - y_ref).max() <= yscale * 2.0 ** -10
+
+
+@pytest.mark.parametrize("algo", [0, 1, 2])
+def test_repeat_calls_bit_identical(wg, algo):
+    x, wt = O.uniform_inputs(3, 2, 48, 30, 30, 40)
+    xt = torch.from_numpy(x).cuda()
+    wtt = torch.from_numpy(wt).cuda()
+    y, op = wg.conv2d_torch(xt, wtt, 1, 1, opts_for(wg, algo))
+    first = y.clone()
+    for _ in range(3):
+        op(torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    assert torch.equal(first, y)
+
+
+def test_reference_harness_replay_cfg1(wg):
+    """1x64x56x56 -> 64, reference-style inputs, the reference's own selection
+    (F(4x3)), checked as the reference benchmark checks it."""
+    _, x, wt, p, q, ref = golden_case("refstyle_cfg1")
+    y, op = run(wg, x, wt, p, q, None)
+    assert op.algo == 0
+    assert O.reference_criterion_failures(y, ref) == 0
+    assert O.rel_errors(y, ref)[0] <= TOL[4]
+
+
+def test_legacy_void_entry_point(wg):
+    import ctypes
+    x, wt = O.uniform_inputs(8, 1, 16, 12, 12, 16)
+    xt, wtt = torch.from_numpy(x).cuda(), torch.from_numpy(wt).cuda()
+    y = torch.empty((1, 16, 12, 12), dtype=torch.float16, device="cuda")
+    prob = wg.make_problem(xt.data_ptr(), wtt.data_ptr(), y.data_ptr(), 1, 16, 12, 12, 16)
+    op = wg.Conv2d(prob)
+    torch.cuda.synchronize()
+    wg.lib().conv2d_fp16(op.ptr)  # legacy default stream, like the reference harness
+    torch.cuda.synchronize()
+    _, r64 = O.conv2d_direct(x, wt)
+    assert O.rel_errors(y.cpu().numpy(), r64)[0] <= TOL[2]
+
+
+def test_side_stream(wg):
+    x, wt = O.uniform_inputs(9, 2, 32, 24, 24, 32)
+    s = torch.cuda.Stream()
+    with torch.cuda.stream(s):
+        y, op = run(wg, x, wt, 1, 1, opts_for(wg, 1), stream=s.cuda_stream)
+    _, r64 = O.conv2d_direct(x, wt)
+    assert O.rel_errors(y, r64)[0] <= TOL[2]
+
+
+def test_tile_scaling_is_exact(wg):
+    """Power-of-two per-tile scaling changes no rounding for normal-range data."""
+    x, wt = O.normal_inputs(4, 2, 64, 20, 20, 48, heavy=True)
+    a, _ = run(wg, x, wt, 1, 1, opts_for(wg, 0, tile_scaling=0))
+    b, _ = run(wg, x, wt, 1, 1, opts_for(wg, 0, tile_scaling=1))
+    _, r64 = O.conv2d_direct(x, wt, nthreads=8)
+    assert O.rel_errors(b, r64)[0] <= TOL[4]
+    assert O.rel_errors(a, b)[0] <= 2e-3
+
+
+@pytest.mark.parametrize("algo", [0, 1])
+def test_l2_chunking_is_bit_identical(wg, algo):
+    x, wt = O.uniform_inputs(5, 7, 32, 16, 16, 40)
+    a, _ = run(wg, x, wt, 1, 1, opts_for(wg, algo))
+    b, opb = run(wg, x, wt, 1, 1, opts_for(wg, algo, l2_chunk_bytes=1))  # one image per chunk
+    assert opb.launches_per_call == 7 * 3
+    assert np.array_equal(a.view(np.uint16), b.view(np.uint16))
+
+
+@pytest.mark.parametrize("algo", [0, 1, 2])
+def test_bf16_operands(wg, algo):
+    x, wt = O.uniform_inputs(6, 2, 64, 18, 18, 64, filt="normal")
+    y, _ = run(wg, x, wt, 1, 1, opts_for(wg, algo, operand_bf16=1))
+    _, r64 = O.conv2d_direct(x, wt, nthreads=8)
+    mx = O.rel_errors(y, r64)[0]
+    assert mx <= (0.3 if algo == 0 else 6e-2), mx
+
+
+def test_refresh_filter_after_in_place_change(wg):
+    x, wt = O.uniform_inputs(12, 1, 16, 10, 10, 8)
+    xt, wtt = torch.from_numpy(x).cuda(), torch.from_numpy(wt).cuda()
+    y, op = wg.conv2d_torch(xt, wtt, 1, 1, opts_for(wg, 1))
+    wt2 = (wt * np.float16(-0.5)).astype(np.float16)
+    wtt.copy_(torch.from_numpy(wt2))
+    s = torch.cuda.current_stream().cuda_stream
+    op.refresh_filter(s)
+    op(s)
+    torch.cuda.synchronize()
+    _, r64 = O.conv2d_direct(x, wt2)
+    assert O.rel_errors(y.cpu().numpy(), r64)[0] <= TOL[2]
+
+
+def test_host_buffer_entry_point(wg):
+    x, wt = O.uniform_inputs(13, 2, 24, 16, 16, 24)
+    xt = torch.empty((2, 24, 16, 16), dtype=torch.float16, device="cuda")
+    wtt = torch.from_numpy(wt).cuda()
+    y = torch.empty((2, 24, 16, 16), dtype=torch.float16, device="cuda")
+    prob = wg.make_problem(xt.data_ptr(), wtt.data_ptr(), y.data_ptr(), 2, 24, 16, 16, 24)
+    op = wg.Conv2d(prob, opts_for(wg, 2))
+    hin = torch.from_numpy(x).pin_memory()
+    hout = torch.empty((2, 24, 16, 16), dtype=torch.float16).pin_memory()
+    torch.cuda.synchronize()
+    op.host(hin.data_ptr(), hout.data_ptr(), torch.cuda.current_stream().cuda_stream)
+    _, r64 = O.conv2d_direct(x, wt)
+    assert O.rel_errors(hout.numpy(), r64)[0] <= TOL[2]

@@ -61,11 +61,12 @@ def test_multithreaded_oracle_is_identical():
     assert np.array_equal(a64, b64)
 
 
-@pytest.mark.parametrize("m", [2, 4])
+@pytest.mark.parametrize("variant", ["F2", "F4", "F4Ref"])
 @pytest.mark.parametrize("pad", [(1, 1), (0, 0), (2, 2), (1, 0)])
-def test_winograd_restatement_equals_direct_fp64(m, pad):
+def test_winograd_restatement_equals_direct_fp64(variant, pad):
     x, wt = O.uniform_inputs(5, 2, 5, 9, 11, 6)
-    y = O.winograd_conv(x.astype(np.float64), wt.astype(np.float64), m, *pad)
+    m = O.XFORMS[variant][0]
+    y = O.winograd_conv(x.astype(np.float64), wt.astype(np.float64), m, *pad, variant=variant)
     _, r64 = O.conv2d_direct(x, wt, p=pad[0], q=pad[1])
     assert np.abs(y - r64).max() < 1e-10
 
