@@ -93,7 +93,7 @@ typedef struct
     int algo;            /* CONV2D_ALGO_* */
     int operand_bf16;    /* 0: fp16 Winograd-domain operands, 1: bf16 */
     int tile_scaling;    /* F(4x3): per-tile power-of-two scaling of the input transform */
-    int f4_points;       /* F(4x3) interpolation points: 0 = {0,+-1,2,-1/2}, 1 = reference {0,+-1,+-2} */
+    int f4_points;       /* F(4x3) interpolation points: 0 = {0,+-1,1/2,-2}, 1 = reference {0,+-1,+-2} */
     int filter_policy;   /* 0: transform the filter on the first call, then reuse; 1: every call */
     int gemm_bn;         /* GEMM output-channel tile: 0 = automatic, else 32/64/128/256 */
     long long l2_chunk_bytes; /* non-fused: process images in chunks whose V+M fit this many bytes (0 = one pass) */

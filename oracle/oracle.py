@@ -238,17 +238,17 @@ AT = {
     4: _mat([[1, 1, 1, 1, 1, 0], [0, 1, -1, 2, -2, 0], [0, 1, 1, 4, 4, 0], [0, 1, -1, 8, -8, 1]]),
 }
 
-# F(4x3) with interpolation points 0, +-1, 2, -1/2 (the operator's default
+# F(4x3) with interpolation points 0, +-1, 1/2, -2 (the operator's default
 # F(4x3) transform; the reference's points are 0, +-1, +-2 above).  Same
 # Cook-Toom construction: A^T columns are the points' powers, G rows are the
 # Lagrange weights, B^T solves A^T((G g) . (B^T d)) = correlation(d, g).
-BT_F4S = _mat([[1, "3/2", -2, "-3/2", 1, 0], [0, -1, "-5/2", "-1/2", 1, 0], [0, 1, "1/2", "-5/2", 1, 0],
-               [0, "-1/2", -1, "1/2", 1, 0], [0, 2, -1, -2, 1, 0], [0, 1, "3/2", -2, "-3/2", 1]])
-G_F4S = _mat([[1, 0, 0], ["-1/3", "-1/3", "-1/3"], ["1/3", "-1/3", "1/3"], ["1/15", "2/15", "4/15"],
-              ["-16/15", "8/15", "-4/15"], [0, 0, 1]])
-AT_F4S = _mat([[1, 1, 1, 1, 1, 0], [0, 1, -1, 2, "-1/2", 0], [0, 1, 1, 4, "1/4", 0], [0, 1, -1, 8, "-1/8", 1]])
+BT_F4S = _mat([[1, "-3/2", -2, "3/2", 1, 0], [0, -1, "1/2", "5/2", 1, 0], [0, 1, "-5/2", "1/2", 1, 0],
+               [0, -2, -1, 2, 1, 0], [0, "1/2", -1, "-1/2", 1, 0], [0, 1, "-3/2", -2, "3/2", 1]])
+G_F4S = _mat([[1, 0, 0], ["1/3", "1/3", "1/3"], ["-1/3", "1/3", "-1/3"], ["-16/15", "-8/15", "-4/15"],
+              ["1/15", "-2/15", "4/15"], [0, 0, 1]])
+AT_F4S = _mat([[1, 1, 1, 1, 1, 0], [0, 1, -1, "1/2", -2, 0], [0, 1, 1, "1/4", 4, 0], [0, 1, -1, "1/8", -8, 1]])
 
-# transform sets by name: "F2", "F4" (points 0,+-1,2,-1/2), "F4Ref" (0,+-1,+-2)
+# transform sets by name: "F2", "F4" (points 0,+-1,1/2,-2), "F4Ref" (0,+-1,+-2)
 XFORMS = {
     "F2": (2, BT[2], G[2], AT[2]),
     "F4": (4, BT_F4S, G_F4S, AT_F4S),

@@ -167,7 +167,7 @@ def test_legacy_void_entry_point(wg):
     wg.lib().conv2d_fp16(op.ptr)  # legacy default stream, like the reference harness
     torch.cuda.synchronize()
     _, r64 = O.conv2d_direct(x, wt)
-    assert O.rel_errors(y.cpu().numpy(), r64)[0] <= TOL[2]
+    assert O.rel_errors(y.cpu().numpy(), r64)[0] <= TOL[algo_m(op.algo)]
 
 
 def test_side_stream(wg):
