@@ -137,6 +137,8 @@ int Plan::build(const problem_t* pr, const conv2d_options_t* opt_in) {
         opt = *opt_in;
     else
         options_default(&opt);
+    if (reinterpret_cast<uintptr_t>(pr->in) % 16 != 0)
+        return fail(CONV2D_ERR_UNSUPPORTED, "input pointer must be 16-byte aligned");
     if (cudaGetDevice(&device) != cudaSuccess) return fail(CONV2D_ERR_CUDA, "no CUDA device");
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
@@ -150,6 +152,14 @@ int Plan::build(const problem_t* pr, const conv2d_options_t* opt_in) {
     if (algo < 0 || algo > 2) return fail(CONV2D_ERR_INVALID, "bad algorithm");
 
     op = opt.operand_bf16 ? OpType::BF16 : OpType::F16;
+    if (algo == CONV2D_ALGO_2X3_FUSED) {
+        // the fused kernel stages the input rows of 128 tiles in shared memory;
+        // for very wide images they do not fit and F(2x3) runs non-fused
+        FusedPlan probe{};
+        const Geom g2 = make_geom(pr->n, pr->c, pr->h, pr->w, pr->k, pr->p, pr->q, 2);
+        if (plan_fused2x3(probe, op, g2, nullptr) == cudaErrorNotSupported) algo = CONV2D_ALGO_2X3_NON_FUSED;
+        cudaGetLastError();
+    }
     const int m = algo == CONV2D_ALGO_4X3_NON_FUSED ? 4 : 2;
     xf = m == 2 ? Xform::F2 : (opt.f4_points ? Xform::F4Ref : Xform::F4);
     m_fp32 = (m == 4);
@@ -240,8 +250,9 @@ int Plan::run(cudaStream_t s) {
         if (st) return st;
     }
     cudaError_t ce;
+    const void* x_end = static_cast<const uint16_t*>(prob.in) + static_cast<long long>(prob.n) * g.c * g.h * g.w;
     if (algo == CONV2D_ALGO_2X3_FUSED) {
-        ce = launch_fused2x3(fused, g, prob.in, prob.out, err, s);
+        ce = launch_fused2x3(fused, g, prob.in, x_end, prob.out, err, s);
         if (ce != cudaSuccess) return cuda_fail(ce, "fused F(2x3) launch");
         mark(s);
         return CONV2D_OK;
@@ -259,7 +270,7 @@ int Plan::run(cudaStream_t s) {
             if (ce != cudaSuccess) return cuda_fail(ce, "tile scale launch");
             mark(s);
         }
-        ce = launch_input_transform(xf, op, gc, xin, V, scale, s);
+        ce = launch_input_transform(xf, op, gc, xin, x_end, V, scale, err, s);
         if (ce != cudaSuccess) return cuda_fail(ce, "input transform launch");
         mark(s);
         const GemmPlan& gp = (has_tail && ci == n_chunks - 1) ? gemm_tail : gemm_full;

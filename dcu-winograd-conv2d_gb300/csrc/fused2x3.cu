@@ -3,20 +3,25 @@
 //
 // This is the reference's winograd_2x3_kernel (src/winograd_2x3_fused.cpp:10-369,
 // launcher :372-392) re-designed for tcgen05:
-//   * CTA = 128 output tiles x 32 output channels, looping over the input
-//     channels in chunks of 16 (the reference: 32 tiles x 32 channels,
+//   * CTA = 128 consecutive output tiles x 32 output channels, looping over the
+//     input channels in chunks of 16 (the reference: 32 tiles x 32 channels,
 //     chunks of 16, 16 wave64 MMAC GEMMs);
-//   * warps 0-7 load the 4x4 input patches (zero halo), run B^T d B in fp32
-//     and write the 16 Winograd-domain tiles straight into shared memory in
-//     the tcgen05 canonical K-major layout (no swizzle);
-//   * the transformed filter U (made once per weight set) arrives by TMA;
-//   * warp 8 issues the 16 tcgen05.mma (M=128, N=32, K=16) per chunk from
-//     one thread, accumulating all 16 elements in the 512 TMEM columns;
-//   * after the last chunk warps 0-7 read TMEM, apply A^T m A and write
-//     the 2x2 outputs to NCHW.
-// Two pipeline stages; every wait is bounded (wg_ptx.cuh).
+//   * the input rows a chunk needs are staged with cp.async.bulk (one
+//     contiguous copy per channel and image), double-buffered one chunk ahead;
+//   * warps 0-7 (lanes over consecutive tiles) run B^T d B in fp32 from shared
+//     memory and write the 16 Winograd-domain tiles into shared memory in the
+//     tcgen05 canonical K-major layout;
+//   * the transformed filter U (made once per weight set) arrives by one 4-D
+//     TMA per chunk;
+//   * warp 8 issues the 16 tcgen05.mma (M=128, N=32, K=16) per chunk from one
+//     thread, accumulating all 16 elements in the 512 TMEM columns;
+//   * after the last chunk warps 0-7 read TMEM, apply A^T m A and write the
+//     2x2 outputs to NCHW.
+// Every wait is bounded (wg_ptx.cuh).
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
+
+#include <algorithm>
 
 #include "wg_kernels.h"
 #include "wg_ptx.cuh"
@@ -30,15 +35,15 @@ constexpr int kTilesPerCta = 128;
 constexpr int kOcPerCta = 32;
 constexpr int kChunk = 16;                               // input channels per stage
 constexpr int kElems = 16;                               // 4x4 Winograd elements
-constexpr int kAHalf = kElems * kTilesPerCta * 16;       // 8 channels of every element: 32 KB
+constexpr int kAHalf = kElems * kTilesPerCta * 16;       // one granule of every element: 32 KB
 constexpr int kABytes = 2 * kAHalf;                      // 64 KB
-constexpr int kBHalf = kElems * kOcPerCta * 16;          // 8 KB
-constexpr int kBBytes = 2 * kBHalf;                      // 16 KB
+constexpr int kBBytes = kElems * 2 * kOcPerCta * 16;     // 16 KB: [e][granule][k][8]
 constexpr int kStageBytes = kABytes + kBBytes;           // 80 KB
 constexpr int kStages = 2;
-constexpr int kSmem = kStages * kStageBytes + 1024 + 256;
+constexpr int kMaxSeg = 16;                              // images one CTA's tiles may span
 constexpr int kProducers = 256;
 constexpr int kThreads = kProducers + 32;
+constexpr int kSmemFixed = kStages * kStageBytes + 1024 /*align*/ + 512 /*barriers, segment table*/;
 
 template <bool BF16> struct OpT;
 template <> struct OpT<false> {
@@ -54,11 +59,18 @@ template <> struct OpT<true> {
     }
 };
 
+struct SegTable {
+    int nseg;
+    int n_first;
+    int ylo[kMaxSeg], yhi[kMaxSeg], off[kMaxSeg];
+};
+
 template <bool BF16>
 __global__ void __launch_bounds__(kThreads, 1)
-    fused2x3_kernel(const __half* __restrict__ x, const __grid_constant__ CUtensorMap tmU, __half* __restrict__ out,
-                    int C, int H, int W, int K, int pad_h, int pad_w, int OH, int OW, int tiles_h, int tiles_w,
-                    int P, int c_chunks, int n_blocks, DevErr* err) {
+    fused2x3_kernel(const __half* __restrict__ x, const __half* __restrict__ x_end,
+                    const __grid_constant__ CUtensorMap tmU, __half* __restrict__ out, int C, int H, int W, int K,
+                    int pad_h, int pad_w, int OH, int OW, int tiles_h, int tiles_w, int P, int c_chunks, int n_blocks,
+                    int stg_ch_bytes, int nbuf, DevErr* err) {
     constexpr uint32_t kIdesc = make_idesc_f16(128, kOcPerCta, BF16);
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     unsigned char* smem = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
@@ -66,20 +78,46 @@ __global__ void __launch_bounds__(kThreads, 1)
     uint64_t* full = bars;             // [2] producers (256) + TMA expect_tx (1)
     uint64_t* empty = bars + 2;        // [2] MMA commit
     uint64_t* tfull = bars + 4;        // accumulators ready
-    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 5);
+    uint64_t* sfull = bars + 5;        // [2] staging copies landed
+    uint64_t* sempty = bars + 7;       // [2] staging buffer read by all producers
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 9);
     volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
+    SegTable* seg = reinterpret_cast<SegTable*>(bars + 10);
+    unsigned char* stg = smem + kStages * kStageBytes + 512;  // nbuf x 16 channels x stg_ch_bytes
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int n_blk = blockIdx.x % n_blocks;
     const int m_blk = blockIdx.x / n_blocks;
+    const int tpi = tiles_h * tiles_w;
+    const int p_first = m_blk * kTilesPerCta;
+    const int p_last = min(P, p_first + kTilesPerCta) - 1;
+    const long long plane = static_cast<long long>(H) * W;
+    const uintptr_t lim = reinterpret_cast<uintptr_t>(x_end) & ~uintptr_t(15);
 
     if (tid == 0) {
         for (int i = 0; i < kStages; ++i) {
             mbar_init(&full[i], kProducers + 1);
             mbar_init(&empty[i], 1);
+            mbar_init(&sfull[i], 1);
+            mbar_init(&sempty[i], kProducers);
         }
         mbar_init(tfull, 1);
         *abort_flag = 0;
+        // images covered by this CTA's tiles and the input rows each needs
+        const int na = p_first / tpi, nb = p_last / tpi;
+        seg->nseg = nb - na + 1;
+        seg->n_first = na;
+        int off = 0;
+        for (int s = 0; s <= nb - na; ++s) {
+            const int n = na + s;
+            const int pa = max(p_first, n * tpi) - n * tpi, pb = min(p_last, n * tpi + tpi - 1) - n * tpi;
+            const int tha = pa / tiles_w, thb = pb / tiles_w;
+            const int ylo = max(0, tha * 2 - pad_h), yhi = min(H, thb * 2 - pad_h + 4);
+            seg->ylo[s] = ylo;
+            seg->yhi[s] = max(ylo, yhi);
+            seg->off[s] = off;
+            off += (max(0, yhi - ylo) * W * 2 + 16 + 15) / 16 * 16;
+        }
         fence_barrier_init();
     }
     if (warp == 8) tmem_alloc(tmem_slot, 512);
@@ -87,16 +125,49 @@ __global__ void __launch_bounds__(kThreads, 1)
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem_base = *tmem_slot;
+    if (seg->nseg > kMaxSeg) {  // host sizing guarantees this never happens
+        if (tid == 0) record_error(err, ERR_SITE_CONFIG);
+        __syncthreads();
+        if (warp == 8) tmem_dealloc(tmem_base, 512);
+        return;
+    }
+
+    // staging of chunk `c` (16 channels) into buffer c % nbuf, issued by thread 0
+    auto issue_stage = [&](int c) {
+        const int bsel = c % nbuf;
+        unsigned char* buf = stg + bsel * (kChunk * stg_ch_bytes);
+        uint32_t total = 0;
+        for (int pass = 0; pass < 2; ++pass) {
+            if (pass == 1) mbar_arrive_expect_tx(&sfull[bsel], total);
+            for (int j = 0; j < kChunk; ++j) {
+                const int ch = c * kChunk + j;
+                if (ch >= C) break;
+                for (int s = 0; s < seg->nseg; ++s) {
+                    const int rows = seg->yhi[s] - seg->ylo[s];
+                    if (rows <= 0) continue;
+                    const uintptr_t a = reinterpret_cast<uintptr_t>(
+                        x + (static_cast<long long>(seg->n_first + s) * C + ch) * plane +
+                        static_cast<long long>(seg->ylo[s]) * W);
+                    const uintptr_t a16 = a & ~uintptr_t(15);
+                    const uintptr_t b16 = min_uptr((a + static_cast<uintptr_t>(rows) * W * 2 + 15) & ~uintptr_t(15), lim);
+                    if (b16 <= a16) continue;
+                    if (pass == 0)
+                        total += static_cast<uint32_t>(b16 - a16);
+                    else
+                        bulk_g2s(buf + j * stg_ch_bytes + seg->off[s], reinterpret_cast<const void*>(a16),
+                                 static_cast<uint32_t>(b16 - a16), &sfull[bsel]);
+                }
+            }
+        }
+    };
 
     if (warp == 8) {
         if (lane == 0) {
             tma_prefetch_desc(&tmU);
             auto issue_tma = [&](int chunk) {
                 const int s = chunk & 1;
-                unsigned char* b = smem + s * kStageBytes + kABytes;
                 mbar_arrive_expect_tx(&full[s], kBBytes);
-                tma_load_3d(b, &tmU, &full[s], chunk * kChunk, n_blk * kOcPerCta, 0);
-                tma_load_3d(b + kBHalf, &tmU, &full[s], chunk * kChunk + 8, n_blk * kOcPerCta, 0);
+                tma_load_4d(smem + s * kStageBytes + kABytes, &tmU, &full[s], 0, n_blk * kOcPerCta, chunk * 2, 0);
             };
             issue_tma(0);
             if (c_chunks > 1) issue_tma(1);
@@ -109,7 +180,7 @@ __global__ void __launch_bounds__(kThreads, 1)
 #pragma unroll
                 for (int e = 0; e < kElems; ++e) {
                     const uint64_t ad = make_smem_desc(a_base + e * (kTilesPerCta * 16), kAHalf, 128, Swz::None);
-                    const uint64_t bd = make_smem_desc(b_base + e * (kOcPerCta * 16), kBHalf, 128, Swz::None);
+                    const uint64_t bd = make_smem_desc(b_base + e * (2 * kOcPerCta * 16), kOcPerCta * 16, 128, Swz::None);
                     tc_mma_f16(tmem_base + e * kOcPerCta, ad, bd, kIdesc, c > 0 ? 1u : 0u);
                 }
                 tc_commit(&empty[s]);
@@ -123,46 +194,60 @@ __global__ void __launch_bounds__(kThreads, 1)
             if (!*abort_flag) tc_commit(tfull);
         }
     } else {
-        // ---- producers: one tile row and 8 channels of every chunk per thread
+        // ---- producers: one tile and 8 channels of every chunk per thread,
+        //      lanes over consecutive tiles
         const int r = tid & 127;
         const int hsel = tid >> 7;
-        const int p = m_blk * kTilesPerCta + r;
+        const int p = p_first + r;
         const bool pvalid = p < P;
         int n = 0, th = 0, tw = 0;
         if (pvalid) {
-            const int tpi = tiles_h * tiles_w;
             n = p / tpi;
             const int rem = p - n * tpi;
             th = rem / tiles_w;
             tw = rem - th * tiles_w;
         }
+        const int s_idx = pvalid ? n - seg->n_first : 0;
+        const int ylo = seg->ylo[s_idx], yhi = seg->yhi[s_idx], soff = seg->off[s_idx];
         const int y0 = th * 2 - pad_h, x0 = tw * 2 - pad_w;
         bool rv[4], cv[4];
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
-            rv[i] = pvalid && (y0 + i >= 0) && (y0 + i < H);
+            rv[i] = pvalid && (y0 + i >= ylo) && (y0 + i < yhi);
             cv[i] = (x0 + i >= 0) && (x0 + i < W);
         }
-        const long long plane = static_cast<long long>(H) * W;
-        const __half* img = x + static_cast<long long>(n) * C * plane + static_cast<long long>(y0) * W + x0;
+        const long long row0 = static_cast<long long>(y0 - ylo) * W + x0;  // patch origin within the staged rows
 
+        if (tid == 0)
+            for (int c = 0; c < nbuf && c < c_chunks; ++c) issue_stage(c);
         bool ok = true;
         for (int c = 0; c < c_chunks && ok; ++c) {
             const int s = c & 1;
-            if (!mbar_wait(&empty[s], ((c >> 1) & 1) ^ 1, abort_flag, err, ERR_SITE_EMPTY)) {
+            const int bsel = c % nbuf;
+            const uint32_t bpar = (c / nbuf) & 1;
+            if (!mbar_wait(&sfull[bsel], bpar, abort_flag, err, ERR_SITE_FULL)) {
                 ok = false;
                 break;
             }
+            const unsigned char* buf = stg + bsel * (kChunk * stg_ch_bytes);
             uint32_t pk[kElems][4];
 #pragma unroll
             for (int j2 = 0; j2 < 4; ++j2) {
                 float v[2][16];
 #pragma unroll
                 for (int h = 0; h < 2; ++h) {
-                    const int ch = c * kChunk + hsel * 8 + j2 * 2 + h;
-                    float d[16];
+                    const int jl = hsel * 8 + j2 * 2 + h;
+                    const int ch = c * kChunk + jl;
                     const bool chv = ch < C;
-                    const __half* src = img + static_cast<long long>(ch) * plane;
+                    const __half* gsrc = x + (static_cast<long long>(n) * C + ch) * plane;
+                    const uintptr_t a = reinterpret_cast<uintptr_t>(gsrc + static_cast<long long>(ylo) * W);
+                    // rows staged whole unless they run into the input's last
+                    // partial 16-byte block (then read from global memory)
+                    const bool staged = a + static_cast<uintptr_t>(yhi - ylo) * W * 2 <= lim;
+                    const __half* src =
+                        (staged ? reinterpret_cast<const __half*>(buf + jl * stg_ch_bytes + soff + (a & 15))
+                                : gsrc + static_cast<long long>(ylo) * W) + row0;
+                    float d[16];
 #pragma unroll
                     for (int i = 0; i < 4; ++i)
 #pragma unroll
@@ -172,6 +257,18 @@ __global__ void __launch_bounds__(kThreads, 1)
                 }
 #pragma unroll
                 for (int e = 0; e < kElems; ++e) pk[e][j2] = OpT<BF16>::pack(v[0][e], v[1][e]);
+            }
+            mbar_arrive(&sempty[bsel]);  // this thread is done reading the staged rows
+            if (tid == 0 && c + nbuf < c_chunks) {
+                if (!mbar_wait(&sempty[bsel], bpar, abort_flag, err, ERR_SITE_EMPTY)) {
+                    ok = false;
+                    break;
+                }
+                issue_stage(c + nbuf);
+            }
+            if (!mbar_wait(&empty[s], ((c >> 1) & 1) ^ 1, abort_flag, err, ERR_SITE_EMPTY)) {
+                ok = false;
+                break;
             }
             unsigned char* a = smem + s * kStageBytes + hsel * kAHalf + r * 16;
 #pragma unroll
@@ -187,11 +284,10 @@ __global__ void __launch_bounds__(kThreads, 1)
             const int quarter = warp & 3;
             const int chalf = warp >> 2;
             const int row = quarter * 32 + lane;
-            const int pe = m_blk * kTilesPerCta + row;
+            const int pe = p_first + row;
             int en = 0, eth = 0, etw = 0;
             const bool pev = pe < P;
             if (pev) {
-                const int tpi = tiles_h * tiles_w;
                 en = pe / tpi;
                 const int rem = pe - en * tpi;
                 eth = rem / tiles_w;
@@ -231,10 +327,13 @@ __global__ void __launch_bounds__(kThreads, 1)
 #pragma unroll
                         for (int a = 0; a < 2; ++a) {
                             if (oh0 + a >= OH) continue;
-#pragma unroll
-                            for (int b = 0; b < 2; ++b)
-                                if (ow0 + b < OW)
-                                    o[static_cast<long long>(oh0 + a) * OW + ow0 + b] = __float2half_rn(y[q][a * 2 + b]);
+                            __half* dst = o + static_cast<long long>(oh0 + a) * OW + ow0;
+                            if (ow0 + 1 < OW && (reinterpret_cast<uintptr_t>(dst) & 3) == 0) {
+                                *reinterpret_cast<__half2*>(dst) = __floats2half2_rn(y[q][a * 2], y[q][a * 2 + 1]);
+                            } else {
+                                dst[0] = __float2half_rn(y[q][a * 2]);
+                                if (ow0 + 1 < OW) dst[1] = __float2half_rn(y[q][a * 2 + 1]);
+                            }
                         }
                     }
                 }
@@ -255,36 +354,74 @@ __global__ void __launch_bounds__(kThreads, 1)
     }
 }
 
+// Bytes of staged input per channel: the largest over all CTAs of the sum,
+// over the images its 128 tiles touch, of the rows those tiles need.
+int staging_bytes_per_channel(const Geom& g, int* max_segments) {
+    const int tpi = g.tiles_h * g.tiles_w;
+    const long long blocks = (g.P + kTilesPerCta - 1) / kTilesPerCta;
+    long long best = 0;
+    int segs = 0;
+    // the pattern repeats every tpi tiles; one period of block starts suffices
+    const long long lim = std::min<long long>(blocks, static_cast<long long>(tpi) + 1);
+    for (long long b = 0; b < lim; ++b) {
+        const long long pf = b * kTilesPerCta, pl = std::min<long long>(g.P, pf + kTilesPerCta) - 1;
+        const long long na = pf / tpi, nb = pl / tpi;
+        long long bytes = 0;
+        for (long long n = na; n <= nb; ++n) {
+            const long long pa = std::max(pf, n * tpi) - n * tpi, pb = std::min(pl, n * tpi + tpi - 1) - n * tpi;
+            const int tha = static_cast<int>(pa / g.tiles_w), thb = static_cast<int>(pb / g.tiles_w);
+            const int ylo = std::max(0, tha * 2 - g.pad_h), yhi = std::min(g.h, thb * 2 - g.pad_h + 4);
+            bytes += (std::max(0, yhi - ylo) * 2LL * g.w + 16 + 15) / 16 * 16;
+        }
+        best = std::max(best, bytes);
+        segs = std::max(segs, static_cast<int>(nb - na + 1));
+    }
+    *max_segments = segs;
+    return static_cast<int>(std::min<long long>(best, 1 << 30));
+}
+
 }  // namespace
 
 cudaError_t plan_fused2x3(FusedPlan& fp, OpType op, const Geom& g, const void* U) {
     if (g.m != 2) return cudaErrorInvalidValue;
+    int segs = 0;
+    fp.stg_ch_bytes = staging_bytes_per_channel(g, &segs);
+    // two staging buffers when they fit (copies run a chunk ahead), else one
+    fp.nbuf = 2;
+    fp.smem_bytes = kSmemFixed + fp.nbuf * kChunk * fp.stg_ch_bytes;
+    if (fp.smem_bytes > 227 * 1024) {
+        fp.nbuf = 1;
+        fp.smem_bytes = kSmemFixed + kChunk * fp.stg_ch_bytes;
+    }
+    if (segs > kMaxSeg || fp.smem_bytes > 227 * 1024) return cudaErrorNotSupported;
     fp.op = op;
     fp.m_blocks = static_cast<int>((g.P + kTilesPerCta - 1) / kTilesPerCta);
     fp.n_blocks = (g.k + kOcPerCta - 1) / kOcPerCta;
     fp.c_chunks = (g.c + kChunk - 1) / kChunk;
-    fp.smem_bytes = kSmem;
     const CUtensorMapDataType dt = op == OpType::BF16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT16;
-    cuuint64_t dims[3] = {static_cast<cuuint64_t>(g.cp), static_cast<cuuint64_t>(g.k), 16};
-    cuuint64_t strides[2] = {static_cast<cuuint64_t>(g.cp) * 2, static_cast<cuuint64_t>(g.k) * g.cp * 2};
-    cuuint32_t box[3] = {8, kOcPerCta, 16};
-    if (encode_tiled(&fp.tmU, dt, 3, const_cast<void*>(U), dims, strides, box, CU_TENSOR_MAP_SWIZZLE_NONE) !=
+    // U[16][CG][K][8]: box of 8 channels x 32 output channels x 2 granules x 16 elements
+    const cuuint64_t CG = static_cast<cuuint64_t>(g.cp / 8);
+    cuuint64_t dims[4] = {8, static_cast<cuuint64_t>(g.k), CG, 16};
+    cuuint64_t strides[3] = {16, static_cast<cuuint64_t>(g.k) * 16, CG * static_cast<cuuint64_t>(g.k) * 16};
+    cuuint32_t box[4] = {8, kOcPerCta, 2, 16};
+    if (encode_tiled(&fp.tmU, dt, 4, const_cast<void*>(U), dims, strides, box, CU_TENSOR_MAP_SWIZZLE_NONE) !=
         CUDA_SUCCESS)
         return cudaErrorInvalidValue;
     return cudaSuccess;
 }
 
-cudaError_t launch_fused2x3(const FusedPlan& fp, const Geom& g, const void* x, void* out, DevErr* err,
-                            cudaStream_t stream) {
+cudaError_t launch_fused2x3(const FusedPlan& fp, const Geom& g, const void* x, const void* x_end, void* out,
+                            DevErr* err, cudaStream_t stream) {
     if (g.P > 0x7fffffffLL) return cudaErrorInvalidValue;
     const long long blocks = static_cast<long long>(fp.m_blocks) * fp.n_blocks;
     if (blocks > 0x7fffffffLL) return cudaErrorInvalidValue;
     auto kern = fp.op == OpType::BF16 ? fused2x3_kernel<true> : fused2x3_kernel<false>;
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmem);
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, fp.smem_bytes);
     if (e != cudaSuccess) return e;
-    kern<<<static_cast<unsigned>(blocks), kThreads, kSmem, stream>>>(
-        static_cast<const __half*>(x), fp.tmU, static_cast<__half*>(out), g.c, g.h, g.w, g.k, g.pad_h, g.pad_w, g.oh,
-        g.ow, g.tiles_h, g.tiles_w, static_cast<int>(g.P), fp.c_chunks, fp.n_blocks, err);
+    kern<<<static_cast<unsigned>(blocks), kThreads, fp.smem_bytes, stream>>>(
+        static_cast<const __half*>(x), static_cast<const __half*>(x_end), fp.tmU, static_cast<__half*>(out), g.c, g.h,
+        g.w, g.k, g.pad_h, g.pad_w, g.oh, g.ow, g.tiles_h, g.tiles_w, static_cast<int>(g.P), fp.c_chunks, fp.n_blocks,
+        fp.stg_ch_bytes, fp.nbuf, err);
     return cudaGetLastError();
 }
 

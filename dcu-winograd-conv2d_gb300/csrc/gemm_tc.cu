@@ -7,13 +7,14 @@
 // the operands stored K-major.
 //
 // Design (one persistent CTA per SM, 192 threads):
-//   warp 0      TMA producer: 128x64 V tile + BNx64 U tile per stage
-//               (128-byte swizzle), S-stage mbarrier ring;
+//   warp 0      TMA producer: 128 tiles x 64 channels of V plus BN x 64 of U
+//               per stage, as 4-D boxes of 8 granules (16-byte rows) that land
+//               in the canonical no-swizzle K-major layout; S-stage ring;
 //   warp 1      allocates TMEM and issues tcgen05.mma (M=128, N=BN, K=16)
 //               from one thread; accumulators double-buffered in TMEM so the
 //               epilogue of one output tile overlaps the main loop of the next;
 //   warps 2-5   epilogue: tcgen05.ld 32 lanes x 16 columns, convert, 16-byte
-//               stores of M rows (fp16 or fp32).
+//               granule stores of M (a warp writes 512 contiguous bytes).
 // Output tiles are (e, 128-tile block, BN-channel block), handed out round
 // robin; channel blocks of one (e, tile block) are adjacent so the V tile is
 // reused from L2.
@@ -31,7 +32,7 @@ namespace wg {
 namespace {
 
 constexpr int kBM = 128;
-constexpr int kBK = 64;                 // 64 fp16 = one 128-byte swizzle row
+constexpr int kBK = 64;                 // 8 granules of 8 channels per stage
 constexpr int kTileABytes = kBM * kBK * 2;
 
 template <int BN>
@@ -43,45 +44,52 @@ struct GemmCfg {
     static constexpr int kSmem = kStages * kStageBytes + 1024 /*align*/ + 256 /*barriers*/;
 };
 
+// Epilogue stores of 16 accumulator columns (output channels k0..k0+15) of
+// one tile row p into the granule layout.
 template <class MT>
-__device__ __forceinline__ void store16(MT* dst, const uint32_t (&r)[16], int valid8);
+__device__ __forceinline__ void store16(MT* Mw, const uint32_t (&r)[16], long long P, long long p, int k0, int kg_count,
+                                        int e);
 
-// fp16 M: 16 values = two 16-byte stores; `valid8` = number of 8-wide groups inside Kp.
+// fp16 M[e][Kp/8][P][8]: two granules
 template <>
-__device__ __forceinline__ void store16<__half>(__half* dst, const uint32_t (&r)[16], int valid8) {
+__device__ __forceinline__ void store16<__half>(__half* Mw, const uint32_t (&r)[16], long long P, long long p, int k0,
+                                                int kg_count, int e) {
     uint32_t h[8];
 #pragma unroll
     for (int i = 0; i < 8; ++i) {
         __half2 v = __floats2half2_rn(__uint_as_float(r[2 * i]), __uint_as_float(r[2 * i + 1]));
         h[i] = *reinterpret_cast<uint32_t*>(&v);
     }
-    if (valid8 > 0) *reinterpret_cast<uint4*>(dst) = make_uint4(h[0], h[1], h[2], h[3]);
-    if (valid8 > 1) *reinterpret_cast<uint4*>(dst + 8) = make_uint4(h[4], h[5], h[6], h[7]);
+    const int g0 = k0 / 8;
+#pragma unroll
+    for (int j = 0; j < 2; ++j)
+        if (g0 + j < kg_count)
+            *reinterpret_cast<uint4*>(Mw + ((static_cast<long long>(e) * kg_count + g0 + j) * P + p) * 8) =
+                make_uint4(h[4 * j], h[4 * j + 1], h[4 * j + 2], h[4 * j + 3]);
 }
 
+// fp32 M[e][Kp/4][P][4]: four granules
 template <>
-__device__ __forceinline__ void store16<float>(float* dst, const uint32_t (&r)[16], int valid8) {
-    if (valid8 > 0) {
-        *reinterpret_cast<uint4*>(dst) = make_uint4(r[0], r[1], r[2], r[3]);
-        *reinterpret_cast<uint4*>(dst + 4) = make_uint4(r[4], r[5], r[6], r[7]);
-    }
-    if (valid8 > 1) {
-        *reinterpret_cast<uint4*>(dst + 8) = make_uint4(r[8], r[9], r[10], r[11]);
-        *reinterpret_cast<uint4*>(dst + 12) = make_uint4(r[12], r[13], r[14], r[15]);
-    }
+__device__ __forceinline__ void store16<float>(float* Mw, const uint32_t (&r)[16], long long P, long long p, int k0,
+                                               int kg_count, int e) {
+    const int g0 = k0 / 4;
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+        if (g0 + j < kg_count)
+            *reinterpret_cast<uint4*>(Mw + ((static_cast<long long>(e) * kg_count + g0 + j) * P + p) * 4) =
+                make_uint4(r[4 * j], r[4 * j + 1], r[4 * j + 2], r[4 * j + 3]);
 }
 
 template <int BN, bool BF16, class MT>
 __global__ void __launch_bounds__(192, 1)
     wino_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
-                     MT* __restrict__ Mw, int P, int Kp, int m_blocks, int n_blocks, int k_blocks, int total_tiles,
-                     DevErr* err) {
+                     MT* __restrict__ Mw, int P, int kg_count, int m_blocks, int n_blocks, int k_blocks,
+                     int total_tiles, DevErr* err) {
     using Cfg = GemmCfg<BN>;
     constexpr int S = Cfg::kStages;
     constexpr uint32_t kIdesc = make_idesc_f16(kBM, BN, BF16);
 
     extern __shared__ __align__(1024) unsigned char smem_raw[];
-    // 1024-byte alignment for the 128-byte swizzle atoms
     unsigned char* smem = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     unsigned char* sA = smem;
     unsigned char* sB = smem + S * kTileABytes;
@@ -131,8 +139,8 @@ __global__ void __launch_bounds__(192, 1)
                         break;
                     }
                     mbar_arrive_expect_tx(&full[stage], Cfg::kStageBytes);
-                    tma_load_3d(sA + stage * kTileABytes, &tmA, &full[stage], kb * kBK, mb * kBM, e);
-                    tma_load_3d(sB + stage * Cfg::kTileB, &tmB, &full[stage], kb * kBK, nb * BN, e);
+                    tma_load_4d(sA + stage * kTileABytes, &tmA, &full[stage], 0, mb * kBM, kb * 8, e);
+                    tma_load_4d(sB + stage * Cfg::kTileB, &tmB, &full[stage], 0, nb * BN, kb * 8, e);
                     if (++stage == S) {
                         stage = 0;
                         phase ^= 1u;
@@ -160,10 +168,11 @@ __global__ void __launch_bounds__(192, 1)
                     tc_fence_after();
                     const uint32_t a_base = smem_u32(sA + stage * kTileABytes);
                     const uint32_t b_base = smem_u32(sB + stage * Cfg::kTileB);
+                    // K = 16 per MMA = 2 granules: core matrices at +0 and +LBO
 #pragma unroll
                     for (int k = 0; k < kBK / 16; ++k) {
-                        const uint64_t ad = make_smem_desc(a_base + k * 32, 16, 1024, Swz::B128);
-                        const uint64_t bd = make_smem_desc(b_base + k * 32, 16, 1024, Swz::B128);
+                        const uint64_t ad = make_smem_desc(a_base + k * (2 * kBM * 16), kBM * 16, 128, Swz::None);
+                        const uint64_t bd = make_smem_desc(b_base + k * (2 * BN * 16), BN * 16, 128, Swz::None);
                         tc_mma_f16(d_tmem, ad, bd, kIdesc, (kb | k) != 0 ? 1u : 0u);
                     }
                     tc_commit(&empty[stage]);
@@ -194,18 +203,13 @@ __global__ void __launch_bounds__(192, 1)
             if (!mbar_wait(&tfull[acc], acc_phase, abort_flag, err, ERR_SITE_TMEM_FULL)) break;
             tc_fence_after();
             const int p = mb * kBM + row;
-            MT* dst_row = Mw + (static_cast<long long>(e) * P + p) * Kp;
             const uint32_t taddr = tmem_base + (static_cast<uint32_t>(quarter * 32) << 16) + static_cast<uint32_t>(acc * BN);
 #pragma unroll 1
             for (int c0 = 0; c0 < BN; c0 += 16) {
                 uint32_t r[16];
                 tmem_ld_x16(taddr + c0, r);
                 tc_wait_ld();
-                const int k0 = nb * BN + c0;
-                if (p < P && k0 < Kp) {
-                    const int valid8 = (Kp - k0) >= 16 ? 2 : 1;
-                    store16<MT>(dst_row + k0, r, valid8);
-                }
+                if (p < P) store16<MT>(Mw, r, P, p, nb * BN + c0, kg_count, e);
             }
             tc_fence_before();
             mbar_arrive(&tempty[acc]);
@@ -235,7 +239,8 @@ cudaError_t gemm_launch(const GemmPlan& gp, void* Mw, DevErr* err, cudaStream_t 
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, GemmCfg<BN>::kSmem);
     if (e != cudaSuccess) return e;
     const int total = gp.E * gp.m_blocks * gp.n_blocks;
-    kern<<<gp.grid, 192, GemmCfg<BN>::kSmem, s>>>(gp.tmA, gp.tmB, static_cast<MT*>(Mw), gp.P, gp.Kp, gp.m_blocks,
+    const int kg_count = gp.m_fp32 ? gp.Kp / 4 : gp.Kp / 8;
+    kern<<<gp.grid, 192, GemmCfg<BN>::kSmem, s>>>(gp.tmA, gp.tmB, static_cast<MT*>(Mw), gp.P, kg_count, gp.m_blocks,
                                                   gp.n_blocks, gp.k_blocks, total, err);
     return cudaGetLastError();
 }
@@ -295,19 +300,22 @@ cudaError_t plan_gemm(GemmPlan& gp, OpType op, int E, long long P, int K, int Kp
     gp.grid = static_cast<int>(std::min<long long>(total, num_sms));
     gp.smem_bytes = gemm_smem(bn);
     const CUtensorMapDataType dt = op == OpType::BF16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT16;
+    const cuuint64_t CG = static_cast<cuuint64_t>(Cp / 8);
     {
-        cuuint64_t dims[3] = {static_cast<cuuint64_t>(Cp), static_cast<cuuint64_t>(P), static_cast<cuuint64_t>(E)};
-        cuuint64_t strides[2] = {static_cast<cuuint64_t>(Cp) * 2, static_cast<cuuint64_t>(P) * Cp * 2};
-        cuuint32_t box[3] = {kBK, kBM, 1};
-        if (encode_tiled(&gp.tmA, dt, 3, const_cast<void*>(V), dims, strides, box, CU_TENSOR_MAP_SWIZZLE_128B) !=
+        // V[E][CG][P][8]: box of 8 granules x 128 tiles
+        cuuint64_t dims[4] = {8, static_cast<cuuint64_t>(P), CG, static_cast<cuuint64_t>(E)};
+        cuuint64_t strides[3] = {16, static_cast<cuuint64_t>(P) * 16, CG * static_cast<cuuint64_t>(P) * 16};
+        cuuint32_t box[4] = {8, kBM, 8, 1};
+        if (encode_tiled(&gp.tmA, dt, 4, const_cast<void*>(V), dims, strides, box, CU_TENSOR_MAP_SWIZZLE_NONE) !=
             CUDA_SUCCESS)
             return cudaErrorInvalidValue;
     }
     {
-        cuuint64_t dims[3] = {static_cast<cuuint64_t>(Cp), static_cast<cuuint64_t>(K), static_cast<cuuint64_t>(E)};
-        cuuint64_t strides[2] = {static_cast<cuuint64_t>(Cp) * 2, static_cast<cuuint64_t>(K) * Cp * 2};
-        cuuint32_t box[3] = {kBK, static_cast<cuuint32_t>(bn), 1};
-        if (encode_tiled(&gp.tmB, dt, 3, const_cast<void*>(U), dims, strides, box, CU_TENSOR_MAP_SWIZZLE_128B) !=
+        // U[E][CG][K][8]: box of 8 granules x BN output channels
+        cuuint64_t dims[4] = {8, static_cast<cuuint64_t>(K), CG, static_cast<cuuint64_t>(E)};
+        cuuint64_t strides[3] = {16, static_cast<cuuint64_t>(K) * 16, CG * static_cast<cuuint64_t>(K) * 16};
+        cuuint32_t box[4] = {8, static_cast<cuuint32_t>(bn), 8, 1};
+        if (encode_tiled(&gp.tmB, dt, 4, const_cast<void*>(U), dims, strides, box, CU_TENSOR_MAP_SWIZZLE_NONE) !=
             CUDA_SUCCESS)
             return cudaErrorInvalidValue;
     }

@@ -37,8 +37,8 @@ struct Geom {
 
 Geom make_geom(int n, int c, int h, int w, int k, int pad_h, int pad_w, int m);
 
-// U[e][K][Cp] = G g G^T, from KCRS fp16 weights; fp32 arithmetic, result in
-// the operand type; zero for c >= C.
+// U[e][Cp/8][K][8] = G g G^T, from KCRS fp16 weights; fp32 arithmetic, result
+// in the operand type; zero for c >= C.
 cudaError_t launch_filter_transform(Xform xf, OpType op, const void* weight, void* U, int K, int C, int Cp,
                                     cudaStream_t stream);
 
@@ -46,17 +46,19 @@ cudaError_t launch_filter_transform(Xform xf, OpType op, const void* weight, voi
 // over the tile's input patch in every channel; 1 for an all-zero patch.
 cudaError_t launch_tile_scale(const Geom& g, const void* x, float* scale, cudaStream_t stream);
 
-// V[e][P][Cp] = B^T d B for images [n0, n0 + g.n) of the input; tile p is
-// counted from image n0 (the caller offsets V).  scale may be null.
-cudaError_t launch_input_transform(Xform xf, OpType op, const Geom& g, const void* x, void* V, const float* scale,
-                                   cudaStream_t stream);
+// V[e][Cp/8][P][8] = B^T d B for the g.n images starting at x (x may point
+// into a larger tensor that ends at x_end; the full tensor must start on a
+// 16-byte boundary).  scale may be null.
+cudaError_t launch_input_transform(Xform xf, OpType op, const Geom& g, const void* x, const void* x_end, void* V,
+                                   const float* scale, DevErr* err, cudaStream_t stream);
 
-// out[N][K][OH][OW] = A^T M A from M[e][P][Kp] (fp16 when m_fp32 is false,
-// else fp32); divides by scale[p] when scale is not null.
+// out[N][K][OH][OW] = A^T M A from M[e][Kp/8][P][8] (fp16, m_fp32 false) or
+// M[e][Kp/4][P][4] (fp32); divides by scale[p] when scale is not null.
 cudaError_t launch_output_transform(Xform xf, bool m_fp32, const Geom& g, const void* Mw, void* out,
                                     const float* scale, cudaStream_t stream);
 
 // ---- tcgen05 batched GEMM: M_e[P][K] = V_e[P][Cp] * U_e[K][Cp]^T -----------
+// (operands and result in the 16-byte granule layouts above)
 struct GemmPlan {
     CUtensorMap tmA;     // V
     CUtensorMap tmB;     // U
@@ -78,13 +80,17 @@ cudaError_t launch_gemm(const GemmPlan& gp, void* Mw, DevErr* err, cudaStream_t 
 struct FusedPlan {
     CUtensorMap tmU;
     int m_blocks, n_blocks, c_chunks;
+    int stg_ch_bytes;    // staged input bytes per channel of one chunk
+    int nbuf;            // staging buffers (2 = copies one chunk ahead)
     int smem_bytes;
     OpType op;
 };
 
+// cudaErrorNotSupported when the staged rows of one CTA do not fit in shared
+// memory (very wide images); the caller then uses the non-fused path.
 cudaError_t plan_fused2x3(FusedPlan& fp, OpType op, const Geom& g, const void* U);
-cudaError_t launch_fused2x3(const FusedPlan& fp, const Geom& g, const void* x, void* out, DevErr* err,
-                            cudaStream_t stream);
+cudaError_t launch_fused2x3(const FusedPlan& fp, const Geom& g, const void* x, const void* x_end, void* out,
+                            DevErr* err, cudaStream_t stream);
 
 // Tensor-map encoder from the driver (resolved once through the runtime).
 CUresult encode_tiled(CUtensorMap* map, CUtensorMapDataType dt, cuuint32_t rank, void* addr, const cuuint64_t* dims,
