@@ -179,10 +179,10 @@ int Plan::build(const problem_t* pr, const conv2d_options_t* opt_in) {
 
     // one workspace: U | V | M | scale | device error word (256-byte aligned parts)
     auto al = [](long long b) { return (b + 255) / 256 * 256; };
-    const long long bU = al(static_cast<long long>(E) * g.k * g.cp * op_bytes);
+    const long long bU = al(static_cast<long long>(E) * g.kp * g.cp * op_bytes);
     long long bV = 0, bM = 0, bS = 0;
     if (algo != CONV2D_ALGO_2X3_FUSED) {
-        bV = al(static_cast<long long>(E) * Pc * g.cp * op_bytes);
+        bV = al(static_cast<long long>(E) * round_rows(Pc) * g.cp * op_bytes);
         bM = al(static_cast<long long>(E) * Pc * g.kp * (m_fp32 ? 4 : 2));
         if (scaling) bS = al(Pc * 4);
     }

