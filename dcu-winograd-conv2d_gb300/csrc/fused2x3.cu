@@ -244,15 +244,26 @@ __global__ void __launch_bounds__(kThreads, 1)
                     // rows staged whole unless they run into the input's last
                     // partial 16-byte block (then read from global memory)
                     const bool staged = a + static_cast<uintptr_t>(yhi - ylo) * W * 2 <= lim;
-                    const __half* src =
-                        (staged ? reinterpret_cast<const __half*>(buf + jl * stg_ch_bytes + soff + (a & 15))
-                                : gsrc + static_cast<long long>(ylo) * W) + row0;
                     float d[16];
+                    // staged rows through shared-memory loads; the rare rows
+                    // that run into the input's last partial 16-byte block
+                    // through global loads (separate code, not one pointer)
+                    if (staged) {
+                        const __half* src =
+                            reinterpret_cast<const __half*>(buf + jl * stg_ch_bytes + soff + (a & 15)) + row0;
 #pragma unroll
-                    for (int i = 0; i < 4; ++i)
+                        for (int i = 0; i < 4; ++i)
 #pragma unroll
-                        for (int j = 0; j < 4; ++j)
-                            d[i * 4 + j] = (chv && rv[i] && cv[j]) ? __half2float(src[i * W + j]) : 0.f;
+                            for (int j = 0; j < 4; ++j)
+                                d[i * 4 + j] = (chv && rv[i] && cv[j]) ? __half2float(src[i * W + j]) : 0.f;
+                    } else {
+                        const __half* src = gsrc + static_cast<long long>(ylo) * W + row0;
+#pragma unroll
+                        for (int i = 0; i < 4; ++i)
+#pragma unroll
+                            for (int j = 0; j < 4; ++j)
+                                d[i * 4 + j] = (chv && rv[i] && cv[j]) ? __half2float(src[i * W + j]) : 0.f;
+                    }
                     input_tile_transform<F2>(d, v[h]);
                 }
 #pragma unroll

@@ -218,22 +218,30 @@ __global__ void __launch_bounds__(kInThreads, 2) input_transform_kernel(
             // rows staged whole unless they run into the last partial 16-byte
             // block of the input (then read from global memory)
             const bool staged = a + static_cast<uintptr_t>(rows) * W * 2 <= lim;
-            const __half* src = staged ? sm : gsrc + static_cast<long long>(ylo) * W;
+            const __half* gsrc_rows = gsrc + static_cast<long long>(ylo) * W;
             float t[A * A];
+            // two copies of the column loop so the staged path compiles to
+            // shared-memory loads (a pointer that may be either would not)
+            auto columns = [&](const __half* src) {
 #pragma unroll
-            for (int j = 0; j < A; ++j) {
-                const int xx = x0 + j;
-                const bool xv = cv && xx >= 0 && xx < W;
-                float col[A];
+                for (int j = 0; j < A; ++j) {
+                    const int xx = x0 + j;
+                    const bool xv = cv && xx >= 0 && xx < W;
+                    float col[A];
 #pragma unroll
-                for (int i = 0; i < A; ++i) {
-                    const int y = y0 + i;
-                    float v = 0.f;
-                    if (xv && y >= ylo && y < yhi) v = __half2float(src[(y - ylo) * W + xx]);
-                    col[i] = v * s;
+                    for (int i = 0; i < A; ++i) {
+                        const int y = y0 + i;
+                        float v = 0.f;
+                        if (xv && y >= ylo && y < yhi) v = __half2float(src[(y - ylo) * W + xx]);
+                        col[i] = v * s;
+                    }
+                    TF::bt(col, 1, &t[j], A);
                 }
-                TF::bt(col, 1, &t[j], A);
-            }
+            };
+            if (staged)
+                columns(sm);
+            else
+                columns(gsrc_rows);
 #pragma unroll
             for (int i = 0; i < A; ++i) {
                 float row[A];
