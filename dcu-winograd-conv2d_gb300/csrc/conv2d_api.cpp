@@ -208,7 +208,7 @@ int Plan::build(const problem_t* pr, const conv2d_options_t* opt_in) {
         if (ce != cudaSuccess) return cuda_fail(ce, "fused plan");
         launches = 1;
         info_grid = static_cast<unsigned>(fused.m_blocks * fused.n_blocks);
-        info_threads = 288;
+        info_threads = 320;
         info_smem = fused.smem_bytes;
     } else {
         const int bn = opt.gemm_bn ? opt.gemm_bn : default_bn(g.k);

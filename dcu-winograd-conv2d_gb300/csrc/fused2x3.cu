@@ -15,6 +15,8 @@
 //     TMA per chunk;
 //   * warp 8 issues the 16 tcgen05.mma (M=128, N=32, K=16) per chunk from one
 //     thread, accumulating all 16 elements in the 512 TMEM columns;
+//   * warp 9 issues the staging copies (so no producer warp diverges to
+//     wait for the others);
 //   * after the last chunk warps 0-7 read TMEM, apply A^T m A and write the
 //     2x2 outputs to NCHW.
 // Every wait is bounded (wg_ptx.cuh).
@@ -42,7 +44,7 @@ constexpr int kStageBytes = kABytes + kBBytes;           // 80 KB
 constexpr int kStages = 2;
 constexpr int kMaxSeg = 16;                              // images one CTA's tiles may span
 constexpr int kProducers = 256;
-constexpr int kThreads = kProducers + 32;
+constexpr int kThreads = kProducers + 64;  // + MMA warp + staging-loader warp
 constexpr int kSmemFixed = kStages * kStageBytes + 1024 /*align*/ + 512 /*barriers, segment table*/;
 
 template <bool BF16> struct OpT;
@@ -132,7 +134,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         return;
     }
 
-    // staging of chunk `c` (16 channels) into buffer c % nbuf, issued by thread 0
+    // staging of chunk `c` (16 channels) into buffer c % nbuf, issued by the loader warp
     auto issue_stage = [&](int c) {
         const int bsel = c % nbuf;
         unsigned char* buf = stg + bsel * (kChunk * stg_ch_bytes);
@@ -161,7 +163,16 @@ __global__ void __launch_bounds__(kThreads, 1)
         }
     };
 
-    if (warp == 8) {
+    if (warp == 9) {
+        if (lane == 0) {
+            for (int c = 0; c < nbuf && c < c_chunks; ++c) issue_stage(c);
+            for (int c = 0; c + nbuf < c_chunks; ++c) {
+                // buffer c % nbuf is free once every producer has read chunk c
+                if (!mbar_wait(&sempty[c % nbuf], (c / nbuf) & 1, abort_flag, err, ERR_SITE_EMPTY)) break;
+                issue_stage(c + nbuf);
+            }
+        }
+    } else if (warp == 8) {
         if (lane == 0) {
             tma_prefetch_desc(&tmU);
             auto issue_tma = [&](int chunk) {
@@ -218,8 +229,6 @@ __global__ void __launch_bounds__(kThreads, 1)
         }
         const long long row0 = static_cast<long long>(y0 - ylo) * W + x0;  // patch origin within the staged rows
 
-        if (tid == 0)
-            for (int c = 0; c < nbuf && c < c_chunks; ++c) issue_stage(c);
         bool ok = true;
         for (int c = 0; c < c_chunks && ok; ++c) {
             const int s = c & 1;
@@ -270,13 +279,6 @@ __global__ void __launch_bounds__(kThreads, 1)
                 for (int e = 0; e < kElems; ++e) pk[e][j2] = OpT<BF16>::pack(v[0][e], v[1][e]);
             }
             mbar_arrive(&sempty[bsel]);  // this thread is done reading the staged rows
-            if (tid == 0 && c + nbuf < c_chunks) {
-                if (!mbar_wait(&sempty[bsel], bpar, abort_flag, err, ERR_SITE_EMPTY)) {
-                    ok = false;
-                    break;
-                }
-                issue_stage(c + nbuf);
-            }
             if (!mbar_wait(&empty[s], ((c >> 1) & 1) ^ 1, abort_flag, err, ERR_SITE_EMPTY)) {
                 ok = false;
                 break;
