@@ -195,11 +195,11 @@ __global__ void __launch_bounds__(kThreads, 1)
                     tc_mma_f16(tmem_base + e * kOcPerCta, ad, bd, kIdesc, c > 0 ? 1u : 0u);
                 }
                 tc_commit(&empty[s]);
-                if (c >= 1 && c + 1 < c_chunks) {
-                    // stage of chunk c+1 is free once the MMAs of chunk c-1 are done
-                    const int u = (c + 1) >> 1;
-                    if (!mbar_wait(&empty[(c + 1) & 1], (u - 1) & 1, abort_flag, err, ERR_SITE_EMPTY)) break;
-                    issue_tma(c + 1);
+                if (c + 2 < c_chunks) {
+                    // the filter tile of chunk c+2 reuses this stage: issue it as
+                    // soon as these MMAs retire, a whole chunk ahead of its use
+                    if (!mbar_wait(&empty[s], (c >> 1) & 1, abort_flag, err, ERR_SITE_EMPTY)) break;
+                    issue_tma(c + 2);
                 }
             }
             if (!*abort_flag) tc_commit(tfull);

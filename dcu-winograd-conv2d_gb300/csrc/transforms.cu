@@ -26,7 +26,6 @@
 #include <cuda_fp16.h>
 
 #include <algorithm>
-#include <type_traits>
 
 #include "wg_kernels.h"
 #include "wg_ptx.cuh"
@@ -208,57 +207,41 @@ __global__ void __launch_bounds__(kInThreads, 2) input_transform_kernel(
         const int y0 = (th0 + tr) * M - pad_h, x0 = tw * M - pad_w;
         const float s = scale ? scale[p] : 1.f;
         OutT* dst = V + ((static_cast<long long>(c0 / 8 + g)) * Pp + p) * 8;
-        // per-tile geometry, shared by all 8 channels of the granule
-        const bool interior = y0 >= ylo && y0 + A <= yhi && x0 >= 0 && x0 + A <= W;
-        int rowoff[A];
-        bool rowok[A], colok[A];
-#pragma unroll
-        for (int i = 0; i < A; ++i) {
-            rowoff[i] = (y0 + i - ylo) * W + x0;
-            rowok[i] = y0 + i >= ylo && y0 + i < yhi;
-            colok[i] = x0 + i >= 0 && x0 + i < W;
-        }
         // one channel's 2-D transform: column pass t = B^T d one input column
         // at a time, then the row pass hands each finished value to `put`
         // (d is never held whole)
         auto channel = [&](int c, auto&& put) {
+            const bool cv = c < nch;
+            const __half* gsrc = x + (n * C + c0 + c) * plane;
+            const uintptr_t a = reinterpret_cast<uintptr_t>(gsrc + static_cast<long long>(ylo) * W);
+            const __half* sm = reinterpret_cast<const __half*>(stage + static_cast<size_t>(c) * stride_bytes + (a & 15));
+            // rows staged whole unless they run into the last partial 16-byte
+            // block of the input (then read from global memory)
+            const bool staged = a + static_cast<uintptr_t>(rows) * W * 2 <= lim;
+            const __half* gsrc_rows = gsrc + static_cast<long long>(ylo) * W;
             float t[A * A];
-            if (c >= nch) {
+            // two copies of the column loop so the staged path compiles to
+            // shared-memory loads (a pointer that may be either would not)
+            auto columns = [&](const __half* src) {
 #pragma unroll
-                for (int e = 0; e < A * A; ++e) t[e] = 0.f;
-            } else {
-                const __half* gsrc = x + (n * C + c0 + c) * plane;
-                const uintptr_t a = reinterpret_cast<uintptr_t>(gsrc + static_cast<long long>(ylo) * W);
-                const __half* sm =
-                    reinterpret_cast<const __half*>(stage + static_cast<size_t>(c) * stride_bytes + (a & 15));
-                // rows staged whole unless they run into the last partial
-                // 16-byte block of the input (then read from global memory)
-                const bool staged = a + static_cast<uintptr_t>(rows) * W * 2 <= lim;
-                // separate copies of the column loop: the staged paths compile
-                // to shared-memory loads, interior tiles skip the bounds tests
-                auto columns = [&](const __half* src, auto checked) {
+                for (int j = 0; j < A; ++j) {
+                    const int xx = x0 + j;
+                    const bool xv = cv && xx >= 0 && xx < W;
+                    float col[A];
 #pragma unroll
-                    for (int j = 0; j < A; ++j) {
-                        float col[A];
-#pragma unroll
-                        for (int i = 0; i < A; ++i) {
-                            float v;
-                            if constexpr (decltype(checked)::value)
-                                v = (rowok[i] && colok[j]) ? __half2float(src[rowoff[i] + j]) : 0.f;
-                            else
-                                v = __half2float(src[rowoff[i] + j]);
-                            col[i] = v * s;
-                        }
-                        TF::bt(col, 1, &t[j], A);
+                    for (int i = 0; i < A; ++i) {
+                        const int y = y0 + i;
+                        float v = 0.f;
+                        if (xv && y >= ylo && y < yhi) v = __half2float(src[(y - ylo) * W + xx]);
+                        col[i] = v * s;
                     }
-                };
-                if (staged && interior)
-                    columns(sm, std::false_type{});
-                else if (staged)
-                    columns(sm, std::true_type{});
-                else
-                    columns(gsrc + static_cast<long long>(ylo) * W, std::true_type{});
-            }
+                    TF::bt(col, 1, &t[j], A);
+                }
+            };
+            if (staged)
+                columns(sm);
+            else
+                columns(gsrc_rows);
 #pragma unroll
             for (int i = 0; i < A; ++i) {
                 float row[A];
