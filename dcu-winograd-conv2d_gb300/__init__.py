@@ -48,6 +48,7 @@ EXPORTS = [
     "conv2d_refresh_filter", "conv2d_destroy", "conv2d_get_algo", "conv2d_workspace_bytes",
     "conv2d_launches_per_call", "conv2d_check_device", "conv2d_last_error", "conv2d_last_error_message",
     "conv2d_status_string", "conv2d_select_reference", "conv2d_copy_to_host", "conv2d_fp16_timed",
+    "conv2d_autotune", "conv2d_autotune_clear",
 ]
 
 _lib = None
@@ -96,6 +97,8 @@ def lib():
         L.conv2d_select_reference.argtypes = [ctypes.POINTER(Problem)]
         L.conv2d_copy_to_host.argtypes = [vp, vp, ctypes.c_size_t]
         L.conv2d_fp16_timed.argtypes = [vp, vp, ctypes.POINTER(ctypes.c_float), ctypes.c_int]
+        L.conv2d_autotune.argtypes = [ctypes.POINTER(Problem), ctypes.POINTER(Options), ip, ip]
+        L.conv2d_autotune_clear.restype = None
         _lib = L
     return _lib
 
@@ -199,6 +202,14 @@ class Conv2d:
                 _lib.conv2d_destroy(self.ptr)
         except Exception:
             pass
+
+
+def autotune(problem: Problem, options: Options | None = None):
+    """(algo, gemm_bn) the autotuner picks for this shape (measures once)."""
+    a, b = ctypes.c_int(0), ctypes.c_int(0)
+    _check(lib().conv2d_autotune(ctypes.byref(problem), ctypes.byref(options) if options is not None else None,
+                                 ctypes.byref(a), ctypes.byref(b)))
+    return a.value, b.value
 
 
 def copy_to_host(host_ptr: int, dev_ptr: int, nbytes: int):

@@ -148,7 +148,12 @@ int Plan::build(const problem_t* pr, const conv2d_options_t* opt_in) {
     algo = opt.algo;
     if (algo == CONV2D_ALGO_REFERENCE || algo == CONV2D_ALGO_AUTO)
         algo = select_reference64(pr->n, pr->c, pr->h, pr->w, pr->k, pr->r, pr->s, oh, ow);
-    if (opt.algo == CONV2D_ALGO_AUTO) algo = autotune_pick(*pr, opt, algo);
+    if (opt.algo == CONV2D_ALGO_AUTO) {
+        int a = algo, bn = 0;
+        autotune_choose(*pr, opt, algo, &a, &bn);
+        algo = a;
+        if (bn) opt.gemm_bn = bn;
+    }
     if (algo < 0 || algo > 2) return fail(CONV2D_ERR_INVALID, "bad algorithm");
 
     op = opt.operand_bf16 ? OpType::BF16 : OpType::F16;
@@ -501,6 +506,22 @@ int conv2d_fp16_timed(const void* param_ptr, void* stream, float* kernel_ms, int
     if (ce != cudaSuccess) return -cuda_fail(ce, "stream sync");
     return got;
 }
+
+int conv2d_autotune(const problem_t* problem, const conv2d_options_t* opt, int* algo, int* gemm_bn) {
+    int st = validate_problem(problem);
+    if (st) return st;
+    if (!algo || !gemm_bn) return fail(CONV2D_ERR_INVALID, "null output");
+    conv2d_options_t o;
+    if (opt)
+        o = *opt;
+    else
+        options_default(&o);
+    const unsigned oh = problem->h + 2 * problem->p - 2, ow = problem->w + 2 * problem->q - 2;
+    const int ref = select_reference64(problem->n, problem->c, problem->h, problem->w, problem->k, 3, 3, oh, ow);
+    return autotune_choose(*problem, o, ref, algo, gemm_bn);
+}
+
+void conv2d_autotune_clear(void) { autotune_clear(); }
 
 int conv2d_copy_to_host(void* host_dst, const void* device_src, size_t bytes) {
     if (!host_dst || !device_src) return fail(CONV2D_ERR_INVALID, "null pointer");

@@ -75,7 +75,9 @@ __global__ void __launch_bounds__(kThreads, 1)
                     int stg_ch_bytes, int nbuf, DevErr* err) {
     constexpr uint32_t kIdesc = make_idesc_f16(128, kOcPerCta, BF16);
     extern __shared__ __align__(1024) unsigned char smem_raw[];
-    unsigned char* smem = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    // 1024-byte aligned base by pointer arithmetic (an integer round trip would
+    // hide that this is shared memory and turn every access generic)
+    unsigned char* smem = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
     uint64_t* bars = reinterpret_cast<uint64_t*>(smem + kStages * kStageBytes);
     uint64_t* full = bars;             // [2] producers (256) + TMA expect_tx (1)
     uint64_t* empty = bars + 2;        // [2] MMA commit

@@ -154,6 +154,14 @@ const char* conv2d_status_string(int status);
 /* The reference selection rule evaluated in 64-bit arithmetic (0..2). */
 int conv2d_select_reference(const problem_t* problem);
 
+/* Per-shape choice of algorithm and GEMM output-channel tile, as
+ * CONV2D_ALGO_AUTO makes it: measured on the device the first time a shape is
+ * seen (candidates run on scratch output memory, reading the problem's input
+ * and weights), then cached; WG_CONV2D_TUNE_FILE persists the cache.  The
+ * reference selection is kept unless another candidate is >3% faster. */
+int conv2d_autotune(const problem_t* problem, const conv2d_options_t* opt, int* algo, int* gemm_bn);
+void conv2d_autotune_clear(void);
+
 /* One call with a CUDA event recorded on the stream after every kernel
  * launch; waits, writes each launch's duration (ms, launch order) to
  * kernel_ms and returns the number of launches (negative status on error). */

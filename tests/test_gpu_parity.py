@@ -257,3 +257,20 @@ def test_host_buffer_entry_point(wg):
     op.host(hin.data_ptr(), hout.data_ptr(), torch.cuda.current_stream().cuda_stream)
     _, r64 = O.conv2d_direct(x, wt)
     assert O.rel_errors(hout.numpy(), r64)[0] <= TOL[2]
+
+
+def test_autotune_choice_is_cached_and_correct(wg):
+    x, wt = O.uniform_inputs(21, 2, 64, 24, 24, 96)
+    xt, wtt = torch.from_numpy(x).cuda(), torch.from_numpy(wt).cuda()
+    y = torch.empty((2, 96, 24, 24), dtype=torch.float16, device="cuda")
+    prob = wg.make_problem(xt.data_ptr(), wtt.data_ptr(), y.data_ptr(), 2, 64, 24, 24, 96)
+    wg.lib().conv2d_autotune_clear()
+    a1 = wg.autotune(prob)
+    a2 = wg.autotune(prob)
+    assert a1 == a2 and a1[0] in (0, 1, 2)
+    op = wg.Conv2d(prob, opts_for(wg, wg.ALGO_AUTO))
+    assert op.algo == a1[0]
+    op(torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    _, r64 = O.conv2d_direct(x, wt, nthreads=8)
+    assert O.rel_errors(y.cpu().numpy(), r64)[0] <= TOL[algo_m(op.algo)]
