@@ -102,7 +102,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         for (int i = 0; i < kStages; ++i) {
             mbar_init(&full[i], kProducers + 1);
             mbar_init(&empty[i], 1);
-            mbar_init(&sfull[i], 1);
+            mbar_init(&sfull[i], kChunk);  // one arrival per staged channel (loader lanes)
             mbar_init(&sempty[i], kProducers);
         }
         mbar_init(tfull, 1);
@@ -136,42 +136,42 @@ __global__ void __launch_bounds__(kThreads, 1)
         return;
     }
 
-    // staging of chunk `c` (16 channels) into buffer c % nbuf, issued by the loader warp
-    auto issue_stage = [&](int c) {
+    // staging of chunk `c` (16 channels) into buffer c % nbuf: loader lane j
+    // copies channel j's rows of every image segment and accounts its own
+    // bytes on the barrier (16 arrivals complete the phase)
+    auto issue_stage = [&](int c, int j) {
         const int bsel = c % nbuf;
-        unsigned char* buf = stg + bsel * (kChunk * stg_ch_bytes);
+        unsigned char* buf = stg + bsel * (kChunk * stg_ch_bytes) + j * stg_ch_bytes;
+        const int ch = c * kChunk + j;
         uint32_t total = 0;
-        for (int pass = 0; pass < 2; ++pass) {
-            if (pass == 1) mbar_arrive_expect_tx(&sfull[bsel], total);
-            for (int j = 0; j < kChunk; ++j) {
-                const int ch = c * kChunk + j;
-                if (ch >= C) break;
-                for (int s = 0; s < seg->nseg; ++s) {
-                    const int rows = seg->yhi[s] - seg->ylo[s];
-                    if (rows <= 0) continue;
-                    const uintptr_t a = reinterpret_cast<uintptr_t>(
-                        x + (static_cast<long long>(seg->n_first + s) * C + ch) * plane +
-                        static_cast<long long>(seg->ylo[s]) * W);
-                    const uintptr_t a16 = a & ~uintptr_t(15);
-                    const uintptr_t b16 = min_uptr((a + static_cast<uintptr_t>(rows) * W * 2 + 15) & ~uintptr_t(15), lim);
-                    if (b16 <= a16) continue;
-                    if (pass == 0)
-                        total += static_cast<uint32_t>(b16 - a16);
-                    else
-                        bulk_g2s(buf + j * stg_ch_bytes + seg->off[s], reinterpret_cast<const void*>(a16),
-                                 static_cast<uint32_t>(b16 - a16), &sfull[bsel]);
-                }
-            }
+        uintptr_t a16s[kMaxSeg];
+        uint32_t lens[kMaxSeg];
+        const int nseg = seg->nseg;
+        for (int s = 0; s < nseg; ++s) {
+            lens[s] = 0;
+            const int rows = seg->yhi[s] - seg->ylo[s];
+            if (ch >= C || rows <= 0) continue;
+            const uintptr_t a = reinterpret_cast<uintptr_t>(
+                x + (static_cast<long long>(seg->n_first + s) * C + ch) * plane + static_cast<long long>(seg->ylo[s]) * W);
+            const uintptr_t a16 = a & ~uintptr_t(15);
+            const uintptr_t b16 = min_uptr((a + static_cast<uintptr_t>(rows) * W * 2 + 15) & ~uintptr_t(15), lim);
+            if (b16 <= a16) continue;
+            a16s[s] = a16;
+            lens[s] = static_cast<uint32_t>(b16 - a16);
+            total += lens[s];
         }
+        mbar_arrive_expect_tx(&sfull[bsel], total);
+        for (int s = 0; s < nseg; ++s)
+            if (lens[s]) bulk_g2s(buf + seg->off[s], reinterpret_cast<const void*>(a16s[s]), lens[s], &sfull[bsel]);
     };
 
     if (warp == 9) {
-        if (lane == 0) {
-            for (int c = 0; c < nbuf && c < c_chunks; ++c) issue_stage(c);
+        if (lane < kChunk) {
+            for (int c = 0; c < nbuf && c < c_chunks; ++c) issue_stage(c, lane);
             for (int c = 0; c + nbuf < c_chunks; ++c) {
                 // buffer c % nbuf is free once every producer has read chunk c
                 if (!mbar_wait(&sempty[c % nbuf], (c / nbuf) & 1, abort_flag, err, ERR_SITE_EMPTY)) break;
-                issue_stage(c + nbuf);
+                issue_stage(c + nbuf, lane);
             }
         }
     } else if (warp == 8) {

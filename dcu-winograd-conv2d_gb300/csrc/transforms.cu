@@ -166,29 +166,25 @@ __global__ void __launch_bounds__(kInThreads, 2) input_transform_kernel(
     const uintptr_t lim = reinterpret_cast<uintptr_t>(x_end) & ~uintptr_t(15);
 
     if (threadIdx.x == 0) {
-        mbar_init(bar, 1);
+        mbar_init(bar, cb);  // one arrival per channel of the block
         fence_barrier_init();
     }
     __syncthreads();
-    if (threadIdx.x == 0) {
-        uint32_t total = 0;
-        for (int c = 0; c < nch; ++c) {
+    // thread c copies channel c's rows and accounts its own bytes
+    if (threadIdx.x < cb) {
+        const int c = threadIdx.x;
+        uint32_t bytes = 0;
+        uintptr_t a16 = 0;
+        if (c < nch && rows > 0) {
             const uintptr_t a = reinterpret_cast<uintptr_t>(x + (n * C + c0 + c) * plane + static_cast<long long>(ylo) * W);
             const uintptr_t b = a + static_cast<uintptr_t>(rows) * W * 2;
-            const uintptr_t a16 = a & ~uintptr_t(15);
+            a16 = a & ~uintptr_t(15);
             const uintptr_t b16 = min_uptr((b + 15) & ~uintptr_t(15), lim);
-            if (rows > 0 && b16 > a16) total += static_cast<uint32_t>(b16 - a16);
+            if (b16 > a16) bytes = static_cast<uint32_t>(b16 - a16);
         }
-        mbar_arrive_expect_tx(bar, total);
-        for (int c = 0; c < nch; ++c) {
-            const uintptr_t a = reinterpret_cast<uintptr_t>(x + (n * C + c0 + c) * plane + static_cast<long long>(ylo) * W);
-            const uintptr_t b = a + static_cast<uintptr_t>(rows) * W * 2;
-            const uintptr_t a16 = a & ~uintptr_t(15);
-            const uintptr_t b16 = min_uptr((b + 15) & ~uintptr_t(15), lim);
-            if (rows > 0 && b16 > a16)
-                bulk_g2s(stage + static_cast<size_t>(c) * stride_bytes, reinterpret_cast<const void*>(a16),
-                         static_cast<uint32_t>(b16 - a16), bar);
-        }
+        mbar_arrive_expect_tx(bar, bytes);
+        if (bytes)
+            bulk_g2s(stage + static_cast<size_t>(c) * stride_bytes, reinterpret_cast<const void*>(a16), bytes, bar);
     }
     // every bulk copy of this CTA has landed before anyone reads the stage
     if (!mbar_wait(bar, 0, nullptr, err, ERR_SITE_FULL)) {
