@@ -48,7 +48,7 @@ EXPORTS = [
     "conv2d_refresh_filter", "conv2d_destroy", "conv2d_get_algo", "conv2d_workspace_bytes",
     "conv2d_launches_per_call", "conv2d_check_device", "conv2d_last_error", "conv2d_last_error_message",
     "conv2d_status_string", "conv2d_select_reference", "conv2d_copy_to_host", "conv2d_fp16_timed",
-    "conv2d_autotune", "conv2d_autotune_clear",
+    "conv2d_autotune", "conv2d_autotune_clear", "conv2d_fp16_noalloc",
 ]
 
 _lib = None
@@ -99,6 +99,7 @@ def lib():
         L.conv2d_fp16_timed.argtypes = [vp, vp, ctypes.POINTER(ctypes.c_float), ctypes.c_int]
         L.conv2d_autotune.argtypes = [ctypes.POINTER(Problem), ctypes.POINTER(Options), ip, ip]
         L.conv2d_autotune_clear.restype = None
+        L.conv2d_fp16_noalloc.argtypes = [ctypes.POINTER(Problem), vp]
         _lib = L
     return _lib
 
@@ -210,6 +211,12 @@ def autotune(problem: Problem, options: Options | None = None):
     _check(lib().conv2d_autotune(ctypes.byref(problem), ctypes.byref(options) if options is not None else None,
                                  ctypes.byref(a), ctypes.byref(b)))
     return a.value, b.value
+
+
+def conv2d_noalloc(problem: Problem, stream: int | None = None):
+    """F(2x3) convolution through the entry point that allocates no device
+    memory (workspace in the library's fixed scratch array)."""
+    _check(lib().conv2d_fp16_noalloc(ctypes.byref(problem), ctypes.c_void_p(stream or 0)))
 
 
 def copy_to_host(host_ptr: int, dev_ptr: int, nbytes: int):

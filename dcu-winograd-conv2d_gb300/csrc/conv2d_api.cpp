@@ -289,6 +289,8 @@ int Plan::run(cudaStream_t s) {
     return CONV2D_OK;
 }
 
+int set_last_error(int status, const char* msg) { return fail(status, msg); }
+
 Plan* plan_of(const void* param) {
     if (!param) return nullptr;
     const ParamBlob* pb = static_cast<const ParamBlob*>(param);

@@ -1,0 +1,108 @@
+// conv2d_fp16_noalloc: the F(2x3) non-fused convolution with its Winograd-
+// domain workspace (transformed filter U, transformed input V, GEMM result M
+// and the device error word) in a fixed device array that lives in this
+// library, instead of memory from cudaMalloc.
+//
+// Who needs this: callers that must not allocate device memory while they
+// run -- for example a host that gives all of its device memory to its own
+// pool at start-up and has none left for a library, or a latency-bound loop
+// that cannot afford cudaMalloc/cudaFree, which synchronise the device.  The
+// price is a fixed array of kNoAllocScratchBytes on every GPU that loads this
+// library, held until the process exits, and a size limit per call.
+//
+// Setup: the first call on a device, with that device current, looks up the
+// array's device address (cudaGetSymbolAddress) and caches it for the device;
+// make that first call before any stream capture.  Every call on a device
+// uses the same array: calls whose work overlaps on the GPU (two streams, or
+// two host threads) race on it and must be ordered by the caller.
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstdio>
+#include <mutex>
+
+#include "../../include/conv2d.h"
+#include "wg_kernels.h"
+#include "wg_plan.h"
+
+namespace wg {
+
+// 32 MiB: enough for the F(2x3) workspace of, e.g., N=1, C=K=64, 56x56
+// (U 0.13 MB, V 1.6 MB, M 1.6 MB) or N=8, C=K=128, 56x56 (26 MB).
+constexpr size_t kNoAllocScratchBytes = size_t(32) << 20;
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+namespace {
+
+constexpr int kMaxDevices = 64;
+std::mutex g_mu;
+void* g_dev_ptr[kMaxDevices] = {};
+
+// Device address of the array for the current device (looked up once).
+cudaError_t scratch_for(int device, void** out) {
+    if (device < 0 || device >= kMaxDevices) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lk(g_mu);
+    if (!g_dev_ptr[device]) {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess) return e;
+        g_dev_ptr[device] = p;
+    }
+    *out = g_dev_ptr[device];
+    return cudaSuccess;
+}
+
+int noalloc_fail(int status, const char* msg) { return set_last_error(status, msg); }
+
+}  // namespace
+
+}  // namespace wg
+
+using namespace wg;
+
+extern "C" int conv2d_fp16_noalloc(const problem_t* problem, void* stream) {
+    const int st = validate_problem(problem);
+    if (st) return st;
+    if (reinterpret_cast<uintptr_t>(problem->in) % 16 != 0)
+        return noalloc_fail(CONV2D_ERR_UNSUPPORTED, "input pointer must be 16-byte aligned");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const Geom g = make_geom(problem->n, problem->c, problem->h, problem->w, problem->k, problem->p, problem->q, 2);
+    const long long E = 16;
+    auto al = [](long long b) { return (b + 255) / 256 * 256; };
+    const long long bErr = 256;
+    const long long bU = al(E * g.kp * g.cp * 2);
+    const long long bV = al(E * round_rows(g.P) * g.cp * 2);
+    const long long bM = al(E * g.P * g.kp * 2);
+    if (bErr + bU + bV + bM > static_cast<long long>(kNoAllocScratchBytes))
+        return noalloc_fail(CONV2D_ERR_UNSUPPORTED,
+                            "problem needs more workspace than the 32 MiB no-allocation scratch holds");
+    int device = 0;
+    if (cudaGetDevice(&device) != cudaSuccess) return noalloc_fail(CONV2D_ERR_CUDA, "no CUDA device");
+    void* base = nullptr;
+    if (scratch_for(device, &base) != cudaSuccess)
+        return noalloc_fail(CONV2D_ERR_CUDA, "cudaGetSymbolAddress of the scratch array failed");
+    char* b = static_cast<char*>(base);
+    DevErr* err = reinterpret_cast<DevErr*>(b);
+    void* U = b + bErr;
+    void* V = b + bErr + bU;
+    void* Mw = b + bErr + bU + bV;
+
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    GemmPlan gp;
+    if (plan_gemm(gp, OpType::F16, 16, g.P, g.k, g.kp, g.cp, V, U, false, default_bn(g.k), sms > 0 ? sms : 1) !=
+        cudaSuccess)
+        return noalloc_fail(CONV2D_ERR_CUDA, "tensor map encoding failed");
+    // the error word starts every call at zero; U, V and M are rewritten in
+    // full (padding included) by the kernels below
+    if (cudaMemsetAsync(err, 0, sizeof(DevErr), s) != cudaSuccess)
+        return noalloc_fail(CONV2D_ERR_CUDA, "cudaMemsetAsync failed");
+    const void* x_end = static_cast<const uint16_t*>(problem->in) + static_cast<long long>(g.n) * g.c * g.h * g.w;
+    if (launch_filter_transform(Xform::F2, OpType::F16, problem->weight, U, g.k, g.c, g.cp, s) != cudaSuccess ||
+        launch_input_transform(Xform::F2, OpType::F16, g, problem->in, x_end, V, nullptr, err, s) != cudaSuccess ||
+        launch_gemm(gp, Mw, err, s) != cudaSuccess ||
+        launch_output_transform(Xform::F2, false, g, Mw, problem->out, nullptr, s) != cudaSuccess)
+        return noalloc_fail(CONV2D_ERR_CUDA, "kernel launch failed");
+    return CONV2D_OK;
+}

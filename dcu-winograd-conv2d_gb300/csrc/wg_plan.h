@@ -73,6 +73,9 @@ int select_reference64(unsigned long long n, unsigned long long c, unsigned long
                        unsigned long long ow);
 Plan* plan_of(const void* param);
 
+// Records the status and message conv2d_last_error / _message report.
+int set_last_error(int status, const char* msg);
+
 // Per-shape algorithm and GEMM tile choice for CONV2D_ALGO_AUTO
 // (autotune.cpp): measured once per shape, cached, optionally persisted.
 int autotune_choose(const problem_t& pr, const conv2d_options_t& opt, int fallback, int* algo, int* bn);

@@ -167,6 +167,20 @@ void conv2d_autotune_clear(void);
  * kernel_ms and returns the number of launches (negative status on error). */
 int conv2d_fp16_timed(const void* param_ptr, void* stream, float* kernel_ms, int max_kernels);
 
+/* No counterpart in the reference.  The F(2x3) non-fused convolution of
+ * `problem` on `stream`, for callers that must not allocate device memory
+ * while they run (a host that hands all device memory to its own pool at
+ * start-up, or a latency-bound loop that cannot afford the device-wide
+ * synchronisation of cudaMalloc/cudaFree).  It needs no param blob and calls
+ * no allocator: its Winograd-domain workspace lives in a 32 MiB array inside
+ * this library that every GPU loading the library holds until the process
+ * exits.  Problems whose workspace (16*Kp*Cp + 16*P8*Cp + 16*P*Kp halves, P
+ * tiles rounded up to 8 for P8) exceeds it return CONV2D_ERR_UNSUPPORTED.
+ * The first call on a device looks the array up (make it before any stream
+ * capture); all calls on a device share the array, so calls that overlap on
+ * the GPU race and the caller must order them. */
+int conv2d_fp16_noalloc(const problem_t* problem, void* stream);
+
 /* Copies `bytes` from device memory to host memory and waits (used by tests
  * to read the Winograd-domain workspaces U_d/V_d/M_d of the param blob). */
 int conv2d_copy_to_host(void* host_dst, const void* device_src, size_t bytes);
