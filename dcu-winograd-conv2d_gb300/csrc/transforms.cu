@@ -194,91 +194,84 @@ __global__ void __launch_bounds__(kInThreads, 2) input_transform_kernel(
         return;
     }
 
+    // Tasks: (granule g, tile t, piece sub) with sub fastest.  A thread
+    // transforms CPT channels of one tile; LPG consecutive lanes complete one
+    // 16-byte granule row, so a warp's stores of one element are contiguous.
+    constexpr int CPT = (A == 6) ? 2 : 4;  // channels per thread
+    constexpr int LPG = 8 / CPT;           // lanes per granule row
     const int ntiles = ntb * tiles_w;
     const int G = (min(cb, CG * 8 - c0) + 7) / 8;
-    for (int task = threadIdx.x; task < ntiles * G; task += blockDim.x) {
-        const int g = task / ntiles, t = task - g * ntiles;
+    const long long estride = static_cast<long long>(CG) * Pp * 8;
+    for (int task = threadIdx.x; task < ntiles * G * LPG; task += blockDim.x) {
+        const int sub = task % LPG;
+        const int rest = task / LPG;
+        const int t = rest % ntiles, g = rest / ntiles;
         const int tr = t / tiles_w, tw = t - tr * tiles_w;
         const long long p = (n * tiles_h + th0 + tr) * tiles_w + tw;
         const int y0 = (th0 + tr) * M - pad_h, x0 = tw * M - pad_w;
         const float s = scale ? scale[p] : 1.f;
-        OutT* dst = V + ((static_cast<long long>(c0 / 8 + g)) * Pp + p) * 8;
-        // one channel's 2-D transform: column pass t = B^T d one input column
-        // at a time, then the row pass hands each finished value to `put`
-        // (d is never held whole)
-        auto channel = [&](int c, auto&& put) {
-            const bool cv = c < nch;
-            const __half* gsrc = x + (n * C + c0 + c) * plane;
-            const uintptr_t a = reinterpret_cast<uintptr_t>(gsrc + static_cast<long long>(ylo) * W);
-            const __half* sm = reinterpret_cast<const __half*>(stage + static_cast<size_t>(c) * stride_bytes + (a & 15));
-            // rows staged whole unless they run into the last partial 16-byte
-            // block of the input (then read from global memory)
-            const bool staged = a + static_cast<uintptr_t>(rows) * W * 2 <= lim;
-            const __half* gsrc_rows = gsrc + static_cast<long long>(ylo) * W;
-            float t[A * A];
-            // two copies of the column loop so the staged path compiles to
-            // shared-memory loads (a pointer that may be either would not)
-            auto columns = [&](const __half* src) {
+        int rowoff[A];
+        bool rowok[A], colok[A];
 #pragma unroll
-                for (int j = 0; j < A; ++j) {
-                    const int xx = x0 + j;
-                    const bool xv = cv && xx >= 0 && xx < W;
-                    float col[A];
+        for (int i = 0; i < A; ++i) {
+            rowoff[i] = (y0 + i - ylo) * W + x0;
+            rowok[i] = y0 + i >= ylo && y0 + i < yhi;
+            colok[i] = x0 + i >= 0 && x0 + i < W;
+        }
+        uint32_t pk[A * A][CPT / 2];
 #pragma unroll
-                    for (int i = 0; i < A; ++i) {
-                        const int y = y0 + i;
-                        float v = 0.f;
-                        if (xv && y >= ylo && y < yhi) v = __half2float(src[(y - ylo) * W + xx]);
-                        col[i] = v * s;
+        for (int cc = 0; cc < CPT; ++cc) {
+            const int c = g * 8 + sub * CPT + cc;
+            float t2[A * A];
+            if (c >= nch) {
+#pragma unroll
+                for (int e = 0; e < A * A; ++e) t2[e] = 0.f;
+            } else {
+                const __half* gsrc = x + (n * C + c0 + c) * plane;
+                const uintptr_t a = reinterpret_cast<uintptr_t>(gsrc + static_cast<long long>(ylo) * W);
+                const __half* sm =
+                    reinterpret_cast<const __half*>(stage + static_cast<size_t>(c) * stride_bytes + (a & 15));
+                // rows staged whole unless they run into the last partial
+                // 16-byte block of the input (then read from global memory);
+                // two copies of the column pass so the staged one compiles to
+                // shared-memory loads
+                const bool staged = a + static_cast<uintptr_t>(rows) * W * 2 <= lim;
+                auto columns = [&](const __half* src) {
+#pragma unroll
+                    for (int j = 0; j < A; ++j) {
+                        float col[A];
+#pragma unroll
+                        for (int i = 0; i < A; ++i)
+                            col[i] = (rowok[i] && colok[j]) ? __half2float(src[rowoff[i] + j]) * s : 0.f;
+                        TF::bt(col, 1, &t2[j], A);  // column pass B^T d
                     }
-                    TF::bt(col, 1, &t[j], A);
-                }
-            };
-            if (staged)
-                columns(sm);
-            else
-                columns(gsrc_rows);
+                };
+                if (staged)
+                    columns(sm);
+                else
+                    columns(gsrc + static_cast<long long>(ylo) * W);
+            }
 #pragma unroll
             for (int i = 0; i < A; ++i) {
                 float row[A];
-                TF::bt(&t[i * A], 1, row, 1);
+                TF::bt(&t2[i * A], 1, row, 1);  // row pass (B^T d) B
 #pragma unroll
-                for (int j = 0; j < A; ++j) put(i * A + j, row[j]);
-            }
-        };
-        const long long estride = static_cast<long long>(CG) * Pp * 8;
-        if constexpr (A == 4) {
-            // F(2x3): all 8 channels of the granule, one 16-byte store per element
-            uint32_t pk[A * A][4];
-#pragma unroll
-            for (int cc = 0; cc < 8; ++cc)
-                channel(g * 8 + cc, [&](int e, float v) {
+                for (int j = 0; j < A; ++j) {
+                    uint32_t& slot = pk[i * A + j][cc >> 1];
                     if (cc & 1)
-                        pk[e][cc >> 1] |= pack2<OutT>(0.f, v);
+                        slot |= pack2<OutT>(0.f, row[j]);
                     else
-                        pk[e][cc >> 1] = pack2<OutT>(v, 0.f);
-                });
-#pragma unroll
-            for (int e = 0; e < A * A; ++e)
-                *reinterpret_cast<uint4*>(dst + e * estride) = make_uint4(pk[e][0], pk[e][1], pk[e][2], pk[e][3]);
-        } else {
-            // F(4x3): two channels per pass (4-byte stores) keep the 36 packed
-            // elements within the register budget; the four passes complete
-            // every 16-byte granule row, and the pieces merge in L2
-#pragma unroll 1
-            for (int pass = 0; pass < 4; ++pass) {
-                uint32_t pk[A * A];
-#pragma unroll 1
-                for (int cc = 0; cc < 2; ++cc)
-                    channel(g * 8 + pass * 2 + cc, [&](int e, float v) {
-                        if (cc)
-                            pk[e] |= pack2<OutT>(0.f, v);
-                        else
-                            pk[e] = pack2<OutT>(v, 0.f);
-                    });
-#pragma unroll
-                for (int e = 0; e < A * A; ++e) *reinterpret_cast<uint32_t*>(dst + e * estride + pass * 2) = pk[e];
+                        slot = pack2<OutT>(row[j], 0.f);
+                }
             }
+        }
+        OutT* dst = V + ((static_cast<long long>(c0 / 8 + g)) * Pp + p) * 8 + sub * CPT;
+#pragma unroll
+        for (int e = 0; e < A * A; ++e) {
+            if constexpr (CPT == 4)
+                *reinterpret_cast<uint2*>(dst + e * estride) = make_uint2(pk[e][0], pk[e][1]);
+            else
+                *reinterpret_cast<uint32_t*>(dst + e * estride) = pk[e][0];
         }
     }
 }
@@ -329,7 +322,11 @@ __global__ void __launch_bounds__(128) output_transform_kernel(const MT* __restr
                                                                int tiles_h, int tiles_w, long long P, int KG) {
     constexpr int M = TF::M, A = TF::ALPHA;
     constexpr int PG = MG<MT>::kPerGranule, PH = MG<MT>::kPerHalf;
-    const long long p = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+    // thread = (tile, half granule): two consecutive lanes read the two halves
+    // of one 16-byte granule row, so a warp reads 256 contiguous bytes
+    const long long task = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+    const int hh = static_cast<int>(task & 1);
+    const long long p = task >> 1;
     const int g = blockIdx.y;
     if (p >= P) return;
     const int tw = static_cast<int>(p % tiles_w);
@@ -339,26 +336,23 @@ __global__ void __launch_bounds__(128) output_transform_kernel(const MT* __restr
     const int oh0 = th * M, ow0 = tw * M;
     const int vr = min(M, OH - oh0), vc = min(M, OW - ow0);
     const float inv = scale ? 1.f / scale[p] : 1.f;  // exact: scale is a power of two
-    const MT* src = Mw + (static_cast<long long>(g) * P + p) * PG;
+    const MT* src = Mw + (static_cast<long long>(g) * P + p) * PG + hh * PH;
     const long long estride = static_cast<long long>(KG) * P * PG;
-#pragma unroll 1
-    for (int hh = 0; hh < 2; ++hh) {
-        float m[A * A][PH];
+    float m[A * A][PH];
 #pragma unroll
-        for (int e = 0; e < A * A; ++e) MG<MT>::load(src + e * estride + hh * PH, m[e]);
+    for (int e = 0; e < A * A; ++e) MG<MT>::load(src + e * estride, m[e]);
 #pragma unroll
-        for (int ch = 0; ch < PH; ++ch) {
-            const int k = g * PG + hh * PH + ch;
-            if (k >= K) break;
-            float mm[A * A], y[M * M];
+    for (int ch = 0; ch < PH; ++ch) {
+        const int k = g * PG + hh * PH + ch;
+        if (k >= K) break;
+        float mm[A * A], y[M * M];
 #pragma unroll
-            for (int e = 0; e < A * A; ++e) mm[e] = m[e][ch];
-            output_tile_transform<TF>(mm, y);
-            __half* o = out + ((n * K + k) * OH + oh0) * static_cast<long long>(OW) + ow0;
+        for (int e = 0; e < A * A; ++e) mm[e] = m[e][ch];
+        output_tile_transform<TF>(mm, y);
+        __half* o = out + ((n * K + k) * OH + oh0) * static_cast<long long>(OW) + ow0;
 #pragma unroll
-            for (int i = 0; i < M; ++i)
-                if (i < vr) store_row<M>(o + static_cast<long long>(i) * OW, &y[i * M], vc, inv);
-        }
+        for (int i = 0; i < M; ++i)
+            if (i < vr) store_row<M>(o + static_cast<long long>(i) * OW, &y[i * M], vc, inv);
     }
 }
 
@@ -405,7 +399,7 @@ template <class TF, class MT>
 cudaError_t output_launch(const Geom& g, const void* Mw, void* out, const float* scale, cudaStream_t s) {
     constexpr int PG = MG<MT>::kPerGranule;
     const int KG = g.kp / PG;
-    dim3 grid(static_cast<unsigned>((g.P + 127) / 128), KG);
+    dim3 grid(static_cast<unsigned>((2 * g.P + 127) / 128), KG);
     output_transform_kernel<TF, MT><<<grid, 128, 0, s>>>(static_cast<const MT*>(Mw), static_cast<__half*>(out), scale,
                                                          g.k, g.oh, g.ow, g.tiles_h, g.tiles_w, g.P, KG);
     return cudaGetLastError();
