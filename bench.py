@@ -49,6 +49,26 @@ WORKLOADS = {
     "final6": (2, 320, 64, 64, 4, "uniform", "uniform", "contest shape 2x320x64x64 -> 4"),
 }
 ALGO_ARG = {"ref": -1, "4x3": 0, "2x3": 1, "fused": 2, "auto": 3}
+BATCH_WORKLOADS = {
+    "cfg4": "24 uneven 3x3 pad-1 problems in one grouped graph launch: C,K in {64,128,256,512}, "
+            "H=W in {7,14,28,56,112}, N in {1,...,128}, U[-1,1], seed 20261203",
+}
+
+
+def batch_shapes(seed=20261203, count=24):
+    """The seeded draw of the batched workload: (n, c, h, k) per problem."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(count):
+        c = int(rng.choice([64, 128, 256, 512]))
+        k = int(rng.choice([64, 128, 256, 512]))
+        h = int(rng.choice([7, 14, 28, 56, 112]))
+        n = int(rng.choice([1, 2, 4, 8, 16, 32, 64, 128]))
+        out.append((n, c, h, k))
+    return out
+
+
 FALLBACK_PEAKS = {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}
 
 
@@ -430,13 +450,118 @@ def our_arm(args):
     return 0
 
 
+def batch_arm(args):
+    """Batched workload: every problem of the draw in one grouped run (grouped
+    launches replayed from a CUDA graph) against the same problems launched
+    one conv2d call at a time."""
+    import torch
+    rank, world, local = env_dist()
+    torch.cuda.set_device(local)
+    device = torch.device("cuda", local)
+    wg = load_pkg()
+    wg.lib()
+    shapes = batch_shapes()
+    g = torch.Generator(device=device)
+    g.manual_seed(99 + rank)
+    probs, keep = [], []
+    flops = 0.0
+    in_bytes = out_bytes = 0
+    for n, c, h, k in shapes:
+        x = (torch.rand((n, c, h, h), generator=g, device=device) * 2 - 1).half()
+        w = (torch.rand((k, c, 3, 3), generator=g, device=device) * 2 - 1).half()
+        y = torch.empty((n, k, h, h), dtype=torch.float16, device=device)
+        probs.append(wg.make_problem(x.data_ptr(), w.data_ptr(), y.data_ptr(), n, c, h, h, k))
+        keep.append((x, w, y))
+        flops += direct_flops(n, c, h, h, k)
+        in_bytes += x.numel() * 2
+        out_bytes += y.numel() * 2
+    t0 = time.perf_counter()
+    batch = wg.Batch(probs, wg.default_options(algo=ALGO_ARG[args.algo if args.algo != "ref" else "auto"]))
+    setup_s = time.perf_counter() - t0
+    stream = torch.cuda.current_stream(device)
+    sptr = stream.cuda_stream
+    for _ in range(args.warmup):
+        batch.run(sptr)
+        batch.run_percall(sptr)
+    torch.cuda.synchronize(device)
+    st, site = batch.check_device()
+    if st != wg.OK:
+        raise RuntimeError(f"device wait gave up at site {site}")
+
+    def timed(fn):
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+        torch.cuda.synchronize(device)
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for i in range(args.steps):
+            evs[i][0].record(stream)
+            fn(sptr)
+            evs[i][1].record(stream)
+        b.record(stream)
+        torch.cuda.synchronize(device)
+        return a.elapsed_time(b), sorted(x.elapsed_time(y) for x, y in evs)
+
+    sampler = ClockSampler(local)
+    sampler.start()
+    time.sleep(0.3)
+    grouped_ms, lat = timed(batch.run)
+    clocks = sampler.stop()
+    percall_ms, lat_pc = timed(batch.run_percall)
+    value = world * flops * args.steps / (grouped_ms * 1e-3) / 1e12
+    percall = world * flops * args.steps / (percall_ms * 1e-3) / 1e12
+
+    # end to end: inputs copied in from pinned host memory, outputs copied out
+    e2e = None
+    if not args.no_e2e:
+        hin = [torch.empty(x.shape, dtype=torch.float16).pin_memory() for x, _, _ in keep]
+        hout = [torch.empty(y.shape, dtype=torch.float16).pin_memory() for _, _, y in keep]
+        for h, (x, _, _) in zip(hin, keep):
+            h.copy_(x.cpu())
+        e_steps = max(3, min(args.steps, 10))
+        torch.cuda.synchronize(device)
+        t0 = time.perf_counter()
+        for _ in range(e_steps):
+            for h, (x, _, _) in zip(hin, keep):
+                x.copy_(h, non_blocking=True)
+            batch.run(sptr)
+            for h, (_, _, y) in zip(hout, keep):
+                h.copy_(y, non_blocking=True)
+            torch.cuda.synchronize(device)
+        el = time.perf_counter() - t0
+        e2e = {"value": world * flops * e_steps / el / 1e12, "unit": "TFLOP/s", "h2d_bytes_per_step": in_bytes,
+               "d2h_bytes_per_step": out_bytes, "ms_per_step": el / e_steps * 1e3,
+               "path": "pinned host copies of all 24 inputs/outputs around one grouped batch run"}
+    algos = [batch.info(i) for i in range(len(shapes))]
+    line = {
+        "metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": grouped_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f16", "data": "synthetic (seeded torch RNG)",
+        "config": {"workload": BATCH_WORKLOADS[args.workload], "problems": [list(s) for s in shapes],
+                   "algo_bn": algos, "total_gflop": flops / 1e9, "accumulate": "fp32",
+                   "l2": f"working set {(in_bytes + out_bytes) / 2**30:.1f} GiB of inputs/outputs > L2",
+                   "setup_s": setup_s},
+        "percall": {"value": percall, "ms_per_step": percall_ms / args.steps,
+                    "launches": batch.launches(False)},
+        "grouped_over_percall": value / percall,
+        "latency_us": {"p50": lat[len(lat) // 2] * 1e3, "p99": lat[min(len(lat) - 1, int(0.99 * len(lat)))] * 1e3,
+                       "percall_p50": lat_pc[len(lat_pc) // 2] * 1e3},
+        "e2e": e2e, "clocks": clocks, "roofline": None, "cpu_baseline": None,
+        "gpu_launches": args.steps * batch.launches(True),
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    batch.destroy()
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="cfg2")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS) + sorted(BATCH_WORKLOADS), default="cfg2")
     ap.add_argument("--algo", choices=sorted(ALGO_ARG), default="ref")
     ap.add_argument("--gemm-bn", type=int, default=0)
     ap.add_argument("--l2-chunk", type=int, default=None)
@@ -447,6 +572,8 @@ def main():
         args.warmup = 3
     if args.impl == "reference":
         return reference_arm(args)
+    if args.workload in BATCH_WORKLOADS:
+        return batch_arm(args)
     return our_arm(args)
 
 

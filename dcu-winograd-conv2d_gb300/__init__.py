@@ -49,6 +49,8 @@ EXPORTS = [
     "conv2d_launches_per_call", "conv2d_check_device", "conv2d_last_error", "conv2d_last_error_message",
     "conv2d_status_string", "conv2d_select_reference", "conv2d_copy_to_host", "conv2d_fp16_timed",
     "conv2d_autotune", "conv2d_autotune_clear", "conv2d_fp16_noalloc",
+    "conv2d_batch_create", "conv2d_batch_run", "conv2d_batch_run_percall", "conv2d_batch_info",
+    "conv2d_batch_launches", "conv2d_batch_check_device", "conv2d_batch_destroy",
 ]
 
 _lib = None
@@ -100,6 +102,14 @@ def lib():
         L.conv2d_autotune.argtypes = [ctypes.POINTER(Problem), ctypes.POINTER(Options), ip, ip]
         L.conv2d_autotune_clear.restype = None
         L.conv2d_fp16_noalloc.argtypes = [ctypes.POINTER(Problem), vp]
+        L.conv2d_batch_create.argtypes = [ctypes.POINTER(Problem), ctypes.c_int, ctypes.POINTER(Options),
+                                          ctypes.POINTER(vp)]
+        L.conv2d_batch_run.argtypes = [vp, vp]
+        L.conv2d_batch_run_percall.argtypes = [vp, vp]
+        L.conv2d_batch_info.argtypes = [vp, ctypes.c_int, ip, ip]
+        L.conv2d_batch_launches.argtypes = [vp, ctypes.c_int]
+        L.conv2d_batch_check_device.argtypes = [vp, ip]
+        L.conv2d_batch_destroy.argtypes = [vp]
         _lib = L
     return _lib
 
@@ -217,6 +227,51 @@ def conv2d_noalloc(problem: Problem, stream: int | None = None):
     """F(2x3) convolution through the entry point that allocates no device
     memory (workspace in the library's fixed scratch array)."""
     _check(lib().conv2d_fp16_noalloc(ctypes.byref(problem), ctypes.c_void_p(stream or 0)))
+
+
+class Batch:
+    """Many problems of uneven shape: grouped launches replayed from a CUDA
+    graph (run) or one conv2d call each (run_percall)."""
+
+    def __init__(self, problems, options: Options | None = None):
+        L = lib()
+        arr = (Problem * len(problems))(*problems)
+        self._problems = arr
+        h = ctypes.c_void_p()
+        _check(L.conv2d_batch_create(arr, len(problems), ctypes.byref(options) if options is not None else None,
+                                     ctypes.byref(h)))
+        self.handle = h
+        self.count = len(problems)
+
+    def run(self, stream: int | None = None):
+        _check(lib().conv2d_batch_run(self.handle, ctypes.c_void_p(stream or 0)))
+
+    def run_percall(self, stream: int | None = None):
+        _check(lib().conv2d_batch_run_percall(self.handle, ctypes.c_void_p(stream or 0)))
+
+    def info(self, i):
+        a, b = ctypes.c_int(), ctypes.c_int()
+        _check(lib().conv2d_batch_info(self.handle, i, ctypes.byref(a), ctypes.byref(b)))
+        return a.value, b.value
+
+    def launches(self, grouped=True):
+        return lib().conv2d_batch_launches(self.handle, 1 if grouped else 0)
+
+    def check_device(self):
+        site = ctypes.c_int(0)
+        return lib().conv2d_batch_check_device(self.handle, ctypes.byref(site)), site.value
+
+    def destroy(self):
+        if self.handle:
+            _check(lib().conv2d_batch_destroy(self.handle))
+            self.handle = None
+
+    def __del__(self):
+        try:
+            if self.handle and _lib is not None:
+                _lib.conv2d_batch_destroy(self.handle)
+        except Exception:
+            pass
 
 
 def copy_to_host(host_ptr: int, dev_ptr: int, nbytes: int):

@@ -1,0 +1,321 @@
+// Many convolutions of uneven shape in one graph launch.
+//
+// A batch holds one Plan per problem (algorithm and GEMM tile chosen per
+// shape, by default by the autotuner; workspace and transformed filter of
+// each problem resident) and runs them either
+//   * grouped: the input transforms of all problems in one launch per
+//     transform family, the GEMMs of all problems in one persistent launch
+//     per (channel tile, M type) whose work queue holds every (problem,
+//     element, tile block, channel block) item, the output transforms in one
+//     launch per family -- captured once into a CUDA graph and replayed; or
+//   * per call: each problem's own launches, one problem after another
+//     (the comparison the grouped run is measured against).
+// Both use the same workspaces, so their results are bit-identical.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <tuple>
+#include <vector>
+
+#include "../../include/conv2d.h"
+#include "wg_kernels.h"
+#include "wg_plan.h"
+
+namespace wg {
+
+struct Batch {
+    std::vector<std::unique_ptr<Plan>> plans;
+    void* dev = nullptr;         // descriptor arrays + error word
+    DevErr* err = nullptr;
+    struct InGroup {
+        Xform xf;
+        OpType op;
+        const InDesc* descs;
+        int n;
+        long long blocks;
+        int smem;
+    };
+    struct GemmGroup {
+        int bn;
+        bool m_fp32;
+        OpType op;
+        const GemmDesc* descs;
+        int n;
+        long long tiles;
+        int grid;
+    };
+    struct OutGroup {
+        Xform xf;
+        bool m_fp32;
+        const OutDesc* descs;
+        int n;
+        long long blocks;
+    };
+    std::vector<InGroup> in_groups;
+    std::vector<GemmGroup> gemm_groups;
+    std::vector<OutGroup> out_groups;
+    std::vector<int> fused;      // problems run by their own fused kernel
+    std::vector<int> scaled;     // problems whose tile scale is computed per problem
+    cudaGraphExec_t graph = nullptr;
+    int grouped_launches = 0;
+
+    ~Batch() {
+        if (graph) cudaGraphExecDestroy(graph);
+        if (dev) cudaFree(dev);
+    }
+
+    cudaError_t launch_grouped(cudaStream_t s) {
+        cudaError_t e = cudaSuccess;
+        for (int i : scaled) {
+            Plan& p = *plans[i];
+            if ((e = launch_tile_scale(p.g, p.prob.in, p.scale, s)) != cudaSuccess) return e;
+        }
+        for (const InGroup& g : in_groups)
+            if ((e = launch_input_transform_grouped(g.xf, g.op, g.descs, g.n, g.blocks, g.smem, err, s)) != cudaSuccess)
+                return e;
+        for (const GemmGroup& g : gemm_groups)
+            if ((e = launch_gemm_grouped(g.descs, g.n, g.tiles, g.op, g.m_fp32, g.bn, g.grid, err, s)) != cudaSuccess)
+                return e;
+        for (const OutGroup& g : out_groups)
+            if ((e = launch_output_transform_grouped(g.xf, g.m_fp32, g.descs, g.n, g.blocks, s)) != cudaSuccess) return e;
+        for (int i : fused) {
+            Plan& p = *plans[i];
+            const void* x_end =
+                static_cast<const uint16_t*>(p.prob.in) + static_cast<long long>(p.prob.n) * p.g.c * p.g.h * p.g.w;
+            if ((e = launch_fused2x3(p.fused, p.g, p.prob.in, x_end, p.prob.out, err, s)) != cudaSuccess) return e;
+        }
+        return cudaSuccess;
+    }
+};
+
+namespace {
+
+int batch_fail(int st, const char* msg) { return set_last_error(st, msg); }
+
+}  // namespace
+
+int batch_create(const problem_t* problems, int count, const conv2d_options_t* opt_in, Batch** out) {
+    if (!problems || count <= 0 || !out) return batch_fail(CONV2D_ERR_INVALID, "empty batch");
+    conv2d_options_t opt;
+    if (opt_in)
+        opt = *opt_in;
+    else
+        options_default(&opt);
+    opt.l2_chunk_bytes = 0;
+    std::unique_ptr<Batch> b(new Batch());
+    for (int i = 0; i < count; ++i) {
+        std::unique_ptr<Plan> p(new Plan());
+        int st = p->build(&problems[i], &opt);
+        if (st) return st;
+        st = p->filter(nullptr);  // transformed filters stay resident
+        if (st) return st;
+        b->plans.push_back(std::move(p));
+    }
+    // group the problems and lay out their descriptors
+    std::map<std::pair<int, int>, std::vector<int>> in_keys, out_keys;        // (xform, op|mfp32) -> problems
+    std::map<std::tuple<int, int, int>, std::vector<int>> gemm_keys;          // (bn, m_fp32, op) -> problems
+    for (int i = 0; i < count; ++i) {
+        Plan& p = *b->plans[i];
+        if (p.algo == CONV2D_ALGO_2X3_FUSED) {
+            b->fused.push_back(i);
+            continue;
+        }
+        if (p.scaling) b->scaled.push_back(i);
+        in_keys[{static_cast<int>(p.xf), static_cast<int>(p.op)}].push_back(i);
+        out_keys[{static_cast<int>(p.xf), p.m_fp32 ? 1 : 0}].push_back(i);
+        gemm_keys[{p.gemm_full.bn, p.m_fp32 ? 1 : 0, static_cast<int>(p.op)}].push_back(i);
+    }
+    std::vector<InDesc> in_descs;
+    std::vector<OutDesc> out_descs;
+    std::vector<GemmDesc> gemm_descs;
+    struct Range {
+        size_t first, n;
+        long long total;
+        int extra;
+    };
+    std::vector<std::pair<std::pair<int, int>, Range>> in_r, out_r;
+    std::vector<std::pair<std::tuple<int, int, int>, Range>> gemm_r;
+    for (auto& kv : in_keys) {
+        Range r{in_descs.size(), kv.second.size(), 0, 0};
+        for (int i : kv.second) {
+            Plan& p = *b->plans[i];
+            const void* x_end =
+                static_cast<const uint16_t*>(p.prob.in) + static_cast<long long>(p.prob.n) * p.g.c * p.g.h * p.g.w;
+            int smem = 0;
+            InDesc d = make_in_desc(p.g, p.prob.in, x_end, p.V, p.scale, &smem);
+            d.blk_begin = r.total;
+            r.total += d.gx * d.gy;
+            r.extra = std::max(r.extra, smem);
+            in_descs.push_back(d);
+        }
+        in_r.push_back({kv.first, r});
+    }
+    for (auto& kv : out_keys) {
+        Range r{out_descs.size(), kv.second.size(), 0, 0};
+        for (int i : kv.second) {
+            Plan& p = *b->plans[i];
+            OutDesc d = make_out_desc(p.g, p.m_fp32, p.Mw, p.prob.out, p.scale);
+            d.blk_begin = r.total;
+            r.total += d.gx * d.gy;
+            out_descs.push_back(d);
+        }
+        out_r.push_back({kv.first, r});
+    }
+    for (auto& kv : gemm_keys) {
+        Range r{gemm_descs.size(), kv.second.size(), 0, 0};
+        for (int i : kv.second) {
+            GemmDesc d = b->plans[i]->gemm_full.desc;
+            d.tile_begin = r.total;
+            r.total += d.tiles;
+            gemm_descs.push_back(d);
+        }
+        gemm_r.push_back({kv.first, r});
+    }
+    // one device block: error word | GemmDesc[] (64-byte aligned) | InDesc[] | OutDesc[]
+    auto al = [](size_t x) { return (x + 255) / 256 * 256; };
+    const size_t oE = 0, oG = 256, oI = oG + al(gemm_descs.size() * sizeof(GemmDesc)),
+                 oO = oI + al(in_descs.size() * sizeof(InDesc)), total = oO + al(out_descs.size() * sizeof(OutDesc));
+    if (cudaMalloc(&b->dev, total) != cudaSuccess) {
+        cudaGetLastError();
+        return batch_fail(CONV2D_ERR_NOMEM, "batch descriptor allocation failed");
+    }
+    char* base = static_cast<char*>(b->dev);
+    b->err = reinterpret_cast<DevErr*>(base + oE);
+    cudaMemset(b->err, 0, sizeof(DevErr));
+    if (!gemm_descs.empty()) cudaMemcpy(base + oG, gemm_descs.data(), gemm_descs.size() * sizeof(GemmDesc), cudaMemcpyHostToDevice);
+    if (!in_descs.empty()) cudaMemcpy(base + oI, in_descs.data(), in_descs.size() * sizeof(InDesc), cudaMemcpyHostToDevice);
+    if (!out_descs.empty()) cudaMemcpy(base + oO, out_descs.data(), out_descs.size() * sizeof(OutDesc), cudaMemcpyHostToDevice);
+    int sms = b->plans[0]->num_sms;
+    for (auto& kr : in_r)
+        b->in_groups.push_back({static_cast<Xform>(kr.first.first), static_cast<OpType>(kr.first.second),
+                                reinterpret_cast<const InDesc*>(base + oI) + kr.second.first,
+                                static_cast<int>(kr.second.n), kr.second.total, kr.second.extra});
+    for (auto& kr : gemm_r)
+        b->gemm_groups.push_back({std::get<0>(kr.first), std::get<1>(kr.first) != 0,
+                                  static_cast<OpType>(std::get<2>(kr.first)),
+                                  reinterpret_cast<const GemmDesc*>(base + oG) + kr.second.first,
+                                  static_cast<int>(kr.second.n), kr.second.total,
+                                  static_cast<int>(std::min<long long>(kr.second.total, sms))});
+    for (auto& kr : out_r)
+        b->out_groups.push_back({static_cast<Xform>(kr.first.first), kr.first.second != 0,
+                                 reinterpret_cast<const OutDesc*>(base + oO) + kr.second.first,
+                                 static_cast<int>(kr.second.n), kr.second.total});
+    b->grouped_launches = static_cast<int>(b->scaled.size() + b->in_groups.size() + b->gemm_groups.size() +
+                                           b->out_groups.size() + b->fused.size());
+    if (cudaDeviceSynchronize() != cudaSuccess) return batch_fail(CONV2D_ERR_CUDA, "batch setup failed");
+    *out = b.release();
+    return CONV2D_OK;
+}
+
+int batch_run(Batch* b, cudaStream_t s) {
+    if (!b->graph) {
+        // first run: set every kernel up outside capture, then record the
+        // grouped launches once into a graph
+        cudaError_t e = b->launch_grouped(s);
+        if (e != cudaSuccess) return batch_fail(CONV2D_ERR_CUDA, cudaGetErrorString(e));
+        cudaStream_t cs;
+        cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
+        cudaGraph_t g = nullptr;
+        if (cudaStreamSynchronize(s) != cudaSuccess ||
+            cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+            cudaStreamDestroy(cs);
+            return batch_fail(CONV2D_ERR_CUDA, "graph capture could not start");
+        }
+        e = b->launch_grouped(cs);
+        cudaError_t e2 = cudaStreamEndCapture(cs, &g);
+        cudaStreamDestroy(cs);
+        if (e != cudaSuccess || e2 != cudaSuccess || !g) {
+            if (g) cudaGraphDestroy(g);
+            cudaGetLastError();
+            return batch_fail(CONV2D_ERR_CUDA, "graph capture failed");
+        }
+        e = cudaGraphInstantiate(&b->graph, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) {
+            b->graph = nullptr;
+            return batch_fail(CONV2D_ERR_CUDA, "graph instantiation failed");
+        }
+        return CONV2D_OK;
+    }
+    cudaError_t e = cudaGraphLaunch(b->graph, s);
+    if (e != cudaSuccess) return batch_fail(CONV2D_ERR_CUDA, cudaGetErrorString(e));
+    return CONV2D_OK;
+}
+
+int batch_run_percall(Batch* b, cudaStream_t s) {
+    for (auto& p : b->plans) {
+        int st = p->run(s);
+        if (st) return st;
+    }
+    return CONV2D_OK;
+}
+
+}  // namespace wg
+
+using namespace wg;
+
+extern "C" {
+
+int conv2d_batch_create(const problem_t* problems, int count, const conv2d_options_t* opt, conv2d_batch_t** out) {
+    Batch* b = nullptr;
+    const int st = batch_create(problems, count, opt, &b);
+    if (st == CONV2D_OK) *out = reinterpret_cast<conv2d_batch_t*>(b);
+    return st;
+}
+
+int conv2d_batch_run(conv2d_batch_t* batch, void* stream) {
+    if (!batch) return set_last_error(CONV2D_ERR_INVALID, "null batch");
+    return batch_run(reinterpret_cast<Batch*>(batch), static_cast<cudaStream_t>(stream));
+}
+
+int conv2d_batch_run_percall(conv2d_batch_t* batch, void* stream) {
+    if (!batch) return set_last_error(CONV2D_ERR_INVALID, "null batch");
+    return batch_run_percall(reinterpret_cast<Batch*>(batch), static_cast<cudaStream_t>(stream));
+}
+
+int conv2d_batch_info(const conv2d_batch_t* batch, int index, int* algo, int* gemm_bn) {
+    const Batch* b = reinterpret_cast<const Batch*>(batch);
+    if (!b || index < 0 || index >= static_cast<int>(b->plans.size())) return set_last_error(CONV2D_ERR_INVALID, "bad index");
+    const Plan& p = *b->plans[index];
+    if (algo) *algo = p.algo;
+    if (gemm_bn) *gemm_bn = p.algo == CONV2D_ALGO_2X3_FUSED ? 32 : p.gemm_full.bn;
+    return CONV2D_OK;
+}
+
+int conv2d_batch_launches(const conv2d_batch_t* batch, int grouped) {
+    const Batch* b = reinterpret_cast<const Batch*>(batch);
+    if (!b) return -1;
+    if (grouped) return b->grouped_launches;
+    int n = 0;
+    for (const auto& p : b->plans) n += p->launches;
+    return n;
+}
+
+int conv2d_batch_check_device(conv2d_batch_t* batch, int* site) {
+    Batch* b = reinterpret_cast<Batch*>(batch);
+    if (!b) return set_last_error(CONV2D_ERR_INVALID, "null batch");
+    if (cudaDeviceSynchronize() != cudaSuccess) return set_last_error(CONV2D_ERR_CUDA, "device synchronize failed");
+    unsigned code = 0;
+    DevErr h{};
+    cudaMemcpy(&h, b->err, sizeof(h), cudaMemcpyDeviceToHost);
+    code = h.code;
+    for (auto& p : b->plans) {
+        cudaMemcpy(&h, p->err, sizeof(h), cudaMemcpyDeviceToHost);
+        if (!code) code = h.code;
+    }
+    if (site) *site = static_cast<int>(code);
+    return code ? set_last_error(CONV2D_ERR_TIMEOUT, "a kernel gave up a bounded wait") : CONV2D_OK;
+}
+
+int conv2d_batch_destroy(conv2d_batch_t* batch) {
+    Batch* b = reinterpret_cast<Batch*>(batch);
+    if (!b) return set_last_error(CONV2D_ERR_INVALID, "null batch");
+    cudaDeviceSynchronize();
+    delete b;
+    return CONV2D_OK;
+}
+
+}  // extern "C"

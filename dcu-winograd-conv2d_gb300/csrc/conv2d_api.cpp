@@ -217,14 +217,14 @@ int Plan::build(const problem_t* pr, const conv2d_options_t* opt_in) {
         info_smem = fused.smem_bytes;
     } else {
         const int bn = opt.gemm_bn ? opt.gemm_bn : default_bn(g.k);
-        ce = plan_gemm(gemm_full, op, E, Pc, g.k, g.kp, g.cp, V, U, m_fp32, bn, num_sms);
+        ce = plan_gemm(gemm_full, op, E, Pc, g.k, g.kp, g.cp, V, U, Mw, m_fp32, bn, num_sms);
         if (ce != cudaSuccess) return cuda_fail(ce, "GEMM plan (tensor maps)");
         n_chunks = (static_cast<int>(pr->n) + chunk_n - 1) / chunk_n;
         const int tail_n = static_cast<int>(pr->n) - (n_chunks - 1) * chunk_n;
         has_tail = tail_n != chunk_n;
         if (has_tail) {
             const long long Pt = static_cast<long long>(tail_n) * g.tiles_h * g.tiles_w;
-            ce = plan_gemm(gemm_tail, op, E, Pt, g.k, g.kp, g.cp, V, U, m_fp32, bn, num_sms);
+            ce = plan_gemm(gemm_tail, op, E, Pt, g.k, g.kp, g.cp, V, U, Mw, m_fp32, bn, num_sms);
             if (ce != cudaSuccess) return cuda_fail(ce, "GEMM plan (tail)");
         }
         launches = n_chunks * (3 + (scaling ? 1 : 0));
@@ -279,7 +279,7 @@ int Plan::run(cudaStream_t s) {
         if (ce != cudaSuccess) return cuda_fail(ce, "input transform launch");
         mark(s);
         const GemmPlan& gp = (has_tail && ci == n_chunks - 1) ? gemm_tail : gemm_full;
-        ce = launch_gemm(gp, Mw, err, s);
+        ce = launch_gemm(gp, err, s);
         if (ce != cudaSuccess) return cuda_fail(ce, "GEMM launch");
         mark(s);
         ce = launch_output_transform(xf, m_fp32, gc, Mw, yout, scale, s);

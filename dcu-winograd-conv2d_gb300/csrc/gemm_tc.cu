@@ -8,16 +8,18 @@
 //
 // Design (one persistent CTA per SM, 192 threads):
 //   warp 0      TMA producer: 128 tiles x 64 channels of V plus BN x 64 of U
-//               per stage, as 4-D boxes of 8 granules (16-byte rows) that land
-//               in the canonical no-swizzle K-major layout; S-stage ring;
+//               per stage, as 4-D boxes of 8 granules that land in the
+//               canonical no-swizzle K-major layout; S-stage mbarrier ring;
 //   warp 1      allocates TMEM and issues tcgen05.mma (M=128, N=BN, K=16)
 //               from one thread; accumulators double-buffered in TMEM so the
 //               epilogue of one output tile overlaps the main loop of the next;
 //   warps 2-5   epilogue: tcgen05.ld 32 lanes x 16 columns, convert, 16-byte
 //               granule stores of M (a warp writes 512 contiguous bytes).
-// Output tiles are (e, 128-tile block, BN-channel block), handed out round
-// robin; channel blocks of one (e, tile block) are adjacent so the V tile is
-// reused from L2.
+// Work items are (problem, e, 128-tile block, BN-channel block), handed out
+// round robin over one global index; a grouped launch covers many problems
+// (each with its own tensor maps, sizes and output) in one persistent grid.
+// Within a problem, channel blocks of one (e, tile block) are adjacent so the
+// V tile is reused from L2.
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 #include <cudaTypedefs.h>
@@ -80,11 +82,26 @@ __device__ __forceinline__ void store16<float>(float* Mw, const uint32_t (&r)[16
                 make_uint4(r[4 * j], r[4 * j + 1], r[4 * j + 2], r[4 * j + 3]);
 }
 
+// Work item t -> problem index (advanced monotonically) and (e, mb, nb).
+struct Item {
+    int e, mb, nb;
+};
+
+__device__ __forceinline__ Item locate(const GemmDesc* __restrict__ descs, int ndesc, long long t, int& pi) {
+    while (pi + 1 < ndesc && t >= descs[pi + 1].tile_begin) ++pi;
+    const GemmDesc& d = descs[pi];
+    const long long local = t - d.tile_begin;
+    Item it;
+    it.nb = static_cast<int>(local % d.n_blocks);
+    const long long rest = local / d.n_blocks;
+    it.mb = static_cast<int>(rest % d.m_blocks);
+    it.e = static_cast<int>(rest / d.m_blocks);
+    return it;
+}
+
 template <int BN, bool BF16, class MT>
-__global__ void __launch_bounds__(192, 1)
-    wino_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
-                     MT* __restrict__ Mw, int P, int kg_count, int m_blocks, int n_blocks, int k_blocks,
-                     int total_tiles, DevErr* err) {
+__device__ __forceinline__ void gemm_body(const GemmDesc* __restrict__ descs, int ndesc, long long total_tiles,
+                                          DevErr* err) {
     using Cfg = GemmCfg<BN>;
     constexpr int S = Cfg::kStages;
     constexpr uint32_t kIdesc = make_idesc_f16(kBM, BN, BF16);
@@ -116,8 +133,6 @@ __global__ void __launch_bounds__(192, 1)
         }
         *abort_flag = 0;
         fence_barrier_init();
-        tma_prefetch_desc(&tmA);
-        tma_prefetch_desc(&tmB);
     }
     if (warp == 1) tmem_alloc(tmem_slot, Cfg::kTmemCols);
     tc_fence_before();
@@ -129,20 +144,24 @@ __global__ void __launch_bounds__(192, 1)
         if (lane == 0) {
             int stage = 0;
             uint32_t phase = 0;
-            for (int t = blockIdx.x; t < total_tiles; t += gridDim.x) {
-                const int nb = t % n_blocks;
-                const int rest = t / n_blocks;
-                const int mb = rest % m_blocks;
-                const int e = rest / m_blocks;
+            int pi = 0, prefetched = -1;
+            for (long long t = blockIdx.x; t < total_tiles; t += gridDim.x) {
+                const Item it = locate(descs, ndesc, t, pi);
+                const GemmDesc& d = descs[pi];
+                if (prefetched != pi) {
+                    tma_prefetch_desc(&d.tmA);
+                    tma_prefetch_desc(&d.tmB);
+                    prefetched = pi;
+                }
                 bool ok = true;
-                for (int kb = 0; kb < k_blocks; ++kb) {
+                for (int kb = 0; kb < d.k_blocks; ++kb) {
                     if (!mbar_wait(&empty[stage], phase ^ 1u, abort_flag, err, ERR_SITE_EMPTY)) {
                         ok = false;
                         break;
                     }
                     mbar_arrive_expect_tx(&full[stage], Cfg::kStageBytes);
-                    tma_load_4d(sA + stage * kTileABytes, &tmA, &full[stage], 0, mb * (kBM / 8), kb * 8, e);
-                    tma_load_4d(sB + stage * Cfg::kTileB, &tmB, &full[stage], 0, nb * (BN / 8), kb * 8, e);
+                    tma_load_4d(sA + stage * kTileABytes, &d.tmA, &full[stage], 0, it.mb * (kBM / 8), kb * 8, it.e);
+                    tma_load_4d(sB + stage * Cfg::kTileB, &d.tmB, &full[stage], 0, it.nb * (BN / 8), kb * 8, it.e);
                     if (++stage == S) {
                         stage = 0;
                         phase ^= 1u;
@@ -157,7 +176,10 @@ __global__ void __launch_bounds__(192, 1)
             uint32_t phase = 0;
             int acc = 0;
             uint32_t acc_phase = 0;
-            for (int t = blockIdx.x; t < total_tiles; t += gridDim.x) {
+            int pi = 0;
+            for (long long t = blockIdx.x; t < total_tiles; t += gridDim.x) {
+                locate(descs, ndesc, t, pi);
+                const int k_blocks = descs[pi].k_blocks;
                 if (!mbar_wait(&tempty[acc], acc_phase ^ 1u, abort_flag, err, ERR_SITE_TMEM_EMPTY)) break;
                 tc_fence_after();
                 const uint32_t d_tmem = tmem_base + static_cast<uint32_t>(acc * BN);
@@ -197,21 +219,23 @@ __global__ void __launch_bounds__(192, 1)
         const int row = quarter * 32 + lane;
         int acc = 0;
         uint32_t acc_phase = 0;
-        for (int t = blockIdx.x; t < total_tiles; t += gridDim.x) {
-            const int nb = t % n_blocks;
-            const int rest = t / n_blocks;
-            const int mb = rest % m_blocks;
-            const int e = rest / m_blocks;
+        int pi = 0;
+        for (long long t = blockIdx.x; t < total_tiles; t += gridDim.x) {
+            const Item it = locate(descs, ndesc, t, pi);
+            const GemmDesc& d = descs[pi];
+            MT* Mw = static_cast<MT*>(d.Mw);
+            const long long P = d.P;
+            const int kg_count = d.kg_count;
             if (!mbar_wait(&tfull[acc], acc_phase, abort_flag, err, ERR_SITE_TMEM_FULL)) break;
             tc_fence_after();
-            const int p = mb * kBM + row;
+            const long long p = static_cast<long long>(it.mb) * kBM + row;
             const uint32_t taddr = tmem_base + (static_cast<uint32_t>(quarter * 32) << 16) + static_cast<uint32_t>(acc * BN);
 #pragma unroll 1
             for (int c0 = 0; c0 < BN; c0 += 16) {
                 uint32_t r[16];
                 tmem_ld_x16(taddr + c0, r);
                 tc_wait_ld();
-                if (p < P) store16<MT>(Mw, r, P, p, nb * BN + c0, kg_count, e);
+                if (p < P) store16<MT>(Mw, r, P, p, it.nb * BN + c0, kg_count, it.e);
             }
             tc_fence_before();
             mbar_arrive(&tempty[acc]);
@@ -236,23 +260,61 @@ __global__ void __launch_bounds__(192, 1)
 }
 
 template <int BN, bool BF16, class MT>
-cudaError_t gemm_launch(const GemmPlan& gp, void* Mw, DevErr* err, cudaStream_t s) {
+__global__ void __launch_bounds__(192, 1) wino_gemm_kernel(const __grid_constant__ GemmDesc d, DevErr* err) {
+    gemm_body<BN, BF16, MT>(&d, 1, d.tiles, err);
+}
+
+template <int BN, bool BF16, class MT>
+__global__ void __launch_bounds__(192, 1)
+    wino_gemm_grouped(const GemmDesc* __restrict__ descs, int ndesc, long long total_tiles, DevErr* err) {
+    gemm_body<BN, BF16, MT>(descs, ndesc, total_tiles, err);
+}
+
+template <int BN, bool BF16, class MT>
+cudaError_t gemm_launch(const GemmDesc& d, int grid, DevErr* err, cudaStream_t s) {
     auto kern = wino_gemm_kernel<BN, BF16, MT>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, GemmCfg<BN>::kSmem);
     if (e != cudaSuccess) return e;
-    const int total = gp.E * gp.m_blocks * gp.n_blocks;
-    const int kg_count = gp.m_fp32 ? gp.Kp / 4 : gp.Kp / 8;
-    kern<<<gp.grid, 192, GemmCfg<BN>::kSmem, s>>>(gp.tmA, gp.tmB, static_cast<MT*>(Mw), gp.P, kg_count, gp.m_blocks,
-                                                  gp.n_blocks, gp.k_blocks, total, err);
+    kern<<<grid, 192, GemmCfg<BN>::kSmem, s>>>(d, err);
     return cudaGetLastError();
 }
 
+template <int BN, bool BF16, class MT>
+cudaError_t gemm_grouped_launch(const GemmDesc* descs, int ndesc, long long total, int grid, DevErr* err,
+                                cudaStream_t s) {
+    auto kern = wino_gemm_grouped<BN, BF16, MT>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, GemmCfg<BN>::kSmem);
+    if (e != cudaSuccess) return e;
+    kern<<<grid, 192, GemmCfg<BN>::kSmem, s>>>(descs, ndesc, total, err);
+    return cudaGetLastError();
+}
+
+// One template instance per (BN, operand type, M type); `single` selects the
+// one-problem kernel (descriptor by value) or the grouped one (device array).
 template <int BN>
-cudaError_t gemm_dispatch_bn(const GemmPlan& gp, void* Mw, DevErr* err, cudaStream_t s) {
-    const bool bf = gp.op == OpType::BF16;
-    if (gp.m_fp32)
-        return bf ? gemm_launch<BN, true, float>(gp, Mw, err, s) : gemm_launch<BN, false, float>(gp, Mw, err, s);
-    return bf ? gemm_launch<BN, true, __half>(gp, Mw, err, s) : gemm_launch<BN, false, __half>(gp, Mw, err, s);
+cudaError_t dispatch_types(bool bf, bool m_fp32, bool single, const GemmDesc* d, int ndesc, long long total, int grid,
+                           DevErr* err, cudaStream_t s) {
+    if (single) {
+        if (m_fp32)
+            return bf ? gemm_launch<BN, true, float>(*d, grid, err, s) : gemm_launch<BN, false, float>(*d, grid, err, s);
+        return bf ? gemm_launch<BN, true, __half>(*d, grid, err, s) : gemm_launch<BN, false, __half>(*d, grid, err, s);
+    }
+    if (m_fp32)
+        return bf ? gemm_grouped_launch<BN, true, float>(d, ndesc, total, grid, err, s)
+                  : gemm_grouped_launch<BN, false, float>(d, ndesc, total, grid, err, s);
+    return bf ? gemm_grouped_launch<BN, true, __half>(d, ndesc, total, grid, err, s)
+              : gemm_grouped_launch<BN, false, __half>(d, ndesc, total, grid, err, s);
+}
+
+cudaError_t dispatch(int bn, bool bf, bool m_fp32, bool single, const GemmDesc* d, int ndesc, long long total, int grid,
+                     DevErr* err, cudaStream_t s) {
+    switch (bn) {
+        case 32: return dispatch_types<32>(bf, m_fp32, single, d, ndesc, total, grid, err, s);
+        case 64: return dispatch_types<64>(bf, m_fp32, single, d, ndesc, total, grid, err, s);
+        case 128: return dispatch_types<128>(bf, m_fp32, single, d, ndesc, total, grid, err, s);
+        case 256: return dispatch_types<256>(bf, m_fp32, single, d, ndesc, total, grid, err, s);
+    }
+    return cudaErrorInvalidValue;
 }
 
 }  // namespace
@@ -274,7 +336,7 @@ CUresult encode_tiled(CUtensorMap* map, CUtensorMapDataType dt, cuuint32_t rank,
               CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
 }
 
-static int gemm_smem(int bn) {
+int gemm_smem_bytes(int bn) {
     switch (bn) {
         case 32: return GemmCfg<32>::kSmem;
         case 64: return GemmCfg<64>::kSmem;
@@ -283,24 +345,19 @@ static int gemm_smem(int bn) {
     }
 }
 
-cudaError_t plan_gemm(GemmPlan& gp, OpType op, int E, long long P, int K, int Kp, int Cp, const void* V,
-                      const void* U, bool m_fp32, int bn, int num_sms) {
+cudaError_t make_gemm_desc(GemmDesc& d, OpType op, int E, long long P, int K, int Kp, int Cp, const void* V,
+                           const void* U, void* Mw, bool m_fp32, int bn) {
     if (bn != 32 && bn != 64 && bn != 128 && bn != 256) return cudaErrorInvalidValue;
     if (P <= 0 || P > 0x7fffffffLL || Cp % 8 != 0 || Kp % 8 != 0) return cudaErrorInvalidValue;
-    gp.op = op;
-    gp.bn = bn;
-    gp.E = E;
-    gp.P = static_cast<int>(P);
-    gp.K = K;
-    gp.Kp = Kp;
-    gp.Cp = Cp;
-    gp.m_fp32 = m_fp32;
-    gp.m_blocks = static_cast<int>((P + kBM - 1) / kBM);
-    gp.n_blocks = (K + bn - 1) / bn;
-    gp.k_blocks = (Cp + kBK - 1) / kBK;
-    const long long total = static_cast<long long>(E) * gp.m_blocks * gp.n_blocks;
-    gp.grid = static_cast<int>(std::min<long long>(total, num_sms));
-    gp.smem_bytes = gemm_smem(bn);
+    d.Mw = Mw;
+    d.P = static_cast<int>(P);
+    d.kg_count = m_fp32 ? Kp / 4 : Kp / 8;
+    d.m_blocks = static_cast<int>((P + kBM - 1) / kBM);
+    d.n_blocks = (K + bn - 1) / bn;
+    d.k_blocks = (Cp + kBK - 1) / kBK;
+    d.E = E;
+    d.tile_begin = 0;
+    d.tiles = static_cast<long long>(E) * d.m_blocks * d.n_blocks;
     const CUtensorMapDataType dt = op == OpType::BF16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT16;
     // V[E][CG][Pp][8] and U[E][CG][Kp][8] viewed as rows of 64 elements (8
     // tiles or output channels x one granule = 128 contiguous bytes): a box of
@@ -313,7 +370,7 @@ cudaError_t plan_gemm(GemmPlan& gp, OpType op, int E, long long P, int K, int Kp
         cuuint64_t dims[4] = {64, Pr, CG, static_cast<cuuint64_t>(E)};
         cuuint64_t strides[3] = {128, Pr * 128, CG * Pr * 128};
         cuuint32_t box[4] = {64, kBM / 8, 8, 1};
-        if (encode_tiled(&gp.tmA, dt, 4, const_cast<void*>(V), dims, strides, box, CU_TENSOR_MAP_SWIZZLE_NONE) !=
+        if (encode_tiled(&d.tmA, dt, 4, const_cast<void*>(V), dims, strides, box, CU_TENSOR_MAP_SWIZZLE_NONE) !=
             CUDA_SUCCESS)
             return cudaErrorInvalidValue;
     }
@@ -321,21 +378,32 @@ cudaError_t plan_gemm(GemmPlan& gp, OpType op, int E, long long P, int K, int Kp
         cuuint64_t dims[4] = {64, Kr, CG, static_cast<cuuint64_t>(E)};
         cuuint64_t strides[3] = {128, Kr * 128, CG * Kr * 128};
         cuuint32_t box[4] = {64, static_cast<cuuint32_t>(bn / 8), 8, 1};
-        if (encode_tiled(&gp.tmB, dt, 4, const_cast<void*>(U), dims, strides, box, CU_TENSOR_MAP_SWIZZLE_NONE) !=
+        if (encode_tiled(&d.tmB, dt, 4, const_cast<void*>(U), dims, strides, box, CU_TENSOR_MAP_SWIZZLE_NONE) !=
             CUDA_SUCCESS)
             return cudaErrorInvalidValue;
     }
     return cudaSuccess;
 }
 
-cudaError_t launch_gemm(const GemmPlan& gp, void* Mw, DevErr* err, cudaStream_t stream) {
-    switch (gp.bn) {
-        case 32: return gemm_dispatch_bn<32>(gp, Mw, err, stream);
-        case 64: return gemm_dispatch_bn<64>(gp, Mw, err, stream);
-        case 128: return gemm_dispatch_bn<128>(gp, Mw, err, stream);
-        case 256: return gemm_dispatch_bn<256>(gp, Mw, err, stream);
-    }
-    return cudaErrorInvalidValue;
+cudaError_t plan_gemm(GemmPlan& gp, OpType op, int E, long long P, int K, int Kp, int Cp, const void* V,
+                      const void* U, void* Mw, bool m_fp32, int bn, int num_sms) {
+    cudaError_t e = make_gemm_desc(gp.desc, op, E, P, K, Kp, Cp, V, U, Mw, m_fp32, bn);
+    if (e != cudaSuccess) return e;
+    gp.op = op;
+    gp.bn = bn;
+    gp.m_fp32 = m_fp32;
+    gp.grid = static_cast<int>(std::min<long long>(gp.desc.tiles, num_sms));
+    gp.smem_bytes = gemm_smem_bytes(bn);
+    return cudaSuccess;
+}
+
+cudaError_t launch_gemm(const GemmPlan& gp, DevErr* err, cudaStream_t stream) {
+    return dispatch(gp.bn, gp.op == OpType::BF16, gp.m_fp32, true, &gp.desc, 1, gp.desc.tiles, gp.grid, err, stream);
+}
+
+cudaError_t launch_gemm_grouped(const GemmDesc* descs, int ndesc, long long total_tiles, OpType op, bool m_fp32, int bn,
+                                int grid, DevErr* err, cudaStream_t stream) {
+    return dispatch(bn, op == OpType::BF16, m_fp32, false, descs, ndesc, total_tiles, grid, err, stream);
 }
 
 }  // namespace wg

@@ -142,18 +142,20 @@ constexpr int kInThreads = 256;
 // Staged input of one CTA: channel c's rows [ylo, yhi) (all W columns) start
 // at byte c*stride + (src & 15) of the staging buffer.
 template <class TF, class OutT>
-__global__ void __launch_bounds__(kInThreads, 2) input_transform_kernel(
-    const __half* __restrict__ x, const __half* __restrict__ x_end, OutT* __restrict__ V,
-    const float* __restrict__ scale, int C, int H, int W, int pad_h, int pad_w, int tiles_h, int tiles_w, long long Pp,
-    int CG, int tb, int nbh, int cb, int stride_bytes, DevErr* err) {
+__device__ __forceinline__ void input_body(const InDesc& d, int bx, int by, unsigned char* smem_raw, DevErr* err) {
     constexpr int M = TF::M, A = TF::ALPHA;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const __half* __restrict__ x = d.x;
+    OutT* __restrict__ V = static_cast<OutT*>(d.V);
+    const float* __restrict__ scale = d.scale;
+    const int C = d.C, H = d.H, W = d.W, pad_h = d.pad_h, pad_w = d.pad_w, tiles_h = d.tiles_h, tiles_w = d.tiles_w;
+    const long long Pp = d.Pp;
+    const int CG = d.CG, tb = d.tb, nbh = d.nbh, cb = d.cb, stride_bytes = d.stride_bytes;
     uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw);
     unsigned char* stage = smem_raw + 16;
 
-    const int bh = blockIdx.x % nbh;
-    const long long n = blockIdx.x / nbh;
-    const int c0 = blockIdx.y * cb;
+    const int bh = bx % nbh;
+    const long long n = bx / nbh;
+    const int c0 = by * cb;
     const int th0 = bh * tb;
     const int ntb = min(tb, tiles_h - th0);
     const int ylo = max(0, th0 * M - pad_h);
@@ -163,7 +165,7 @@ __global__ void __launch_bounds__(kInThreads, 2) input_transform_kernel(
     const long long plane = static_cast<long long>(H) * W;
     // bulk copies stop at the last 16-byte boundary of the input; the few
     // elements beyond it are read from global memory directly
-    const uintptr_t lim = reinterpret_cast<uintptr_t>(x_end) & ~uintptr_t(15);
+    const uintptr_t lim = reinterpret_cast<uintptr_t>(d.x_end) & ~uintptr_t(15);
 
     if (threadIdx.x == 0) {
         mbar_init(bar, cb);  // one arrival per channel of the block
@@ -276,9 +278,34 @@ __global__ void __launch_bounds__(kInThreads, 2) input_transform_kernel(
     }
 }
 
+template <class TF, class OutT>
+__global__ void __launch_bounds__(kInThreads, 2) input_transform_kernel(const __grid_constant__ InDesc d, DevErr* err) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    input_body<TF, OutT>(d, blockIdx.x, blockIdx.y, smem_raw, err);
+}
+
+// Many problems in one launch: CTA b belongs to the problem whose block range
+// [blk_begin, blk_begin + gx*gy) holds b.
+template <class TF, class OutT>
+__global__ void __launch_bounds__(kInThreads, 2) input_transform_grouped(const InDesc* __restrict__ descs, int ndesc,
+                                                                       DevErr* err) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const long long b = blockIdx.x;
+    int lo = 0, hi = ndesc - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) / 2;
+        if (descs[mid].blk_begin <= b) lo = mid; else hi = mid - 1;
+    }
+    const InDesc& d = descs[lo];
+    const long long local = b - d.blk_begin;
+    input_body<TF, OutT>(d, static_cast<int>(local % d.gx), static_cast<int>(local / d.gx), smem_raw, err);
+}
+
 // ---- output transform ----------------------------------------------------------
 // One thread per (tile, 16-byte granule of M); lanes over consecutive tiles,
 // so both the M reads and the NCHW row writes of a warp are contiguous.
+
+constexpr int kOutThreads = 128;
 
 template <class MT> struct MG;  // 8-byte half granule: 4 fp16 or 2 fp32 channels
 template <> struct MG<__half> {
@@ -317,17 +344,19 @@ __device__ __forceinline__ void store_row(__half* dst, const float* y, int valid
 }
 
 template <class TF, class MT>
-__global__ void __launch_bounds__(128) output_transform_kernel(const MT* __restrict__ Mw, __half* __restrict__ out,
-                                                               const float* __restrict__ scale, int K, int OH, int OW,
-                                                               int tiles_h, int tiles_w, long long P, int KG) {
+__device__ __forceinline__ void output_body(const OutDesc& d, long long bx, int g) {
     constexpr int M = TF::M, A = TF::ALPHA;
     constexpr int PG = MG<MT>::kPerGranule, PH = MG<MT>::kPerHalf;
+    const MT* __restrict__ Mw = static_cast<const MT*>(d.Mw);
+    __half* __restrict__ out = d.out;
+    const float* __restrict__ scale = d.scale;
+    const int K = d.K, OH = d.OH, OW = d.OW, tiles_h = d.tiles_h, tiles_w = d.tiles_w, KG = d.KG;
+    const long long P = d.P;
     // thread = (tile, half granule): two consecutive lanes read the two halves
     // of one 16-byte granule row, so a warp reads 256 contiguous bytes
-    const long long task = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+    const long long task = bx * kOutThreads + threadIdx.x;
     const int hh = static_cast<int>(task & 1);
     const long long p = task >> 1;
-    const int g = blockIdx.y;
     if (p >= P) return;
     const int tw = static_cast<int>(p % tiles_w);
     const long long r = p / tiles_w;
@@ -356,6 +385,24 @@ __global__ void __launch_bounds__(128) output_transform_kernel(const MT* __restr
     }
 }
 
+template <class TF, class MT>
+__global__ void __launch_bounds__(kOutThreads) output_transform_kernel(const __grid_constant__ OutDesc d) {
+    output_body<TF, MT>(d, blockIdx.x, blockIdx.y);
+}
+
+template <class TF, class MT>
+__global__ void __launch_bounds__(kOutThreads) output_transform_grouped(const OutDesc* __restrict__ descs, int ndesc) {
+    const long long b = blockIdx.x;
+    int lo = 0, hi = ndesc - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) / 2;
+        if (descs[mid].blk_begin <= b) lo = mid; else hi = mid - 1;
+    }
+    const OutDesc& d = descs[lo];
+    const long long local = b - d.blk_begin;
+    output_body<TF, MT>(d, local % d.gx, static_cast<int>(local / d.gx));
+}
+
 struct InBlocking {
     int tb, nbh, cb, stride, smem;
 };
@@ -382,26 +429,33 @@ InBlocking choose_in_blocking(const Geom& g) {
 }
 
 template <class TF, class OutT>
-cudaError_t input_launch(const Geom& g, const void* x, const void* x_end, void* V, const float* scale, DevErr* err,
-                         cudaStream_t s) {
-    const InBlocking b = choose_in_blocking(g);
+cudaError_t input_launch(const InDesc& d, int smem, DevErr* err, cudaStream_t s) {
     auto kern = input_transform_kernel<TF, OutT>;
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, b.smem);
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e != cudaSuccess) return e;
-    dim3 grid(static_cast<unsigned>(static_cast<long long>(g.n) * b.nbh), (g.c + b.cb - 1) / b.cb);
-    kern<<<grid, kInThreads, b.smem, s>>>(static_cast<const __half*>(x), static_cast<const __half*>(x_end),
-                                          static_cast<OutT*>(V), scale, g.c, g.h, g.w, g.pad_h, g.pad_w, g.tiles_h,
-                                          g.tiles_w, round_rows(g.P), g.cp / 8, b.tb, b.nbh, b.cb, b.stride, err);
+    kern<<<dim3(static_cast<unsigned>(d.gx), static_cast<unsigned>(d.gy)), kInThreads, smem, s>>>(d, err);
+    return cudaGetLastError();
+}
+
+template <class TF, class OutT>
+cudaError_t input_grouped_launch(const InDesc* descs, int ndesc, long long blocks, int smem, DevErr* err,
+                                 cudaStream_t s) {
+    auto kern = input_transform_grouped<TF, OutT>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return e;
+    kern<<<static_cast<unsigned>(blocks), kInThreads, smem, s>>>(descs, ndesc, err);
     return cudaGetLastError();
 }
 
 template <class TF, class MT>
-cudaError_t output_launch(const Geom& g, const void* Mw, void* out, const float* scale, cudaStream_t s) {
-    constexpr int PG = MG<MT>::kPerGranule;
-    const int KG = g.kp / PG;
-    dim3 grid(static_cast<unsigned>((2 * g.P + 127) / 128), KG);
-    output_transform_kernel<TF, MT><<<grid, 128, 0, s>>>(static_cast<const MT*>(Mw), static_cast<__half*>(out), scale,
-                                                         g.k, g.oh, g.ow, g.tiles_h, g.tiles_w, g.P, KG);
+cudaError_t output_launch(const OutDesc& d, cudaStream_t s) {
+    output_transform_kernel<TF, MT><<<dim3(static_cast<unsigned>(d.gx), static_cast<unsigned>(d.gy)), kOutThreads, 0, s>>>(d);
+    return cudaGetLastError();
+}
+
+template <class TF, class MT>
+cudaError_t output_grouped_launch(const OutDesc* descs, int ndesc, long long blocks, cudaStream_t s) {
+    output_transform_grouped<TF, MT><<<static_cast<unsigned>(blocks), kOutThreads, 0, s>>>(descs, ndesc);
     return cudaGetLastError();
 }
 
@@ -445,35 +499,99 @@ cudaError_t launch_tile_scale(const Geom& g, const void* x, float* scale, cudaSt
     return cudaGetLastError();
 }
 
+InDesc make_in_desc(const Geom& g, const void* x, const void* x_end, void* V, const float* scale, int* smem) {
+    const InBlocking b = choose_in_blocking(g);
+    InDesc d{};
+    d.x = static_cast<const __half*>(x);
+    d.x_end = static_cast<const __half*>(x_end);
+    d.V = V;
+    d.scale = scale;
+    d.C = g.c; d.H = g.h; d.W = g.w; d.pad_h = g.pad_h; d.pad_w = g.pad_w;
+    d.tiles_h = g.tiles_h; d.tiles_w = g.tiles_w;
+    d.Pp = round_rows(g.P);
+    d.CG = g.cp / 8;
+    d.tb = b.tb; d.nbh = b.nbh; d.cb = b.cb; d.stride_bytes = b.stride;
+    d.gx = static_cast<long long>(g.n) * b.nbh;
+    d.gy = (g.c + b.cb - 1) / b.cb;
+    d.blk_begin = 0;
+    *smem = b.smem;
+    return d;
+}
+
+OutDesc make_out_desc(const Geom& g, bool m_fp32, const void* Mw, void* out, const float* scale) {
+    OutDesc d{};
+    d.Mw = Mw;
+    d.out = static_cast<__half*>(out);
+    d.scale = scale;
+    d.K = g.k; d.OH = g.oh; d.OW = g.ow; d.tiles_h = g.tiles_h; d.tiles_w = g.tiles_w;
+    d.P = g.P;
+    d.KG = m_fp32 ? g.kp / 4 : g.kp / 8;
+    d.gx = (2 * g.P + kOutThreads - 1) / kOutThreads;
+    d.gy = d.KG;
+    d.blk_begin = 0;
+    return d;
+}
+
 cudaError_t launch_input_transform(Xform xf, OpType op, const Geom& g, const void* x, const void* x_end, void* V,
                                    const float* scale, DevErr* err, cudaStream_t stream) {
+    int smem = 0;
+    const InDesc d = make_in_desc(g, x, x_end, V, scale, &smem);
     const bool bf = op == OpType::BF16;
     switch (xf) {
         case Xform::F2:
-            return bf ? input_launch<F2, __nv_bfloat16>(g, x, x_end, V, scale, err, stream)
-                      : input_launch<F2, __half>(g, x, x_end, V, scale, err, stream);
+            return bf ? input_launch<F2, __nv_bfloat16>(d, smem, err, stream) : input_launch<F2, __half>(d, smem, err, stream);
         case Xform::F4:
-            return bf ? input_launch<F4, __nv_bfloat16>(g, x, x_end, V, scale, err, stream)
-                      : input_launch<F4, __half>(g, x, x_end, V, scale, err, stream);
+            return bf ? input_launch<F4, __nv_bfloat16>(d, smem, err, stream) : input_launch<F4, __half>(d, smem, err, stream);
         case Xform::F4Ref:
-            return bf ? input_launch<F4Ref, __nv_bfloat16>(g, x, x_end, V, scale, err, stream)
-                      : input_launch<F4Ref, __half>(g, x, x_end, V, scale, err, stream);
+            return bf ? input_launch<F4Ref, __nv_bfloat16>(d, smem, err, stream)
+                      : input_launch<F4Ref, __half>(d, smem, err, stream);
+    }
+    return cudaErrorInvalidValue;
+}
+
+cudaError_t launch_input_transform_grouped(Xform xf, OpType op, const InDesc* descs, int ndesc, long long blocks,
+                                           int smem, DevErr* err, cudaStream_t stream) {
+    const bool bf = op == OpType::BF16;
+    switch (xf) {
+        case Xform::F2:
+            return bf ? input_grouped_launch<F2, __nv_bfloat16>(descs, ndesc, blocks, smem, err, stream)
+                      : input_grouped_launch<F2, __half>(descs, ndesc, blocks, smem, err, stream);
+        case Xform::F4:
+            return bf ? input_grouped_launch<F4, __nv_bfloat16>(descs, ndesc, blocks, smem, err, stream)
+                      : input_grouped_launch<F4, __half>(descs, ndesc, blocks, smem, err, stream);
+        case Xform::F4Ref:
+            return bf ? input_grouped_launch<F4Ref, __nv_bfloat16>(descs, ndesc, blocks, smem, err, stream)
+                      : input_grouped_launch<F4Ref, __half>(descs, ndesc, blocks, smem, err, stream);
     }
     return cudaErrorInvalidValue;
 }
 
 cudaError_t launch_output_transform(Xform xf, bool m_fp32, const Geom& g, const void* Mw, void* out,
                                     const float* scale, cudaStream_t stream) {
+    const OutDesc d = make_out_desc(g, m_fp32, Mw, out, scale);
     switch (xf) {
         case Xform::F2:
-            return m_fp32 ? output_launch<F2, float>(g, Mw, out, scale, stream)
-                          : output_launch<F2, __half>(g, Mw, out, scale, stream);
+            return m_fp32 ? output_launch<F2, float>(d, stream) : output_launch<F2, __half>(d, stream);
         case Xform::F4:
-            return m_fp32 ? output_launch<F4, float>(g, Mw, out, scale, stream)
-                          : output_launch<F4, __half>(g, Mw, out, scale, stream);
+            return m_fp32 ? output_launch<F4, float>(d, stream) : output_launch<F4, __half>(d, stream);
         case Xform::F4Ref:
-            return m_fp32 ? output_launch<F4Ref, float>(g, Mw, out, scale, stream)
-                          : output_launch<F4Ref, __half>(g, Mw, out, scale, stream);
+            return m_fp32 ? output_launch<F4Ref, float>(d, stream) : output_launch<F4Ref, __half>(d, stream);
+    }
+    return cudaErrorInvalidValue;
+}
+
+cudaError_t launch_output_transform_grouped(Xform xf, bool m_fp32, const OutDesc* descs, int ndesc, long long blocks,
+                                            cudaStream_t stream) {
+    switch (xf) {
+        case Xform::F2:
+            return m_fp32 ? output_grouped_launch<F2, float>(descs, ndesc, blocks, stream)
+                          : output_grouped_launch<F2, __half>(descs, ndesc, blocks, stream);
+        case Xform::F4:
+            return m_fp32 ? output_grouped_launch<F4, float>(descs, ndesc, blocks, stream)
+                          : output_grouped_launch<F4, __half>(descs, ndesc, blocks, stream);
+        case Xform::F4Ref:
+            return m_fp32 ? output_grouped_launch<F4Ref, float>(descs, ndesc, blocks, stream)
+                          : output_grouped_launch<F4Ref, __half>(descs, ndesc, blocks, stream);
     }
     return cudaErrorInvalidValue;
 }

@@ -5,6 +5,7 @@
 #include <cstddef>
 #include <cstdint>
 #include <cuda.h>
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 namespace wg {
@@ -56,6 +57,42 @@ cudaError_t launch_tile_scale(const Geom& g, const void* x, float* scale, cudaSt
 cudaError_t launch_input_transform(Xform xf, OpType op, const Geom& g, const void* x, const void* x_end, void* V,
                                    const float* scale, DevErr* err, cudaStream_t stream);
 
+// Per-problem descriptors of the transform kernels (device-resident arrays of
+// them drive the grouped launches that run many problems at once).
+struct InDesc {
+    const __half* x;
+    const __half* x_end;
+    void* V;
+    const float* scale;
+    int C, H, W, pad_h, pad_w, tiles_h, tiles_w;
+    long long Pp;
+    int CG, tb, nbh, cb, stride_bytes;
+    long long gx;         // CTAs along (image, tile-row block)
+    int gy;               // CTAs along channel blocks
+    long long blk_begin;  // first CTA of this problem in a grouped launch
+};
+
+struct OutDesc {
+    const void* Mw;
+    __half* out;
+    const float* scale;
+    int K, OH, OW, tiles_h, tiles_w;
+    long long P;
+    int KG;
+    long long gx;         // CTAs along tiles
+    int gy;               // CTAs along granules
+    long long blk_begin;
+};
+
+// Descriptor of one problem's input transform and its dynamic shared memory.
+InDesc make_in_desc(const Geom& g, const void* x, const void* x_end, void* V, const float* scale, int* smem);
+OutDesc make_out_desc(const Geom& g, bool m_fp32, const void* Mw, void* out, const float* scale);
+// Grouped launches: `blocks` = sum of gx*gy; descs device-resident, sorted by blk_begin.
+cudaError_t launch_input_transform_grouped(Xform xf, OpType op, const InDesc* descs, int ndesc, long long blocks,
+                                           int smem, DevErr* err, cudaStream_t stream);
+cudaError_t launch_output_transform_grouped(Xform xf, bool m_fp32, const OutDesc* descs, int ndesc, long long blocks,
+                                            cudaStream_t stream);
+
 // out[N][K][OH][OW] = A^T M A from M[e][Kp/8][P][8] (fp16, m_fp32 false) or
 // M[e][Kp/4][P][4] (fp32); divides by scale[p] when scale is not null.
 cudaError_t launch_output_transform(Xform xf, bool m_fp32, const Geom& g, const void* Mw, void* out,
@@ -63,12 +100,20 @@ cudaError_t launch_output_transform(Xform xf, bool m_fp32, const Geom& g, const 
 
 // ---- tcgen05 batched GEMM: M_e[P][K] = V_e[P][Cp] * U_e[K][Cp]^T -----------
 // (operands and result in the 16-byte granule layouts above)
-struct GemmPlan {
+// One problem's GEMM: tensor maps of V and U, output, sizes, and its range of
+// the global work index when several problems share one launch.
+struct alignas(64) GemmDesc {
     CUtensorMap tmA;     // V
     CUtensorMap tmB;     // U
+    void* Mw;
+    int P, kg_count, m_blocks, n_blocks, k_blocks, E;
+    long long tile_begin;
+    long long tiles;     // E * m_blocks * n_blocks
+};
+
+struct GemmPlan {
+    GemmDesc desc;
     int bn;              // 32, 64, 128 or 256
-    int E, P, K, Kp, Cp;
-    int m_blocks, n_blocks, k_blocks;
     int grid;
     int smem_bytes;
     bool m_fp32;
@@ -76,9 +121,16 @@ struct GemmPlan {
 };
 
 // Builds the tensor maps; V, U, M must stay at these addresses.
+cudaError_t make_gemm_desc(GemmDesc& d, OpType op, int E, long long P, int K, int Kp, int Cp, const void* V,
+                           const void* U, void* Mw, bool m_fp32, int bn);
 cudaError_t plan_gemm(GemmPlan& gp, OpType op, int E, long long P, int K, int Kp, int Cp, const void* V,
-                      const void* U, bool m_fp32, int bn, int num_sms);
-cudaError_t launch_gemm(const GemmPlan& gp, void* Mw, DevErr* err, cudaStream_t stream);
+                      const void* U, void* Mw, bool m_fp32, int bn, int num_sms);
+cudaError_t launch_gemm(const GemmPlan& gp, DevErr* err, cudaStream_t stream);
+// Many problems (same BN, operand and M types) in one persistent launch; descs
+// device-resident (64-byte aligned), sorted by tile_begin.
+cudaError_t launch_gemm_grouped(const GemmDesc* descs, int ndesc, long long total_tiles, OpType op, bool m_fp32, int bn,
+                                int grid, DevErr* err, cudaStream_t stream);
+int gemm_smem_bytes(int bn);
 
 // ---- fused F(2x3): input transform + tcgen05 GEMM + output transform ------
 struct FusedPlan {

@@ -162,6 +162,26 @@ int conv2d_select_reference(const problem_t* problem);
 int conv2d_autotune(const problem_t* problem, const conv2d_options_t* opt, int* algo, int* gemm_bn);
 void conv2d_autotune_clear(void);
 
+/* ---- batches of uneven problems (no counterpart in the reference) -------- */
+
+/* Many convolutions of different shapes run together: one grouped launch per
+ * kernel family covers every problem (the GEMM as one persistent work queue of
+ * (problem, element, tile block, channel block) items), captured once into a
+ * CUDA graph and replayed.  Each problem's algorithm and GEMM tile follow
+ * `opt->algo` (CONV2D_ALGO_AUTO: per-shape autotuner).  Workspaces and
+ * transformed filters stay resident until conv2d_batch_destroy. */
+typedef struct conv2d_batch conv2d_batch_t;
+int conv2d_batch_create(const problem_t* problems, int count, const conv2d_options_t* opt, conv2d_batch_t** batch);
+/* Grouped run (the first call also records the graph). */
+int conv2d_batch_run(conv2d_batch_t* batch, void* stream);
+/* The same problems, one conv2d call after another (for comparison). */
+int conv2d_batch_run_percall(conv2d_batch_t* batch, void* stream);
+int conv2d_batch_info(const conv2d_batch_t* batch, int index, int* algo, int* gemm_bn);
+/* Kernel launches of one grouped (grouped != 0) or per-call run. */
+int conv2d_batch_launches(const conv2d_batch_t* batch, int grouped);
+int conv2d_batch_check_device(conv2d_batch_t* batch, int* site);
+int conv2d_batch_destroy(conv2d_batch_t* batch);
+
 /* One call with a CUDA event recorded on the stream after every kernel
  * launch; waits, writes each launch's duration (ms, launch order) to
  * kernel_ms and returns the number of launches (negative status on error). */
