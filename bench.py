@@ -555,6 +555,42 @@ def batch_arm(args):
     return 0
 
 
+def precision_arm(args):
+    """F(4x3) precision study on the N=32, C=512, H=W=28, K=512 shape (the batch
+    cut to --images images so the FP64 oracle finishes in seconds): for each
+    input distribution (N(0,1); N(0,1) with 1% of entries x64), operand type
+    (fp16, bf16), per-tile scaling (off, on) and F(4x3) point set, the max /
+    mean relative error |y - ref| / max(|ref|, rms(ref)) against the FP64 direct
+    convolution; F(2x3) rows for comparison."""
+    import torch
+    O = load_oracle()
+    if not os.path.exists(O.LIB_PATH):
+        O.build()
+    wg = load_pkg()
+    wg.lib()
+    n, c, h, k = args.images, 512, 28, 512
+    rows = []
+    for dist in ("normal", "heavy"):
+        x, wt = O.normal_inputs(2026, n, c, h, h, k, heavy=(dist == "heavy"))
+        _, r64 = O.conv2d_direct(x, wt, nthreads=os.cpu_count() or 1)
+        xt, wtt = torch.from_numpy(x).cuda(), torch.from_numpy(wt).cuda()
+        for algo, points in ((0, 0), (0, 1), (1, 0)):
+            for bf16 in (0, 1):
+                for scaling in ((0, 1) if algo == 0 else (0,)):
+                    opts = wg.default_options(algo=algo, operand_bf16=bf16, tile_scaling=scaling, f4_points=points)
+                    y, op = wg.conv2d_torch(xt, wtt, 1, 1, opts)
+                    torch.cuda.synchronize()
+                    mx, mean, l2 = O.rel_errors(y.cpu().numpy(), r64)
+                    rows.append({"input": dist, "algo": wg.ALGO_NAMES[algo],
+                                 "points": ("reference 0,+-1,+-2" if points else "0,+-1,1/2,-2") if algo == 0 else "-",
+                                 "operands": "bf16" if bf16 else "fp16", "tile_scaling": bool(scaling),
+                                 "max_rel": mx, "mean_rel": mean, "l2_rel": l2})
+                    op.destroy()
+    print(json.dumps({"study": "F(4x3) precision vs FP64 direct convolution", "shape": [n, c, h, h, k],
+                      "metric": "max/mean of |y-ref|/max(|ref|,rms(ref))", "rows": rows}), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -567,11 +603,15 @@ def main():
     ap.add_argument("--l2-chunk", type=int, default=None)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--precision", action="store_true", help="F(4x3) precision study instead of timing")
+    ap.add_argument("--images", type=int, default=4, help="images of the precision study")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
         return reference_arm(args)
+    if args.precision:
+        return precision_arm(args)
     if args.workload in BATCH_WORKLOADS:
         return batch_arm(args)
     return our_arm(args)
