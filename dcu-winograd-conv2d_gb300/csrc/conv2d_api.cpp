@@ -122,6 +122,11 @@ int default_bn(int K) {
 Plan::~Plan() { release(); }
 
 void Plan::release() {
+    if (host_in_stream) cudaStreamDestroy(host_in_stream);
+    if (host_out_stream) cudaStreamDestroy(host_out_stream);
+    for (cudaEvent_t& e : host_ev)
+        if (e) cudaEventDestroy(e);
+    host_in_stream = host_out_stream = nullptr;
     if (ws) cudaFree(ws);
     ws = nullptr;
     U = V = Mw = nullptr;
@@ -247,6 +252,37 @@ void Plan::mark(cudaStream_t s) {
     if (marks && n_marks < max_marks) cudaEventRecord(marks[n_marks++], s);
 }
 
+int Plan::run_range(int n0, int nc, const GemmPlan* gp, cudaStream_t s) {
+    cudaError_t ce;
+    const void* x_end = static_cast<const uint16_t*>(prob.in) + static_cast<long long>(prob.n) * g.c * g.h * g.w;
+    const long long in_img = static_cast<long long>(g.c) * g.h * g.w;
+    const long long out_img = static_cast<long long>(g.k) * g.oh * g.ow;
+    const Geom gc = make_geom(nc, g.c, g.h, g.w, g.k, g.pad_h, g.pad_w, g.m);
+    const uint16_t* xin = static_cast<const uint16_t*>(prob.in) + n0 * in_img;
+    uint16_t* yout = static_cast<uint16_t*>(prob.out) + n0 * out_img;
+    if (algo == CONV2D_ALGO_2X3_FUSED) {
+        ce = launch_fused2x3(fused, gc, xin, x_end, yout, err, s);
+        if (ce != cudaSuccess) return cuda_fail(ce, "fused F(2x3) launch");
+        mark(s);
+        return CONV2D_OK;
+    }
+    if (scaling) {
+        ce = launch_tile_scale(gc, xin, scale, s);
+        if (ce != cudaSuccess) return cuda_fail(ce, "tile scale launch");
+        mark(s);
+    }
+    ce = launch_input_transform(xf, op, gc, xin, x_end, V, scale, err, s);
+    if (ce != cudaSuccess) return cuda_fail(ce, "input transform launch");
+    mark(s);
+    ce = launch_gemm(*gp, err, s);
+    if (ce != cudaSuccess) return cuda_fail(ce, "GEMM launch");
+    mark(s);
+    ce = launch_output_transform(xf, m_fp32, gc, Mw, yout, scale, s);
+    if (ce != cudaSuccess) return cuda_fail(ce, "output transform launch");
+    mark(s);
+    return CONV2D_OK;
+}
+
 int Plan::run(cudaStream_t s) {
     int cur = -1;
     if (cudaGetDevice(&cur) == cudaSuccess && cur != device) cudaSetDevice(device);
@@ -254,38 +290,88 @@ int Plan::run(cudaStream_t s) {
         int st = filter(s);
         if (st) return st;
     }
-    cudaError_t ce;
-    const void* x_end = static_cast<const uint16_t*>(prob.in) + static_cast<long long>(prob.n) * g.c * g.h * g.w;
-    if (algo == CONV2D_ALGO_2X3_FUSED) {
-        ce = launch_fused2x3(fused, g, prob.in, x_end, prob.out, err, s);
-        if (ce != cudaSuccess) return cuda_fail(ce, "fused F(2x3) launch");
-        mark(s);
-        return CONV2D_OK;
-    }
-    const long long in_img = static_cast<long long>(g.c) * g.h * g.w;
-    const long long out_img = static_cast<long long>(g.k) * g.oh * g.ow;
+    if (algo == CONV2D_ALGO_2X3_FUSED) return run_range(0, static_cast<int>(prob.n), nullptr, s);
     for (int ci = 0; ci < n_chunks; ++ci) {
         const int n0 = ci * chunk_n;
         const int nc = std::min<int>(chunk_n, static_cast<int>(prob.n) - n0);
-        Geom gc = make_geom(nc, g.c, g.h, g.w, g.k, g.pad_h, g.pad_w, g.m);
-        const uint16_t* xin = static_cast<const uint16_t*>(prob.in) + n0 * in_img;
-        uint16_t* yout = static_cast<uint16_t*>(prob.out) + n0 * out_img;
-        if (scaling) {
-            ce = launch_tile_scale(gc, xin, scale, s);
-            if (ce != cudaSuccess) return cuda_fail(ce, "tile scale launch");
-            mark(s);
-        }
-        ce = launch_input_transform(xf, op, gc, xin, x_end, V, scale, err, s);
-        if (ce != cudaSuccess) return cuda_fail(ce, "input transform launch");
-        mark(s);
         const GemmPlan& gp = (has_tail && ci == n_chunks - 1) ? gemm_tail : gemm_full;
-        ce = launch_gemm(gp, err, s);
-        if (ce != cudaSuccess) return cuda_fail(ce, "GEMM launch");
-        mark(s);
-        ce = launch_output_transform(xf, m_fp32, gc, Mw, yout, scale, s);
-        if (ce != cudaSuccess) return cuda_fail(ce, "output transform launch");
-        mark(s);
+        const int st = run_range(n0, nc, &gp, s);
+        if (st) return st;
     }
+    return CONV2D_OK;
+}
+
+// Host input -> device -> host output.  The batch is cut into up to
+// kHostChunks image chunks; chunk i's input copy (copy-in stream), compute
+// (caller stream) and output copy (copy-out stream) are ordered by events, so
+// the copies of one chunk overlap the compute of its neighbours.
+int Plan::run_host(const void* host_in, void* host_out, cudaStream_t s) {
+    constexpr int kHostChunks = 4;
+    const int n = static_cast<int>(prob.n);
+    const long long in_img_b = static_cast<long long>(g.c) * g.h * g.w * 2;
+    const long long out_img_b = static_cast<long long>(g.k) * g.oh * g.ow * 2;
+    int cur = -1;
+    if (cudaGetDevice(&cur) == cudaSuccess && cur != device) cudaSetDevice(device);
+    if (!filter_ready || opt.filter_policy == 1) {
+        int st = filter(s);
+        if (st) return st;
+    }
+    const int chunks = std::min(n, kHostChunks);
+    const int hc = (n + chunks - 1) / chunks;
+    const int nch = (n + hc - 1) / hc;
+    if (!host_in_stream) {
+        if (cudaStreamCreateWithFlags(&host_in_stream, cudaStreamNonBlocking) != cudaSuccess ||
+            cudaStreamCreateWithFlags(&host_out_stream, cudaStreamNonBlocking) != cudaSuccess)
+            return fail(CONV2D_ERR_CUDA, "copy stream creation failed");
+        for (cudaEvent_t& e : host_ev)
+            if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess)
+                return fail(CONV2D_ERR_CUDA, "event creation failed");
+    }
+    if (algo != CONV2D_ALGO_2X3_FUSED && host_chunk_n != hc) {
+        const int E = g.alpha * g.alpha;
+        const int bn = gemm_full.bn;
+        const int tail = n - (nch - 1) * hc;
+        cudaError_t ce = plan_gemm(host_gemm_full, op, E, static_cast<long long>(hc) * g.tiles_h * g.tiles_w, g.k, g.kp,
+                                   g.cp, V, U, Mw, m_fp32, bn, num_sms);
+        if (ce == cudaSuccess)
+            ce = plan_gemm(host_gemm_tail, op, E, static_cast<long long>(tail) * g.tiles_h * g.tiles_w, g.k, g.kp, g.cp,
+                           V, U, Mw, m_fp32, bn, num_sms);
+        if (ce != cudaSuccess) return cuda_fail(ce, "GEMM plan (host chunks)");
+        host_chunk_n = hc;
+    }
+    cudaEvent_t* ev_in = host_ev;            // [kHostChunks]
+    cudaEvent_t* ev_done = host_ev + 8;      // [kHostChunks]
+    cudaEvent_t ev_start = host_ev[16], ev_end = host_ev[17];
+    // the copies must not overwrite the input before earlier work on s is done
+    cudaEventRecord(ev_start, s);
+    cudaStreamWaitEvent(host_in_stream, ev_start, 0);
+    for (int i = 0; i < nch; ++i) {
+        const int n0 = i * hc, nc = std::min(hc, n - n0);
+        cudaError_t ce = cudaMemcpyAsync(static_cast<char*>(prob.in) + n0 * in_img_b,
+                                         static_cast<const char*>(host_in) + n0 * in_img_b, nc * in_img_b,
+                                         cudaMemcpyHostToDevice, host_in_stream);
+        if (ce != cudaSuccess) return cuda_fail(ce, "input copy");
+        cudaEventRecord(ev_in[i], host_in_stream);
+    }
+    for (int i = 0; i < nch; ++i) {
+        const int n0 = i * hc, nc = std::min(hc, n - n0);
+        cudaStreamWaitEvent(s, ev_in[i], 0);
+        const int st = run_range(n0, nc, i == nch - 1 ? &host_gemm_tail : &host_gemm_full, s);
+        if (st) return st;
+        cudaEventRecord(ev_done[i], s);
+    }
+    for (int i = 0; i < nch; ++i) {
+        const int n0 = i * hc, nc = std::min(hc, n - n0);
+        cudaStreamWaitEvent(host_out_stream, ev_done[i], 0);
+        cudaError_t ce = cudaMemcpyAsync(static_cast<char*>(host_out) + n0 * out_img_b,
+                                         static_cast<const char*>(prob.out) + n0 * out_img_b, nc * out_img_b,
+                                         cudaMemcpyDeviceToHost, host_out_stream);
+        if (ce != cudaSuccess) return cuda_fail(ce, "output copy");
+    }
+    cudaEventRecord(ev_end, host_out_stream);
+    cudaStreamWaitEvent(s, ev_end, 0);
+    cudaError_t ce = cudaStreamSynchronize(s);
+    if (ce != cudaSuccess) return cuda_fail(ce, "stream sync");
     return CONV2D_OK;
 }
 
@@ -392,18 +478,7 @@ int conv2d_fp16_host(const void* param_ptr, const void* host_in, void* host_out,
     Plan* pl = plan_of(param_ptr);
     if (!pl) return fail(CONV2D_ERR_INVALID, "param blob not set up by getkernelInfo");
     if (!host_in || !host_out) return fail(CONV2D_ERR_INVALID, "null host buffer");
-    cudaStream_t s = static_cast<cudaStream_t>(stream);
-    const size_t in_bytes = static_cast<size_t>(pl->prob.n) * pl->g.c * pl->g.h * pl->g.w * 2;
-    const size_t out_bytes = static_cast<size_t>(pl->prob.n) * pl->g.k * pl->g.oh * pl->g.ow * 2;
-    cudaError_t ce = cudaMemcpyAsync(pl->prob.in, host_in, in_bytes, cudaMemcpyHostToDevice, s);
-    if (ce != cudaSuccess) return cuda_fail(ce, "input copy");
-    int st = pl->run(s);
-    if (st) return st;
-    ce = cudaMemcpyAsync(host_out, pl->prob.out, out_bytes, cudaMemcpyDeviceToHost, s);
-    if (ce != cudaSuccess) return cuda_fail(ce, "output copy");
-    ce = cudaStreamSynchronize(s);
-    if (ce != cudaSuccess) return cuda_fail(ce, "stream sync");
-    return CONV2D_OK;
+    return pl->run_host(host_in, host_out, static_cast<cudaStream_t>(stream));
 }
 
 int conv2d_refresh_filter(const void* param_ptr, void* stream) {

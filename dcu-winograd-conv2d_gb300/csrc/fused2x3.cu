@@ -430,7 +430,8 @@ cudaError_t plan_fused2x3(FusedPlan& fp, OpType op, const Geom& g, const void* U
 cudaError_t launch_fused2x3(const FusedPlan& fp, const Geom& g, const void* x, const void* x_end, void* out,
                             DevErr* err, cudaStream_t stream) {
     if (g.P > 0x7fffffffLL) return cudaErrorInvalidValue;
-    const long long blocks = static_cast<long long>(fp.m_blocks) * fp.n_blocks;
+    // tile blocks of this launch (a launch may cover a subset of the images)
+    const long long blocks = (g.P + kTilesPerCta - 1) / kTilesPerCta * fp.n_blocks;
     if (blocks > 0x7fffffffLL) return cudaErrorInvalidValue;
     auto kern = fp.op == OpType::BF16 ? fused2x3_kernel<true> : fused2x3_kernel<false>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, fp.smem_bytes);

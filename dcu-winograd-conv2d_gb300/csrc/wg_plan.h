@@ -56,11 +56,20 @@ struct Plan {
     // when set, run() records an event on the stream after every launch
     cudaEvent_t* marks = nullptr;
     int n_marks = 0, max_marks = 0;
+    // host-buffer pipeline: image chunks, their GEMM plans, copy streams, events
+    int host_chunk_n = 0;
+    GemmPlan host_gemm_full{}, host_gemm_tail{};
+    cudaStream_t host_in_stream = nullptr, host_out_stream = nullptr;
+    cudaEvent_t host_ev[2 * 8 + 2] = {};
 
     ~Plan();
     int build(const problem_t* pr, const conv2d_options_t* opt);
     int filter(cudaStream_t s);
     int run(cudaStream_t s);
+    // images [n0, n0 + nc) with the given GEMM plan (sized for nc images)
+    int run_range(int n0, int nc, const GemmPlan* gp, cudaStream_t s);
+    // host input -> device -> host output, copies overlapped with compute
+    int run_host(const void* host_in, void* host_out, cudaStream_t s);
     void mark(cudaStream_t s);
     void release();
 };

@@ -122,7 +122,9 @@ int conv2d_fp16_ex(const void* param_ptr, void* stream);
 
 /* End-to-end call with HOST buffers: copies host_in (n*c*h*w fp16) to the
  * problem's device input, runs, copies the output to host_out and waits for
- * the stream.  Pinned host memory makes the copies asynchronous. */
+ * the stream.  The batch is cut into up to 4 image chunks whose input copies,
+ * compute and output copies overlap (two internal copy streams); with pinned
+ * host memory the copies run at full link speed. */
 int conv2d_fp16_host(const void* param_ptr, const void* host_in, void* host_out, void* stream);
 
 /* Re-run the filter transform (after the caller changed the weights in place). */

@@ -244,19 +244,28 @@ def test_refresh_filter_after_in_place_change(wg):
     assert O.rel_errors(y.cpu().numpy(), r64)[0] <= TOL[2]
 
 
-def test_host_buffer_entry_point(wg):
-    x, wt = O.uniform_inputs(13, 2, 24, 16, 16, 24)
-    xt = torch.empty((2, 24, 16, 16), dtype=torch.float16, device="cuda")
+@pytest.mark.parametrize("algo", [0, 1, 2])
+@pytest.mark.parametrize("n", [1, 2, 7])
+def test_host_buffer_entry_point(wg, algo, n):
+    """Host in -> device -> host out, with the batch cut into overlapped
+    chunks (uneven for n = 7); equal to the device-buffer call bit for bit."""
+    c, h, k = 24, 16, 24
+    x, wt = O.uniform_inputs(13 + n, n, c, h, h, k)
+    xt = torch.empty((n, c, h, h), dtype=torch.float16, device="cuda")
     wtt = torch.from_numpy(wt).cuda()
-    y = torch.empty((2, 24, 16, 16), dtype=torch.float16, device="cuda")
-    prob = wg.make_problem(xt.data_ptr(), wtt.data_ptr(), y.data_ptr(), 2, 24, 16, 16, 24)
-    op = wg.Conv2d(prob, opts_for(wg, 2))
+    y = torch.empty((n, k, h, h), dtype=torch.float16, device="cuda")
+    prob = wg.make_problem(xt.data_ptr(), wtt.data_ptr(), y.data_ptr(), n, c, h, h, k)
+    op = wg.Conv2d(prob, opts_for(wg, algo))
     hin = torch.from_numpy(x).pin_memory()
-    hout = torch.empty((2, 24, 16, 16), dtype=torch.float16).pin_memory()
+    hout = torch.empty((n, k, h, h), dtype=torch.float16).pin_memory()
     torch.cuda.synchronize()
-    op.host(hin.data_ptr(), hout.data_ptr(), torch.cuda.current_stream().cuda_stream)
+    s = torch.cuda.current_stream().cuda_stream
+    op.host(hin.data_ptr(), hout.data_ptr(), s)
+    op.host(hin.data_ptr(), hout.data_ptr(), s)  # second call reuses the pipeline
+    dev, _ = run(wg, x, wt, 1, 1, opts_for(wg, algo))
+    assert np.array_equal(hout.numpy().view(np.uint16), dev.view(np.uint16))
     _, r64 = O.conv2d_direct(x, wt)
-    assert O.rel_errors(hout.numpy(), r64)[0] <= TOL[2]
+    assert O.rel_errors(hout.numpy(), r64)[0] <= TOL[algo_m(algo)]
 
 
 def test_autotune_choice_is_cached_and_correct(wg):
