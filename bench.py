@@ -49,6 +49,10 @@ WORKLOADS = {
     "final6": (2, 320, 64, 64, 4, "uniform", "uniform", "contest shape 2x320x64x64 -> 4"),
 }
 ALGO_ARG = {"ref": -1, "4x3": 0, "2x3": 1, "fused": 2, "auto": 3}
+SERVE_WORKLOADS = {
+    "cfg5": "serving: 16 resident 3x3 pad-1 layers (C,K in {64..512}, H=W in {7..112}), N ~ U{1..64}, "
+            "Poisson arrivals swept over multiples of the plain per-request capacity, 40 GiB workspace budget",
+}
 BATCH_WORKLOADS = {
     "cfg4": "24 uneven 3x3 pad-1 problems in one grouped graph launch: C,K in {64,128,256,512}, "
             "H=W in {7,14,28,56,112}, N in {1,...,128}, U[-1,1], seed 20261203",
@@ -591,13 +595,103 @@ def precision_arm(args):
     return 0
 
 
+def serve_arm(args):
+    """Serving loop: the same Poisson request trace through the continuous-
+    batching server (3 slots, up to 64 requests per batch) and through the
+    plain per-request path (1 slot, 1 request per launch sequence)."""
+    import numpy as np
+    import torch
+    rank, world, local = env_dist()
+    torch.cuda.set_device(local)
+    device = torch.device("cuda", local)
+    wg = load_pkg()
+    wg.lib()
+    rng = np.random.default_rng(20261203)
+    layers = []
+    for _ in range(16):
+        c = int(rng.choice([64, 128, 256, 512]))
+        k = int(rng.choice([64, 128, 256, 512]))
+        h = int(rng.choice([7, 14, 28, 56, 112]))
+        layers.append((c, k, h))
+    g = torch.Generator(device=device)
+    g.manual_seed(7)
+    bufs = []
+    for c, k, h in layers:
+        w = (torch.randn((k, c, 3, 3), generator=g, device=device) / math.sqrt(9 * c)).half()
+        x = (torch.rand((64, c, h, h), generator=g, device=device) * 2 - 1).half()
+        y = torch.empty((64, k, h, h), dtype=torch.float16, device=device)
+        bufs.append((w, x, y))
+    count = args.requests
+    req_layer = rng.integers(0, 16, count).tolist()
+    req_n = rng.integers(1, 65, count).tolist()
+    flops = sum(direct_flops(req_n[i], layers[req_layer[i]][0], layers[req_layer[i]][2], layers[req_layer[i]][2],
+                             layers[req_layer[i]][1]) for i in range(count))
+    ins = [bufs[li][1].data_ptr() for li in req_layer]
+    outs = [bufs[li][2].data_ptr() for li in req_layer]
+
+    def make(served):
+        srv = wg.Server(slots=3 if served else 1, max_batch=64 if served else 1, hbm_budget_bytes=40 << 30)
+        for (c, k, h), (w, _, _) in zip(layers, bufs):
+            srv.add_layer(c, k, h, h, w.data_ptr())
+        return srv
+
+    def run(srv, rate):
+        gaps = np.random.default_rng(11).exponential(1e6 / rate, count)
+        arrivals = np.cumsum(gaps) - gaps[0]
+        lat, wall = srv.replay(req_layer, req_n, arrivals.tolist(), ins, outs)
+        lat = np.sort(np.array(lat))
+        return {"rate_per_s": rate, "p50_us": float(lat[len(lat) // 2]), "p99_us": float(lat[int(0.99 * len(lat))]),
+                "tflops": flops / (wall * 1e-6) / 1e12, "wall_s": wall * 1e-6}
+
+    plain = make(False)
+    served = make(True)
+    # warm both (kernels, tensor maps) on a short trace, then measure the
+    # plain capacity: all requests arriving at once
+    run(plain, 1e9)
+    run(served, 1e9)
+    sat_plain = run(plain, 1e9)
+    capacity = count / sat_plain["wall_s"]
+    sweep = []
+    sampler = ClockSampler(local)
+    sampler.start()
+    for frac in args.rates:
+        rate = frac * capacity
+        s_row = run(served, rate)
+        p_row = run(plain, rate)
+        sweep.append({"load_vs_plain_capacity": frac, "served": s_row, "plain": p_row})
+    clocks = sampler.stop()
+    sat_served = run(served, 1e9)
+    st = served.stats()
+    plain.destroy()
+    served.destroy()
+    line = {
+        "metric": METRIC, "value": sat_served["tflops"], "unit": "TFLOP/s", "n_gpus": world,
+        "steps": count, "warmup": count, "ms_per_step": sat_served["wall_s"] * 1e3 / count,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f16",
+        "data": "synthetic (seeded)",
+        "config": {"workload": SERVE_WORKLOADS["cfg5"], "layers": [list(l) for l in layers], "requests": count,
+                   "total_gflop": flops / 1e9, "plain_capacity_req_per_s": capacity},
+        "saturated": {"served": sat_served, "plain": sat_plain,
+                      "served_over_plain": sat_served["tflops"] / sat_plain["tflops"]},
+        "sweep": sweep, "server_stats": st, "clocks": clocks, "roofline": None, "cpu_baseline": None,
+        "e2e": None, "gpu_launches": None,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=sorted(WORKLOADS) + sorted(BATCH_WORKLOADS), default="cfg2")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS) + sorted(BATCH_WORKLOADS) + sorted(SERVE_WORKLOADS),
+                    default="cfg2")
+    ap.add_argument("--requests", type=int, default=20000, help="requests of the serving trace")
+    ap.add_argument("--rates", type=float, nargs="*", default=[0.5, 0.9, 1.2],
+                    help="arrival rates of the serving sweep, as multiples of the plain capacity")
     ap.add_argument("--algo", choices=sorted(ALGO_ARG), default="ref")
     ap.add_argument("--gemm-bn", type=int, default=0)
     ap.add_argument("--l2-chunk", type=int, default=None)
@@ -612,6 +706,8 @@ def main():
         return reference_arm(args)
     if args.precision:
         return precision_arm(args)
+    if args.workload in SERVE_WORKLOADS:
+        return serve_arm(args)
     if args.workload in BATCH_WORKLOADS:
         return batch_arm(args)
     return our_arm(args)

@@ -51,6 +51,9 @@ EXPORTS = [
     "conv2d_autotune", "conv2d_autotune_clear", "conv2d_fp16_noalloc",
     "conv2d_batch_create", "conv2d_batch_run", "conv2d_batch_run_percall", "conv2d_batch_info",
     "conv2d_batch_launches", "conv2d_batch_check_device", "conv2d_batch_destroy",
+    "conv2d_server_config_default", "conv2d_server_create", "conv2d_server_add_layer", "conv2d_server_submit",
+    "conv2d_server_poll", "conv2d_server_wait_all", "conv2d_server_replay", "conv2d_server_stats",
+    "conv2d_server_destroy",
 ]
 
 _lib = None
@@ -110,6 +113,17 @@ def lib():
         L.conv2d_batch_launches.argtypes = [vp, ctypes.c_int]
         L.conv2d_batch_check_device.argtypes = [vp, ip]
         L.conv2d_batch_destroy.argtypes = [vp]
+        L.conv2d_server_config_default.argtypes = [vp]
+        L.conv2d_server_create.argtypes = [vp, ctypes.POINTER(vp)]
+        L.conv2d_server_add_layer.argtypes = [vp] + [ctypes.c_uint] * 6 + [vp, ip]
+        L.conv2d_server_submit.argtypes = [vp, ctypes.c_int, ctypes.c_uint, vp, vp, ctypes.POINTER(ctypes.c_longlong)]
+        L.conv2d_server_poll.argtypes = [vp, ctypes.c_longlong, ctypes.POINTER(ctypes.c_double)]
+        L.conv2d_server_wait_all.argtypes = [vp]
+        L.conv2d_server_replay.argtypes = [vp, ctypes.c_int, ip, ctypes.POINTER(ctypes.c_uint),
+                                           ctypes.POINTER(ctypes.c_double), ctypes.POINTER(vp), ctypes.POINTER(vp),
+                                           ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
+        L.conv2d_server_stats.argtypes = [vp, vp]
+        L.conv2d_server_destroy.argtypes = [vp]
         _lib = L
     return _lib
 
@@ -227,6 +241,81 @@ def conv2d_noalloc(problem: Problem, stream: int | None = None):
     """F(2x3) convolution through the entry point that allocates no device
     memory (workspace in the library's fixed scratch array)."""
     _check(lib().conv2d_fp16_noalloc(ctypes.byref(problem), ctypes.c_void_p(stream or 0)))
+
+
+class ServerConfig(ctypes.Structure):
+    """conv2d_server_config_t."""
+    _fields_ = [("hbm_budget_bytes", ctypes.c_longlong), ("max_batch", ctypes.c_int), ("slots", ctypes.c_int),
+                ("algo", ctypes.c_int), ("reserved", ctypes.c_int * 4)]
+
+
+class ServerStats(ctypes.Structure):
+    """conv2d_server_stats_t."""
+    _fields_ = [("completed", ctypes.c_longlong), ("batches", ctypes.c_int), ("mean_batch", ctypes.c_double),
+                ("max_inflight_batches", ctypes.c_int), ("arena_used_bytes", ctypes.c_longlong),
+                ("flops", ctypes.c_double)]
+
+
+class Server:
+    """Continuous-batching request loop over resident layers (C++ scheduler)."""
+
+    def __init__(self, **cfg):
+        L = lib()
+        c = ServerConfig()
+        _check(L.conv2d_server_config_default(ctypes.byref(c)))
+        for k, v in cfg.items():
+            setattr(c, k, v)
+        h = ctypes.c_void_p()
+        _check(L.conv2d_server_create(ctypes.byref(c), ctypes.byref(h)))
+        self.handle = h
+
+    def add_layer(self, c, k, h, w, weight_ptr, p=1, q=1):
+        idx = ctypes.c_int()
+        _check(lib().conv2d_server_add_layer(self.handle, c, k, h, w, p, q, ctypes.c_void_p(weight_ptr),
+                                             ctypes.byref(idx)))
+        return idx.value
+
+    def submit(self, layer, n, in_ptr, out_ptr):
+        rid = ctypes.c_longlong()
+        _check(lib().conv2d_server_submit(self.handle, layer, n, ctypes.c_void_p(in_ptr), ctypes.c_void_p(out_ptr),
+                                          ctypes.byref(rid)))
+        return rid.value
+
+    def wait_all(self):
+        _check(lib().conv2d_server_wait_all(self.handle))
+
+    def poll(self, rid):
+        lat = ctypes.c_double()
+        st = lib().conv2d_server_poll(self.handle, rid, ctypes.byref(lat))
+        return st, lat.value
+
+    def replay(self, layers, ns, arrivals_us, in_ptrs, out_ptrs):
+        """Submit at the given arrival times; returns (latencies_us, wall_us)."""
+        cnt = len(layers)
+        lat = (ctypes.c_double * cnt)()
+        wall = ctypes.c_double()
+        _check(lib().conv2d_server_replay(self.handle, cnt, (ctypes.c_int * cnt)(*layers),
+                                          (ctypes.c_uint * cnt)(*ns), (ctypes.c_double * cnt)(*arrivals_us),
+                                          (ctypes.c_void_p * cnt)(*in_ptrs), (ctypes.c_void_p * cnt)(*out_ptrs),
+                                          lat, ctypes.byref(wall)))
+        return list(lat), wall.value
+
+    def stats(self):
+        st = ServerStats()
+        _check(lib().conv2d_server_stats(self.handle, ctypes.byref(st)))
+        return {f: getattr(st, f) for f, _ in ServerStats._fields_}
+
+    def destroy(self):
+        if self.handle:
+            _check(lib().conv2d_server_destroy(self.handle))
+            self.handle = None
+
+    def __del__(self):
+        try:
+            if self.handle and _lib is not None:
+                _lib.conv2d_server_destroy(self.handle)
+        except Exception:
+            pass
 
 
 class Batch:

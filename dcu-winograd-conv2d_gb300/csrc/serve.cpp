@@ -1,0 +1,526 @@
+// Serving loop: continuous batching of conv2d requests over resident layers.
+//
+// A server owns
+//   * layers: the filter of each is transformed once, for F(2x3) and F(4x3),
+//     and stays on the device;
+//   * a workspace arena of the configured HBM budget, from which every
+//     admitted request takes its Winograd-domain buffers (V and M) and to
+//     which it returns them when it completes;
+//   * `slots` in-flight batches, each on its own stream.
+// A scheduler thread admits queued requests in arrival order while their
+// workspace fits in the arena, packs what it admitted into a batch (at most
+// `max_batch` requests), and launches the batch as grouped kernels on a free
+// slot: one input-transform launch per transform family, one persistent GEMM
+// launch per (channel tile, M type) over every request's tiles, one
+// output-transform launch per family.  Requests that arrive while other
+// batches are on the GPU are admitted as soon as a slot and workspace free
+// up, and their batch runs concurrently with the ones still in flight.
+// A request's arithmetic does not depend on what else is in its batch, so its
+// result is bit-identical alone and in the mix.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <thread>
+#include <tuple>
+#include <unordered_map>
+#include <vector>
+
+#include "../../include/conv2d.h"
+#include "wg_kernels.h"
+#include "wg_plan.h"
+
+namespace wg {
+
+namespace {
+
+double now_us() {
+    using namespace std::chrono;
+    return duration<double, std::micro>(steady_clock::now().time_since_epoch()).count();
+}
+
+// First-fit allocator over one device arena (offsets, 256-byte granules).
+class Arena {
+   public:
+    void init(size_t bytes) {
+        free_.clear();
+        free_[0] = bytes;
+        cap_ = bytes;
+    }
+    bool alloc(size_t bytes, size_t* off) {
+        bytes = (bytes + 255) / 256 * 256;
+        for (auto it = free_.begin(); it != free_.end(); ++it) {
+            if (it->second >= bytes) {
+                *off = it->first;
+                const size_t rest = it->second - bytes;
+                const size_t start = it->first + bytes;
+                free_.erase(it);
+                if (rest) free_[start] = rest;
+                used_ += bytes;
+                return true;
+            }
+        }
+        return false;
+    }
+    void release(size_t off, size_t bytes) {
+        bytes = (bytes + 255) / 256 * 256;
+        used_ -= bytes;
+        auto it = free_.emplace(off, bytes).first;
+        auto nx = std::next(it);
+        if (nx != free_.end() && it->first + it->second == nx->first) {
+            it->second += nx->second;
+            free_.erase(nx);
+        }
+        if (it != free_.begin()) {
+            auto pv = std::prev(it);
+            if (pv->first + pv->second == it->first) {
+                pv->second += it->second;
+                free_.erase(it);
+            }
+        }
+    }
+    size_t used() const { return used_; }
+    size_t capacity() const { return cap_; }
+
+   private:
+    std::map<size_t, size_t> free_;
+    size_t cap_ = 0, used_ = 0;
+};
+
+struct Layer {
+    unsigned c, k, h, w, p, q;
+    void* U2 = nullptr;  // F(2x3) transformed filter
+    void* U4 = nullptr;  // F(4x3)
+};
+
+struct Request {
+    long long id;
+    int layer;
+    unsigned n;
+    const void* in;
+    void* out;
+    double t_arrive, t_start = 0, t_done = 0;
+    int m;              // 2 or 4
+    size_t ws_off = 0, ws_bytes = 0;
+    bool done = false;
+};
+
+struct Slot {
+    cudaStream_t stream = nullptr;
+    cudaEvent_t done = nullptr;
+    void* desc_dev = nullptr;
+    void* desc_host = nullptr;   // pinned staging
+    size_t desc_bytes = 0;
+    std::vector<long long> reqs;
+    bool busy = false;
+};
+
+constexpr size_t kDescBytesPerRequest = sizeof(GemmDesc) + sizeof(InDesc) + sizeof(OutDesc) + 256;
+
+}  // namespace
+
+struct Server {
+    conv2d_server_config_t cfg{};
+    int device = 0, num_sms = 1;
+    std::vector<Layer> layers;
+    void* arena_base = nullptr;
+    void* ufilt = nullptr;       // resident transformed filters of all layers (grown per layer)
+    std::vector<void*> u_blocks;
+    DevErr* err = nullptr;
+    Arena arena;
+    std::vector<Slot> slots;
+    std::mutex mu;
+    std::condition_variable cv;
+    std::deque<long long> pending;
+    std::unordered_map<long long, Request> reqs;
+    long long next_id = 1;
+    std::atomic<bool> stop{false};
+    std::thread sched;
+    long long completed = 0;
+    double flops_done = 0;
+    int batches = 0, batch_requests = 0, max_inflight = 0;
+
+    ~Server() {
+        stop = true;
+        cv.notify_all();
+        if (sched.joinable()) sched.join();
+        for (Slot& s : slots) {
+            if (s.stream) cudaStreamSynchronize(s.stream);
+            if (s.stream) cudaStreamDestroy(s.stream);
+            if (s.done) cudaEventDestroy(s.done);
+            if (s.desc_dev) cudaFree(s.desc_dev);
+            if (s.desc_host) cudaFreeHost(s.desc_host);
+        }
+        for (void* p : u_blocks) cudaFree(p);
+        if (arena_base) cudaFree(arena_base);
+        if (err) cudaFree(err);
+    }
+
+    static size_t ws_bytes_for(const Geom& g) {
+        const long long E = g.alpha * g.alpha;
+        const size_t v = static_cast<size_t>(E * round_rows(g.P) * g.cp * 2);
+        const size_t m = static_cast<size_t>(E * g.P * g.kp * (g.m == 4 ? 4 : 2));
+        return (v + 255) / 256 * 256 + (m + 255) / 256 * 256;
+    }
+
+    int choose_m(const Layer& L) const {
+        if (cfg.algo == CONV2D_ALGO_4X3_NON_FUSED) return 4;
+        if (cfg.algo == CONV2D_ALGO_2X3_NON_FUSED) return 2;
+        // F(4x3) does 44% of F(2x3)'s GEMM work but moves more bytes per tile;
+        // it wins once both channel counts are wide and the image is not tiny
+        return (std::min(L.c, L.k) >= 128 && L.h >= 14 && L.w >= 14) ? 4 : 2;
+    }
+
+    // launch one batch (requests already admitted: workspace assigned)
+    int launch(Slot& slot) {
+        std::vector<InDesc> in2, in4;
+        std::vector<OutDesc> out2, out4;
+        std::map<std::pair<int, int>, std::vector<GemmDesc>> gemm;  // (bn, m) -> descs
+        long long blk_in2 = 0, blk_in4 = 0, blk_out2 = 0, blk_out4 = 0;
+        int smem2 = 0, smem4 = 0;
+        char* arena = static_cast<char*>(arena_base);
+        for (long long id : slot.reqs) {
+            Request& r = reqs[id];
+            const Layer& L = layers[r.layer];
+            const Geom g = make_geom(r.n, L.c, L.h, L.w, L.k, L.p, L.q, r.m);
+            const int E = g.alpha * g.alpha;
+            char* V = arena + r.ws_off;
+            char* Mw = V + (static_cast<size_t>(E) * round_rows(g.P) * g.cp * 2 + 255) / 256 * 256;
+            const void* x_end = static_cast<const uint16_t*>(r.in) + static_cast<long long>(r.n) * L.c * L.h * L.w;
+            int smem = 0;
+            InDesc di = make_in_desc(g, r.in, x_end, V, nullptr, &smem);
+            OutDesc dout = make_out_desc(g, r.m == 4, Mw, r.out, nullptr);
+            GemmDesc dg;
+            const int bn = default_bn(static_cast<int>(L.k));
+            if (make_gemm_desc(dg, OpType::F16, E, g.P, L.k, g.kp, g.cp, V, r.m == 4 ? L.U4 : L.U2, Mw, r.m == 4, bn) !=
+                cudaSuccess)
+                return set_last_error(CONV2D_ERR_CUDA, "tensor map encoding failed");
+            if (r.m == 2) {
+                di.blk_begin = blk_in2;
+                blk_in2 += di.gx * di.gy;
+                smem2 = std::max(smem2, smem);
+                in2.push_back(di);
+                dout.blk_begin = blk_out2;
+                blk_out2 += dout.gx * dout.gy;
+                out2.push_back(dout);
+            } else {
+                di.blk_begin = blk_in4;
+                blk_in4 += di.gx * di.gy;
+                smem4 = std::max(smem4, smem);
+                in4.push_back(di);
+                dout.blk_begin = blk_out4;
+                blk_out4 += dout.gx * dout.gy;
+                out4.push_back(dout);
+            }
+            gemm[{bn, r.m}].push_back(dg);
+        }
+        // descriptors: GemmDesc[] | InDesc[] | OutDesc[] in the slot's staging area
+        char* h = static_cast<char*>(slot.desc_host);
+        size_t off = 0;
+        struct GG {
+            int bn, m;
+            size_t off;
+            int n;
+            long long tiles;
+        };
+        std::vector<GG> gg;
+        for (auto& kv : gemm) {
+            long long t = 0;
+            for (GemmDesc& d : kv.second) {
+                d.tile_begin = t;
+                t += d.tiles;
+            }
+            std::memcpy(h + off, kv.second.data(), kv.second.size() * sizeof(GemmDesc));
+            gg.push_back({kv.first.first, kv.first.second, off, static_cast<int>(kv.second.size()), t});
+            off += kv.second.size() * sizeof(GemmDesc);
+        }
+        const size_t o_in2 = off;
+        std::memcpy(h + off, in2.data(), in2.size() * sizeof(InDesc));
+        off += in2.size() * sizeof(InDesc);
+        const size_t o_in4 = off;
+        std::memcpy(h + off, in4.data(), in4.size() * sizeof(InDesc));
+        off += in4.size() * sizeof(InDesc);
+        const size_t o_out2 = off;
+        std::memcpy(h + off, out2.data(), out2.size() * sizeof(OutDesc));
+        off += out2.size() * sizeof(OutDesc);
+        const size_t o_out4 = off;
+        std::memcpy(h + off, out4.data(), out4.size() * sizeof(OutDesc));
+        off += out4.size() * sizeof(OutDesc);
+        cudaStream_t s = slot.stream;
+        char* d = static_cast<char*>(slot.desc_dev);
+        if (cudaMemcpyAsync(d, h, off, cudaMemcpyHostToDevice, s) != cudaSuccess)
+            return set_last_error(CONV2D_ERR_CUDA, "descriptor copy failed");
+        cudaError_t e = cudaSuccess;
+        if (!in2.empty() && e == cudaSuccess)
+            e = launch_input_transform_grouped(Xform::F2, OpType::F16, reinterpret_cast<const InDesc*>(d + o_in2),
+                                               static_cast<int>(in2.size()), blk_in2, smem2, err, s);
+        if (!in4.empty() && e == cudaSuccess)
+            e = launch_input_transform_grouped(Xform::F4, OpType::F16, reinterpret_cast<const InDesc*>(d + o_in4),
+                                               static_cast<int>(in4.size()), blk_in4, smem4, err, s);
+        for (const GG& g : gg)
+            if (e == cudaSuccess)
+                e = launch_gemm_grouped(reinterpret_cast<const GemmDesc*>(d + g.off), g.n, g.tiles, OpType::F16, g.m == 4,
+                                        g.bn, static_cast<int>(std::min<long long>(g.tiles, num_sms)), err, s);
+        if (!out2.empty() && e == cudaSuccess)
+            e = launch_output_transform_grouped(Xform::F2, false, reinterpret_cast<const OutDesc*>(d + o_out2),
+                                                static_cast<int>(out2.size()), blk_out2, s);
+        if (!out4.empty() && e == cudaSuccess)
+            e = launch_output_transform_grouped(Xform::F4, true, reinterpret_cast<const OutDesc*>(d + o_out4),
+                                                static_cast<int>(out4.size()), blk_out4, s);
+        if (e == cudaSuccess) e = cudaEventRecord(slot.done, s);
+        if (e != cudaSuccess) return set_last_error(CONV2D_ERR_CUDA, cudaGetErrorString(e));
+        return CONV2D_OK;
+    }
+
+    void loop() {
+        cudaSetDevice(device);
+        while (true) {
+            std::unique_lock<std::mutex> lk(mu);
+            // completions
+            int inflight = 0;
+            for (Slot& s : slots) {
+                if (!s.busy) continue;
+                if (cudaEventQuery(s.done) == cudaSuccess) {
+                    const double t = now_us();
+                    for (long long id : s.reqs) {
+                        Request& r = reqs[id];
+                        r.t_done = t;
+                        r.done = true;
+                        arena.release(r.ws_off, r.ws_bytes);
+                        const Layer& L = layers[r.layer];
+                        flops_done += 2.0 * r.n * L.k * (L.h + 2.0 * L.p - 2) * (L.w + 2.0 * L.q - 2) * L.c * 9;
+                        ++completed;
+                    }
+                    s.reqs.clear();
+                    s.busy = false;
+                    cv.notify_all();
+                } else {
+                    ++inflight;
+                }
+            }
+            // admission: arrival order, while a slot and workspace are free
+            Slot* free_slot = nullptr;
+            for (Slot& s : slots)
+                if (!s.busy) {
+                    free_slot = &s;
+                    break;
+                }
+            if (free_slot && !pending.empty()) {
+                std::vector<long long> batch;
+                while (!pending.empty() && static_cast<int>(batch.size()) < cfg.max_batch) {
+                    Request& r = reqs[pending.front()];
+                    const Layer& L = layers[r.layer];
+                    const Geom g = make_geom(r.n, L.c, L.h, L.w, L.k, L.p, L.q, r.m);
+                    r.ws_bytes = ws_bytes_for(g);
+                    size_t off = 0;
+                    if (!arena.alloc(r.ws_bytes, &off)) break;  // wait for workspace
+                    r.ws_off = off;
+                    r.t_start = now_us();
+                    batch.push_back(pending.front());
+                    pending.pop_front();
+                }
+                if (!batch.empty()) {
+                    free_slot->reqs = batch;
+                    free_slot->busy = true;
+                    ++batches;
+                    batch_requests += static_cast<int>(batch.size());
+                    if (launch(*free_slot) != CONV2D_OK) {
+                        // a launch that fails completes its requests at once
+                        for (long long id : batch) {
+                            reqs[id].done = true;
+                            reqs[id].t_done = now_us();
+                            arena.release(reqs[id].ws_off, reqs[id].ws_bytes);
+                        }
+                        free_slot->reqs.clear();
+                        free_slot->busy = false;
+                    }
+                    max_inflight = std::max(max_inflight, inflight + 1);
+                    continue;
+                }
+            }
+            if (stop && pending.empty() && inflight == 0) break;
+            if (inflight == 0 && pending.empty())
+                cv.wait_for(lk, std::chrono::microseconds(200));
+            else {
+                lk.unlock();
+                std::this_thread::sleep_for(std::chrono::microseconds(5));
+            }
+        }
+    }
+};
+
+}  // namespace wg
+
+using namespace wg;
+
+extern "C" {
+
+int conv2d_server_config_default(conv2d_server_config_t* cfg) {
+    if (!cfg) return set_last_error(CONV2D_ERR_INVALID, "null config");
+    std::memset(cfg, 0, sizeof(*cfg));
+    cfg->hbm_budget_bytes = 40ll << 30;
+    cfg->max_batch = 64;
+    cfg->slots = 3;
+    cfg->algo = CONV2D_ALGO_AUTO;
+    return CONV2D_OK;
+}
+
+int conv2d_server_create(const conv2d_server_config_t* cfg, conv2d_server_t** out) {
+    if (!cfg || !out) return set_last_error(CONV2D_ERR_INVALID, "null argument");
+    if (cfg->slots < 1 || cfg->max_batch < 1 || cfg->hbm_budget_bytes < (1 << 20))
+        return set_last_error(CONV2D_ERR_INVALID, "bad server config");
+    std::unique_ptr<Server> sv(new Server());
+    sv->cfg = *cfg;
+    cudaGetDevice(&sv->device);
+    cudaDeviceGetAttribute(&sv->num_sms, cudaDevAttrMultiProcessorCount, sv->device);
+    if (cudaMalloc(&sv->arena_base, static_cast<size_t>(cfg->hbm_budget_bytes)) != cudaSuccess) {
+        cudaGetLastError();
+        return set_last_error(CONV2D_ERR_NOMEM, "workspace arena allocation failed");
+    }
+    sv->arena.init(static_cast<size_t>(cfg->hbm_budget_bytes));
+    if (cudaMalloc(&sv->err, 256) != cudaSuccess) return set_last_error(CONV2D_ERR_NOMEM, "allocation failed");
+    cudaMemset(sv->err, 0, 256);
+    sv->slots.resize(cfg->slots);
+    for (Slot& s : sv->slots) {
+        s.desc_bytes = static_cast<size_t>(cfg->max_batch) * kDescBytesPerRequest + 4096;
+        if (cudaStreamCreateWithFlags(&s.stream, cudaStreamNonBlocking) != cudaSuccess ||
+            cudaEventCreateWithFlags(&s.done, cudaEventDisableTiming) != cudaSuccess ||
+            cudaMalloc(&s.desc_dev, s.desc_bytes) != cudaSuccess ||
+            cudaMallocHost(&s.desc_host, s.desc_bytes) != cudaSuccess)
+            return set_last_error(CONV2D_ERR_NOMEM, "slot setup failed");
+    }
+    Server* raw = sv.get();
+    sv->sched = std::thread([raw] { raw->loop(); });
+    *out = reinterpret_cast<conv2d_server_t*>(sv.release());
+    return CONV2D_OK;
+}
+
+int conv2d_server_add_layer(conv2d_server_t* server, unsigned c, unsigned k, unsigned h, unsigned w, unsigned p,
+                            unsigned q, const void* weight, int* layer) {
+    Server* sv = reinterpret_cast<Server*>(server);
+    if (!sv || !weight || !layer) return set_last_error(CONV2D_ERR_INVALID, "null argument");
+    problem_t pr{reinterpret_cast<void*>(16), const_cast<void*>(weight), reinterpret_cast<void*>(16), 1, c, h, w, k, 3, 3,
+                 1, 1, p, q};
+    int st = validate_problem(&pr);
+    if (st) return st;
+    Layer L{c, k, h, w, p, q};
+    const int cp = (c + 7) / 8 * 8, kp = (k + 7) / 8 * 8;
+    const size_t b2 = static_cast<size_t>(16) * kp * cp * 2, b4 = static_cast<size_t>(36) * kp * cp * 2;
+    void* blk = nullptr;
+    if (cudaMalloc(&blk, b2 + b4) != cudaSuccess) return set_last_error(CONV2D_ERR_NOMEM, "filter allocation failed");
+    sv->u_blocks.push_back(blk);
+    L.U2 = blk;
+    L.U4 = static_cast<char*>(blk) + b2;
+    if (launch_filter_transform(Xform::F2, OpType::F16, weight, L.U2, k, c, cp, nullptr) != cudaSuccess ||
+        launch_filter_transform(Xform::F4, OpType::F16, weight, L.U4, k, c, cp, nullptr) != cudaSuccess ||
+        cudaDeviceSynchronize() != cudaSuccess)
+        return set_last_error(CONV2D_ERR_CUDA, "filter transform failed");
+    std::lock_guard<std::mutex> lk(sv->mu);
+    sv->layers.push_back(L);
+    *layer = static_cast<int>(sv->layers.size()) - 1;
+    return CONV2D_OK;
+}
+
+int conv2d_server_submit(conv2d_server_t* server, int layer, unsigned n, const void* in, void* out,
+                         long long* request) {
+    Server* sv = reinterpret_cast<Server*>(server);
+    if (!sv || !in || !out || n == 0) return set_last_error(CONV2D_ERR_INVALID, "bad request");
+    std::lock_guard<std::mutex> lk(sv->mu);
+    if (layer < 0 || layer >= static_cast<int>(sv->layers.size())) return set_last_error(CONV2D_ERR_INVALID, "bad layer");
+    const Layer& L = sv->layers[layer];
+    Request r;
+    r.id = sv->next_id++;
+    r.layer = layer;
+    r.n = n;
+    r.in = in;
+    r.out = out;
+    r.t_arrive = now_us();
+    r.m = sv->choose_m(L);
+    const Geom g = make_geom(n, L.c, L.h, L.w, L.k, L.p, L.q, r.m);
+    if (Server::ws_bytes_for(g) > sv->arena.capacity())
+        return set_last_error(CONV2D_ERR_BUSY, "request workspace exceeds the server's HBM budget");
+    sv->reqs[r.id] = r;
+    sv->pending.push_back(r.id);
+    if (request) *request = r.id;
+    sv->cv.notify_all();
+    return CONV2D_OK;
+}
+
+int conv2d_server_poll(conv2d_server_t* server, long long request, double* latency_us) {
+    Server* sv = reinterpret_cast<Server*>(server);
+    if (!sv) return -1;
+    std::lock_guard<std::mutex> lk(sv->mu);
+    auto it = sv->reqs.find(request);
+    if (it == sv->reqs.end()) return -1;
+    if (!it->second.done) return 0;
+    if (latency_us) *latency_us = it->second.t_done - it->second.t_arrive;
+    return 1;
+}
+
+int conv2d_server_wait_all(conv2d_server_t* server) {
+    Server* sv = reinterpret_cast<Server*>(server);
+    if (!sv) return set_last_error(CONV2D_ERR_INVALID, "null server");
+    std::unique_lock<std::mutex> lk(sv->mu);
+    sv->cv.wait(lk, [sv] {
+        if (!sv->pending.empty()) return false;
+        for (const Slot& s : sv->slots)
+            if (s.busy) return false;
+        return true;
+    });
+    return CONV2D_OK;
+}
+
+int conv2d_server_replay(conv2d_server_t* server, int count, const int* layer, const unsigned* n,
+                         const double* arrival_us, const void* const* in, void* const* out, double* latency_us,
+                         double* wall_us) {
+    Server* sv = reinterpret_cast<Server*>(server);
+    if (!sv || count <= 0 || !layer || !n || !arrival_us || !in || !out || !latency_us)
+        return set_last_error(CONV2D_ERR_INVALID, "bad replay arguments");
+    std::vector<long long> ids(count);
+    const double t0 = now_us();
+    for (int i = 0; i < count; ++i) {
+        while (now_us() - t0 < arrival_us[i]) {
+        }
+        const int st = conv2d_server_submit(server, layer[i], n[i], in[i], out[i], &ids[i]);
+        if (st) return st;
+    }
+    conv2d_server_wait_all(server);
+    if (wall_us) *wall_us = now_us() - t0;
+    std::lock_guard<std::mutex> lk(sv->mu);
+    for (int i = 0; i < count; ++i) {
+        const Request& r = sv->reqs[ids[i]];
+        latency_us[i] = r.t_done - r.t_arrive;
+    }
+    for (int i = 0; i < count; ++i) sv->reqs.erase(ids[i]);
+    return CONV2D_OK;
+}
+
+int conv2d_server_stats(conv2d_server_t* server, conv2d_server_stats_t* st) {
+    Server* sv = reinterpret_cast<Server*>(server);
+    if (!sv || !st) return set_last_error(CONV2D_ERR_INVALID, "null argument");
+    std::lock_guard<std::mutex> lk(sv->mu);
+    st->completed = sv->completed;
+    st->batches = sv->batches;
+    st->mean_batch = sv->batches ? static_cast<double>(sv->batch_requests) / sv->batches : 0.0;
+    st->max_inflight_batches = sv->max_inflight;
+    st->arena_used_bytes = static_cast<long long>(sv->arena.used());
+    st->flops = sv->flops_done;
+    return CONV2D_OK;
+}
+
+int conv2d_server_destroy(conv2d_server_t* server) {
+    Server* sv = reinterpret_cast<Server*>(server);
+    if (!sv) return set_last_error(CONV2D_ERR_INVALID, "null server");
+    conv2d_server_wait_all(server);
+    delete sv;
+    return CONV2D_OK;
+}
+
+}  // extern "C"

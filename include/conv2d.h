@@ -184,6 +184,55 @@ int conv2d_batch_launches(const conv2d_batch_t* batch, int grouped);
 int conv2d_batch_check_device(conv2d_batch_t* batch, int* site);
 int conv2d_batch_destroy(conv2d_batch_t* batch);
 
+/* ---- serving (no counterpart in the reference) ---------------------------- */
+
+/* A request loop over resident layers: filters transformed once (F(2x3) and
+ * F(4x3)) and kept on the device; requests admitted in arrival order while
+ * their Winograd-domain workspace fits in an arena of `hbm_budget_bytes`;
+ * admitted requests packed into batches of at most `max_batch` and launched
+ * as grouped kernels on one of `slots` streams, so batches overlap on the
+ * device (continuous batching).  A request's result does not depend on what
+ * else is in its batch.  slots = 1, max_batch = 1 gives the plain per-request
+ * path. */
+typedef struct conv2d_server conv2d_server_t;
+typedef struct
+{
+    long long hbm_budget_bytes;  /* workspace arena (default 40 GiB) */
+    int max_batch;               /* requests per batch (default 64) */
+    int slots;                   /* batches in flight (default 3) */
+    int algo;                    /* CONV2D_ALGO_AUTO (shape rule), _2X3_NON_FUSED or _4X3_NON_FUSED */
+    int reserved[4];
+} conv2d_server_config_t;
+typedef struct
+{
+    long long completed;
+    int batches;
+    double mean_batch;
+    int max_inflight_batches;
+    long long arena_used_bytes;
+    double flops;                /* direct-convolution FLOPs of completed requests */
+} conv2d_server_stats_t;
+int conv2d_server_config_default(conv2d_server_config_t* cfg);
+int conv2d_server_create(const conv2d_server_config_t* cfg, conv2d_server_t** server);
+/* Registers a layer (3x3, stride 1, padding p,q, input h x w, c -> k channels)
+ * whose fp16 KCRS weights are on the device; returns its index. */
+int conv2d_server_add_layer(conv2d_server_t* server, unsigned c, unsigned k, unsigned h, unsigned w, unsigned p,
+                            unsigned q, const void* weight, int* layer);
+/* Queues a request of n images (device input/output); returns its id.
+ * CONV2D_ERR_BUSY when its workspace alone exceeds the budget. */
+int conv2d_server_submit(conv2d_server_t* server, int layer, unsigned n, const void* in, void* out,
+                         long long* request);
+/* 1 when done (latency in microseconds, arrival to completion), 0 pending, -1 unknown. */
+int conv2d_server_poll(conv2d_server_t* server, long long request, double* latency_us);
+int conv2d_server_wait_all(conv2d_server_t* server);
+/* Submits `count` requests at their arrival times (microseconds from the call),
+ * waits for all, returns each latency and the wall time. */
+int conv2d_server_replay(conv2d_server_t* server, int count, const int* layer, const unsigned* n,
+                         const double* arrival_us, const void* const* in, void* const* out, double* latency_us,
+                         double* wall_us);
+int conv2d_server_stats(conv2d_server_t* server, conv2d_server_stats_t* stats);
+int conv2d_server_destroy(conv2d_server_t* server);
+
 /* One call with a CUDA event recorded on the stream after every kernel
  * launch; waits, writes each launch's duration (ms, launch order) to
  * kernel_ms and returns the number of launches (negative status on error). */
