@@ -47,7 +47,15 @@ WORKLOADS = {
     "final4": (2, 1920, 32, 32, 640, "uniform", "uniform", "contest shape 2x1920x32x32 -> 640"),
     "final5": (2, 640, 64, 64, 640, "uniform", "uniform", "contest shape 2x640x64x64 -> 640"),
     "final6": (2, 320, 64, 64, 4, "uniform", "uniform", "contest shape 2x320x64x64 -> 4"),
+    "pre1": (64, 256, 14, 14, 256, "uniform", "uniform", "contest shape 64x256x14x14 -> 256"),
+    "pre2": (256, 192, 14, 14, 192, "uniform", "uniform", "contest shape 256x192x14x14 -> 192"),
+    "pre3": (16, 256, 26, 26, 512, "uniform", "uniform", "contest shape 16x256x26x26 -> 512"),
+    "pre4": (32, 256, 14, 14, 256, "uniform", "uniform", "contest shape 32x256x14x14 -> 256"),
+    "pre5": (2, 1280, 16, 16, 1280, "uniform", "uniform", "contest shape 2x1280x16x16 -> 1280"),
+    "pre6": (2, 960, 64, 64, 32, "uniform", "uniform", "contest shape 2x960x64x64 -> 32"),
 }
+# reference latencies read from its published chart (Hygon DCU gfx928), microseconds
+PUBLISHED_US = {"final1": 207, "final2": 367, "final3": 724, "final4": 654, "final5": 593, "final6": 133}
 ALGO_ARG = {"ref": -1, "4x3": 0, "2x3": 1, "fused": 2, "auto": 3}
 SERVE_WORKLOADS = {
     "cfg5": "serving: 16 resident 3x3 pad-1 layers (C,K in {64..512}, H=W in {7..112}), N ~ U{1..64}, "
@@ -427,6 +435,11 @@ def our_arm(args):
         cpu = {"value": fl / dt / 1e12, "unit": "TFLOP/s", "cores": used, "kind": kind,
                "sample": f"1 of {n} images ({fl / 1e9:.2f} GFLOP), all {k} output channels, {dt:.2f} s"}
 
+    cudnn = None
+    if args.cudnn:
+        cms = time_cudnn(torch, xs[0], wt, args.steps, args.warmup)
+        cudnn = {"value": flops / (cms * 1e-3) / 1e12, "unit": "TFLOP/s", "ms_per_step": cms,
+                 "path": "torch.nn.functional.conv2d fp16 NCHW, cudnn.benchmark"}
     lat = sorted(per_step)
     line = {
         "metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": world, "steps": args.steps,
@@ -442,6 +455,7 @@ def our_arm(args):
         "roofline": roof,
         "e2e": e2e,
         "cpu_baseline": cpu,
+        "cudnn": cudnn,
         "clocks": clocks,
         "gpu_launches": args.steps * ops[0].launches_per_call,
     }
@@ -681,6 +695,65 @@ def serve_arm(args):
     return 0
 
 
+def time_cudnn(torch, x, w, steps, warmup):
+    """cuDNN through torch's conv2d (fp16, NCHW, pad 1), device time per call."""
+    import torch.nn.functional as F
+    torch.backends.cudnn.benchmark = True
+    for _ in range(max(3, warmup)):
+        F.conv2d(x, w, padding=1)
+    torch.cuda.synchronize()
+    a = torch.cuda.Event(enable_timing=True)
+    b = torch.cuda.Event(enable_timing=True)
+    a.record()
+    for _ in range(steps):
+        F.conv2d(x, w, padding=1)
+    b.record()
+    torch.cuda.synchronize()
+    return a.elapsed_time(b) / steps
+
+
+def suite_arm(args):
+    """The reference's contest shapes (its pre.sh and final.sh) through the
+    drop-in API, with the reference's selection and with the autotuner, beside
+    cuDNN and the reference's published DCU latencies."""
+    import torch
+    wg = load_pkg()
+    wg.lib()
+    rows = []
+    names = [f"pre{i}" for i in range(1, 7)] + [f"final{i}" for i in range(1, 7)] + ["cfg1", "cfg2", "cfg3"]
+    for name in names:
+        n, c, h, w, k, xd, wd, desc = WORKLOADS[name]
+        x, wt = make_inputs(torch, name, torch.device("cuda"), 77)
+        y = torch.empty((n, k, h, w), dtype=torch.float16, device="cuda")
+        fl = direct_flops(n, c, h, w, k)
+        row = {"shape": name, "n": n, "c": c, "h": h, "w": w, "k": k}
+        for label, algo in (("reference_selection", -1), ("auto", 3)):
+            op = wg.Conv2d(wg.make_problem(x.data_ptr(), wt.data_ptr(), y.data_ptr(), n, c, h, w, k),
+                           wg.default_options(algo=algo))
+            s = torch.cuda.current_stream().cuda_stream
+            for _ in range(3):
+                op(s)
+            torch.cuda.synchronize()
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record()
+            for _ in range(args.steps):
+                op(s)
+            b.record()
+            torch.cuda.synchronize()
+            us = a.elapsed_time(b) / args.steps * 1e3
+            row[label] = {"algo": wg.ALGO_NAMES[op.algo], "us": us, "tflops": fl / (us * 1e-6) / 1e12}
+            op.destroy()
+        us = time_cudnn(torch, x, wt, args.steps, args.warmup) * 1e3
+        row["cudnn"] = {"us": us, "tflops": fl / (us * 1e-6) / 1e12}
+        if name in PUBLISHED_US:
+            row["reference_dcu_us"] = PUBLISHED_US[name]
+        rows.append(row)
+    print(json.dumps({"suite": "contest shapes, 3x3 pad 1 stride 1 fp16", "steps": args.steps, "rows": rows}),
+          flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -692,12 +765,14 @@ def main():
     ap.add_argument("--requests", type=int, default=20000, help="requests of the serving trace")
     ap.add_argument("--rates", type=float, nargs="*", default=[0.5, 0.9, 1.2],
                     help="arrival rates of the serving sweep, as multiples of the plain capacity")
-    ap.add_argument("--algo", choices=sorted(ALGO_ARG), default="ref")
+    ap.add_argument("--algo", choices=sorted(ALGO_ARG), default="auto")
     ap.add_argument("--gemm-bn", type=int, default=0)
     ap.add_argument("--l2-chunk", type=int, default=None)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--precision", action="store_true", help="F(4x3) precision study instead of timing")
+    ap.add_argument("--suite", action="store_true", help="contest shapes through the drop-in API, with cuDNN")
+    ap.add_argument("--cudnn", action="store_true", help="also time cuDNN (torch conv2d) on the workload")
     ap.add_argument("--images", type=int, default=4, help="images of the precision study")
     args = ap.parse_args()
     if args.warmup < 3:
@@ -706,6 +781,8 @@ def main():
         return reference_arm(args)
     if args.precision:
         return precision_arm(args)
+    if args.suite:
+        return suite_arm(args)
     if args.workload in SERVE_WORKLOADS:
         return serve_arm(args)
     if args.workload in BATCH_WORKLOADS:
