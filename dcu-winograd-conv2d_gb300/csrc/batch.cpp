@@ -37,6 +37,7 @@ struct Batch {
         int n;
         long long blocks;
         int smem;
+        bool scaled;
     };
     struct GemmGroup {
         int bn;
@@ -74,7 +75,7 @@ struct Batch {
             if ((e = launch_tile_scale(p.g, p.prob.in, p.scale, s)) != cudaSuccess) return e;
         }
         for (const InGroup& g : in_groups)
-            if ((e = launch_input_transform_grouped(g.xf, g.op, g.descs, g.n, g.blocks, g.smem, err, s)) != cudaSuccess)
+            if ((e = launch_input_transform_grouped(g.xf, g.op, g.descs, g.n, g.blocks, g.smem, g.scaled, err, s)) != cudaSuccess)
                 return e;
         for (const GemmGroup& g : gemm_groups)
             if ((e = launch_gemm_grouped(g.descs, g.n, g.tiles, g.op, g.m_fp32, g.bn, g.grid, err, s)) != cudaSuccess)
@@ -135,13 +136,15 @@ int batch_create(const problem_t* problems, int count, const conv2d_options_t* o
         size_t first, n;
         long long total;
         int extra;
+        bool scaled;
     };
     std::vector<std::pair<std::pair<int, int>, Range>> in_r, out_r;
     std::vector<std::pair<std::tuple<int, int, int>, Range>> gemm_r;
     for (auto& kv : in_keys) {
-        Range r{in_descs.size(), kv.second.size(), 0, 0};
+        Range r{in_descs.size(), kv.second.size(), 0, 0, false};
         for (int i : kv.second) {
             Plan& p = *b->plans[i];
+            r.scaled = r.scaled || p.scale != nullptr;
             const void* x_end =
                 static_cast<const uint16_t*>(p.prob.in) + static_cast<long long>(p.prob.n) * p.g.c * p.g.h * p.g.w;
             int smem = 0;
@@ -154,7 +157,7 @@ int batch_create(const problem_t* problems, int count, const conv2d_options_t* o
         in_r.push_back({kv.first, r});
     }
     for (auto& kv : out_keys) {
-        Range r{out_descs.size(), kv.second.size(), 0, 0};
+        Range r{out_descs.size(), kv.second.size(), 0, 0, false};
         for (int i : kv.second) {
             Plan& p = *b->plans[i];
             OutDesc d = make_out_desc(p.g, p.m_fp32, p.Mw, p.prob.out, p.scale);
@@ -165,7 +168,7 @@ int batch_create(const problem_t* problems, int count, const conv2d_options_t* o
         out_r.push_back({kv.first, r});
     }
     for (auto& kv : gemm_keys) {
-        Range r{gemm_descs.size(), kv.second.size(), 0, 0};
+        Range r{gemm_descs.size(), kv.second.size(), 0, 0, false};
         for (int i : kv.second) {
             GemmDesc d = b->plans[i]->gemm_full.desc;
             d.tile_begin = r.total;
@@ -192,7 +195,7 @@ int batch_create(const problem_t* problems, int count, const conv2d_options_t* o
     for (auto& kr : in_r)
         b->in_groups.push_back({static_cast<Xform>(kr.first.first), static_cast<OpType>(kr.first.second),
                                 reinterpret_cast<const InDesc*>(base + oI) + kr.second.first,
-                                static_cast<int>(kr.second.n), kr.second.total, kr.second.extra});
+                                static_cast<int>(kr.second.n), kr.second.total, kr.second.extra, kr.second.scaled});
     for (auto& kr : gemm_r)
         b->gemm_groups.push_back({std::get<0>(kr.first), std::get<1>(kr.first) != 0,
                                   static_cast<OpType>(std::get<2>(kr.first)),

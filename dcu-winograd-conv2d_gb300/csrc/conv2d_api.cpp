@@ -177,6 +177,12 @@ int Plan::build(const problem_t* pr, const conv2d_options_t* opt_in) {
     g = make_geom(pr->n, pr->c, pr->h, pr->w, pr->k, pr->p, pr->q, m);
     const int E = g.alpha * g.alpha;
     const long long op_bytes = 2;
+    if (algo != CONV2D_ALGO_2X3_FUSED) {
+        // the input transform stages whole input rows of 8 channels, twice
+        int in_smem = 0;
+        make_in_desc(g, pr->in, pr->in, nullptr, nullptr, &in_smem);
+        if (in_smem > 232448) return fail(CONV2D_ERR_UNSUPPORTED, "input rows too wide for the staged input transform");
+    }
 
     // image chunking keeps V and M of one chunk L2-resident between kernels
     chunk_n = static_cast<int>(pr->n);

@@ -26,6 +26,7 @@
 #include <algorithm>
 
 #include "wg_kernels.h"
+#include "wg_launch.h"
 #include "wg_ptx.cuh"
 #include "wg_transforms.cuh"
 
@@ -124,6 +125,8 @@ __global__ void __launch_bounds__(kThreads, 1)
         }
         fence_barrier_init();
     }
+    pdl_wait();     // input written, earlier readers of the output done
+    pdl_trigger();
     if (warp == 8) tmem_alloc(tmem_slot, 512);
     tc_fence_before();
     __syncthreads();
@@ -436,11 +439,10 @@ cudaError_t launch_fused2x3(const FusedPlan& fp, const Geom& g, const void* x, c
     auto kern = fp.op == OpType::BF16 ? fused2x3_kernel<true> : fused2x3_kernel<false>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, fp.smem_bytes);
     if (e != cudaSuccess) return e;
-    kern<<<static_cast<unsigned>(blocks), kThreads, fp.smem_bytes, stream>>>(
-        static_cast<const __half*>(x), static_cast<const __half*>(x_end), fp.tmU, static_cast<__half*>(out), g.c, g.h,
-        g.w, g.k, g.pad_h, g.pad_w, g.oh, g.ow, g.tiles_h, g.tiles_w, static_cast<int>(g.P), fp.c_chunks, fp.n_blocks,
-        fp.stg_ch_bytes, fp.nbuf, err);
-    return cudaGetLastError();
+    return launch_pdl(kern, dim3(static_cast<unsigned>(blocks)), dim3(kThreads), fp.smem_bytes, stream,
+                      static_cast<const __half*>(x), static_cast<const __half*>(x_end), fp.tmU, static_cast<__half*>(out),
+                      g.c, g.h, g.w, g.k, g.pad_h, g.pad_w, g.oh, g.ow, g.tiles_h, g.tiles_w, static_cast<int>(g.P),
+                      fp.c_chunks, fp.n_blocks, fp.stg_ch_bytes, fp.nbuf, err);
 }
 
 }  // namespace wg

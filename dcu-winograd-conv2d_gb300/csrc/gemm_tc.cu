@@ -27,6 +27,7 @@
 #include <algorithm>
 
 #include "wg_kernels.h"
+#include "wg_launch.h"
 #include "wg_ptx.cuh"
 
 namespace wg {
@@ -134,6 +135,8 @@ __device__ __forceinline__ void gemm_body(const GemmDesc* __restrict__ descs, in
         *abort_flag = 0;
         fence_barrier_init();
     }
+    pdl_wait();     // V and U written, earlier readers of M done
+    pdl_trigger();
     if (warp == 1) tmem_alloc(tmem_slot, Cfg::kTmemCols);
     tc_fence_before();
     __syncthreads();
@@ -275,8 +278,7 @@ cudaError_t gemm_launch(const GemmDesc& d, int grid, DevErr* err, cudaStream_t s
     auto kern = wino_gemm_kernel<BN, BF16, MT>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, GemmCfg<BN>::kSmem);
     if (e != cudaSuccess) return e;
-    kern<<<grid, 192, GemmCfg<BN>::kSmem, s>>>(d, err);
-    return cudaGetLastError();
+    return launch_pdl(kern, dim3(grid), dim3(192), GemmCfg<BN>::kSmem, s, d, err);
 }
 
 template <int BN, bool BF16, class MT>
@@ -285,8 +287,7 @@ cudaError_t gemm_grouped_launch(const GemmDesc* descs, int ndesc, long long tota
     auto kern = wino_gemm_grouped<BN, BF16, MT>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, GemmCfg<BN>::kSmem);
     if (e != cudaSuccess) return e;
-    kern<<<grid, 192, GemmCfg<BN>::kSmem, s>>>(descs, ndesc, total, err);
-    return cudaGetLastError();
+    return launch_pdl(kern, dim3(grid), dim3(192), GemmCfg<BN>::kSmem, s, descs, ndesc, total, err);
 }
 
 // One template instance per (BN, operand type, M type); `single` selects the

@@ -260,10 +260,10 @@ struct Server {
         cudaError_t e = cudaSuccess;
         if (!in2.empty() && e == cudaSuccess)
             e = launch_input_transform_grouped(Xform::F2, OpType::F16, reinterpret_cast<const InDesc*>(d + o_in2),
-                                               static_cast<int>(in2.size()), blk_in2, smem2, err, s);
+                                               static_cast<int>(in2.size()), blk_in2, smem2, false, err, s);
         if (!in4.empty() && e == cudaSuccess)
             e = launch_input_transform_grouped(Xform::F4, OpType::F16, reinterpret_cast<const InDesc*>(d + o_in4),
-                                               static_cast<int>(in4.size()), blk_in4, smem4, err, s);
+                                               static_cast<int>(in4.size()), blk_in4, smem4, false, err, s);
         for (const GG& g : gg)
             if (e == cudaSuccess)
                 e = launch_gemm_grouped(reinterpret_cast<const GemmDesc*>(d + g.off), g.n, g.tiles, OpType::F16, g.m == 4,

@@ -28,6 +28,7 @@
 #include <algorithm>
 
 #include "wg_kernels.h"
+#include "wg_launch.h"
 #include "wg_ptx.cuh"
 #include "wg_transforms.cuh"
 
@@ -101,6 +102,8 @@ __global__ void __launch_bounds__(256) tile_scale_kernel(const __half* __restric
                                                          int C, int H, int W, int pad_h, int pad_w, int tiles_h,
                                                          int tiles_w, long long P) {
     constexpr int A = M + 2;
+    pdl_wait();
+    pdl_trigger();
     const long long p = static_cast<long long>(blockIdx.x) * 8 + (threadIdx.x >> 5);
     const int lane = threadIdx.x & 31;
     if (p >= P) return;
@@ -136,169 +139,279 @@ __global__ void __launch_bounds__(256) tile_scale_kernel(const __half* __restric
 }
 
 // ---- input transform -------------------------------------------------------------
+// Persistent CTAs walk a list of work items (image, block of tile rows, block
+// of up to 32 channels).  Each item's input rows are staged in shared memory
+// with one cp.async.bulk per channel, issued by warp 0 one item ahead into the
+// other half of a double buffer, so the copies of item i+1 overlap the
+// arithmetic of item i.  A thread transforms one channel pair of one tile in
+// packed fp32x2 arithmetic; four lanes complete one 16-byte granule row and a
+// warp of eight consecutive tiles stores 128 contiguous bytes per element.
 
-constexpr int kInThreads = 256;
+constexpr int kInComputeWarps = 7;
+constexpr int kInThreads = 32 * (kInComputeWarps + 1);  // + one producer warp
+constexpr int kInHeader = 64;   // four mbarriers, an abort flag, 16 zero bytes
+constexpr int kInSlack = 256;   // bytes before and after the two buffers: reads
+                                // of columns in the padding (masked to zero)
+                                // stay inside the CTA's shared memory
 
-// Staged input of one CTA: channel c's rows [ylo, yhi) (all W columns) start
-// at byte c*stride + (src & 15) of the staging buffer.
-template <class TF, class OutT>
-__device__ __forceinline__ void input_body(const InDesc& d, int bx, int by, unsigned char* smem_raw, DevErr* err) {
-    constexpr int M = TF::M, A = TF::ALPHA;
-    const __half* __restrict__ x = d.x;
-    OutT* __restrict__ V = static_cast<OutT*>(d.V);
-    const float* __restrict__ scale = d.scale;
-    const int C = d.C, H = d.H, W = d.W, pad_h = d.pad_h, pad_w = d.pad_w, tiles_h = d.tiles_h, tiles_w = d.tiles_w;
-    const long long Pp = d.Pp;
-    const int CG = d.CG, tb = d.tb, nbh = d.nbh, cb = d.cb, stride_bytes = d.stride_bytes;
-    uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw);
-    unsigned char* stage = smem_raw + 16;
+__device__ __forceinline__ float2 f2(float a) { return make_float2(a, a); }
+// a*b + c and friends in packed fp32x2 (one instruction for two channels)
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __ffma2_rn(b, f2(-1.f), a); }
 
-    const int bh = bx % nbh;
-    const long long n = bx / nbh;
-    const int c0 = by * cb;
-    const int th0 = bh * tb;
-    const int ntb = min(tb, tiles_h - th0);
-    const int ylo = max(0, th0 * M - pad_h);
-    const int yhi = min(H, (th0 + ntb - 1) * M - pad_h + A);
-    const int rows = max(0, yhi - ylo);
-    const int nch = min(cb, C - c0);
-    const long long plane = static_cast<long long>(H) * W;
-    // bulk copies stop at the last 16-byte boundary of the input; the few
-    // elements beyond it are read from global memory directly
-    const uintptr_t lim = reinterpret_cast<uintptr_t>(d.x_end) & ~uintptr_t(15);
-
-    if (threadIdx.x == 0) {
-        mbar_init(bar, cb);  // one arrival per channel of the block
-        fence_barrier_init();
+// B^T d on an ALPHA-vector of channel pairs (same matrices as TF::bt).
+template <class TF> struct Bt2;
+template <> struct Bt2<F2> {
+    __device__ __forceinline__ static void run(const float2 (&d)[4], float2 (&o)[4]) {
+        o[0] = sub2(d[0], d[2]);
+        o[1] = add2(d[1], d[2]);
+        o[2] = sub2(d[2], d[1]);
+        o[3] = sub2(d[1], d[3]);
     }
-    __syncthreads();
-    // thread c copies channel c's rows and accounts its own bytes
-    if (threadIdx.x < cb) {
-        const int c = threadIdx.x;
-        uint32_t bytes = 0;
-        uintptr_t a16 = 0;
-        if (c < nch && rows > 0) {
-            const uintptr_t a = reinterpret_cast<uintptr_t>(x + (n * C + c0 + c) * plane + static_cast<long long>(ylo) * W);
-            const uintptr_t b = a + static_cast<uintptr_t>(rows) * W * 2;
-            a16 = a & ~uintptr_t(15);
-            const uintptr_t b16 = min_uptr((b + 15) & ~uintptr_t(15), lim);
-            if (b16 > a16) bytes = static_cast<uint32_t>(b16 - a16);
-        }
-        mbar_arrive_expect_tx(bar, bytes);
-        if (bytes)
-            bulk_g2s(stage + static_cast<size_t>(c) * stride_bytes, reinterpret_cast<const void*>(a16), bytes, bar);
+};
+template <> struct Bt2<F4> {  // points 0, +-1, 1/2, -2
+    __device__ __forceinline__ static void run(const float2 (&d)[6], float2 (&o)[6]) {
+        const float2 t = sub2(d[3], d[1]), u = sub2(d[4], d[2]);
+        o[0] = add2(fma2(d[2], f2(-2.f), fma2(t, f2(1.5f), d[0])), d[4]);
+        o[1] = sub2(fma2(d[3], f2(2.5f), fma2(d[2], f2(0.5f), d[4])), d[1]);
+        o[2] = add2(fma2(d[2], f2(-2.5f), fma2(d[3], f2(0.5f), d[4])), d[1]);
+        o[3] = fma2(t, f2(2.f), u);
+        o[4] = fma2(t, f2(-0.5f), u);
+        o[5] = add2(fma2(d[3], f2(-2.f), fma2(u, f2(1.5f), d[1])), d[5]);
     }
-    // every bulk copy of this CTA has landed before anyone reads the stage
-    if (!mbar_wait(bar, 0, nullptr, err, ERR_SITE_FULL)) {
-        const unsigned long long t0 = globaltimer_ns();
-        while (globaltimer_ns() - t0 < 2000000ull) {
-        }
-        return;
+};
+template <> struct Bt2<F4Ref> {  // points 0, +-1, +-2
+    __device__ __forceinline__ static void run(const float2 (&d)[6], float2 (&o)[6]) {
+        const float2 t = sub2(d[3], d[1]), u = sub2(d[4], d[2]);
+        o[0] = fma2(d[2], f2(-5.f), fma2(d[0], f2(4.f), d[4]));
+        o[1] = fma2(add2(d[1], d[2]), f2(-4.f), add2(d[3], d[4]));
+        o[2] = fma2(sub2(d[1], d[2]), f2(4.f), sub2(d[4], d[3]));
+        o[3] = fma2(t, f2(2.f), u);
+        o[4] = fma2(t, f2(-2.f), u);
+        o[5] = fma2(d[3], f2(-5.f), fma2(d[1], f2(4.f), d[5]));
     }
+};
 
-    // Tasks: (granule g, tile t, piece sub) with sub fastest.  A thread
-    // transforms CPT channels of one tile; LPG consecutive lanes complete one
-    // 16-byte granule row, so a warp's stores of one element are contiguous.
-    constexpr int CPT = (A == 6) ? 2 : 4;  // channels per thread
-    constexpr int LPG = 8 / CPT;           // lanes per granule row
-    const int ntiles = ntb * tiles_w;
-    const int G = (min(cb, CG * 8 - c0) + 7) / 8;
-    const long long estride = static_cast<long long>(CG) * Pp * 8;
-    for (int task = threadIdx.x; task < ntiles * G * LPG; task += blockDim.x) {
-        const int sub = task % LPG;
-        const int rest = task / LPG;
-        const int t = rest % ntiles, g = rest / ntiles;
-        const int tr = t / tiles_w, tw = t - tr * tiles_w;
-        const long long p = (n * tiles_h + th0 + tr) * tiles_w + tw;
-        const int y0 = (th0 + tr) * M - pad_h, x0 = tw * M - pad_w;
-        const float s = scale ? scale[p] : 1.f;
-        int rowoff[A];
-        bool rowok[A], colok[A];
-#pragma unroll
-        for (int i = 0; i < A; ++i) {
-            rowoff[i] = (y0 + i - ylo) * W + x0;
-            rowok[i] = y0 + i >= ylo && y0 + i < yhi;
-            colok[i] = x0 + i >= 0 && x0 + i < W;
-        }
-        uint32_t pk[A * A][CPT / 2];
-#pragma unroll
-        for (int cc = 0; cc < CPT; ++cc) {
-            const int c = g * 8 + sub * CPT + cc;
-            float t2[A * A];
-            if (c >= nch) {
-#pragma unroll
-                for (int e = 0; e < A * A; ++e) t2[e] = 0.f;
-            } else {
-                const __half* gsrc = x + (n * C + c0 + c) * plane;
-                const uintptr_t a = reinterpret_cast<uintptr_t>(gsrc + static_cast<long long>(ylo) * W);
-                const __half* sm =
-                    reinterpret_cast<const __half*>(stage + static_cast<size_t>(c) * stride_bytes + (a & 15));
-                // rows staged whole unless they run into the last partial
-                // 16-byte block of the input (then read from global memory);
-                // two copies of the column pass so the staged one compiles to
-                // shared-memory loads
-                const bool staged = a + static_cast<uintptr_t>(rows) * W * 2 <= lim;
-                auto columns = [&](const __half* src) {
-#pragma unroll
-                    for (int j = 0; j < A; ++j) {
-                        float col[A];
-#pragma unroll
-                        for (int i = 0; i < A; ++i)
-                            col[i] = (rowok[i] && colok[j]) ? __half2float(src[rowoff[i] + j]) * s : 0.f;
-                        TF::bt(col, 1, &t2[j], A);  // column pass B^T d
-                    }
-                };
-                if (staged)
-                    columns(sm);
-                else
-                    columns(gsrc + static_cast<long long>(ylo) * W);
-            }
-#pragma unroll
-            for (int i = 0; i < A; ++i) {
-                float row[A];
-                TF::bt(&t2[i * A], 1, row, 1);  // row pass (B^T d) B
-#pragma unroll
-                for (int j = 0; j < A; ++j) {
-                    uint32_t& slot = pk[i * A + j][cc >> 1];
-                    if (cc & 1)
-                        slot |= pack2<OutT>(0.f, row[j]);
-                    else
-                        slot = pack2<OutT>(row[j], 0.f);
-                }
-            }
-        }
-        OutT* dst = V + ((static_cast<long long>(c0 / 8 + g)) * Pp + p) * 8 + sub * CPT;
-#pragma unroll
-        for (int e = 0; e < A * A; ++e) {
-            if constexpr (CPT == 4)
-                *reinterpret_cast<uint2*>(dst + e * estride) = make_uint2(pk[e][0], pk[e][1]);
-            else
-                *reinterpret_cast<uint32_t*>(dst + e * estride) = pk[e][0];
-        }
-    }
+template <class T> __device__ __forceinline__ uint32_t pack2v(float2 v) { return pack2<T>(v.x, v.y); }
+
+// Item geometry.
+struct InItem {
+    long long n;
+    int c0, th0, ntb, ylo, yhi, rows, nch;
+};
+
+__device__ __forceinline__ InItem in_item(const InDesc& d, int bx, int by, int M, int A) {
+    InItem it;
+    const int bh = bx % d.nbh;
+    it.n = bx / d.nbh;
+    it.c0 = by * d.cb;
+    it.th0 = bh * d.tb;
+    it.ntb = min(d.tb, d.tiles_h - it.th0);
+    it.ylo = max(0, it.th0 * M - d.pad_h);
+    it.yhi = min(d.H, (it.th0 + it.ntb - 1) * M - d.pad_h + A);
+    it.rows = max(0, it.yhi - it.ylo);
+    it.nch = min(d.cb, d.C - it.c0);
+    return it;
 }
 
-template <class TF, class OutT>
-__global__ void __launch_bounds__(kInThreads, 2) input_transform_kernel(const __grid_constant__ InDesc d, DevErr* err) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    input_body<TF, OutT>(d, blockIdx.x, blockIdx.y, smem_raw, err);
-}
-
-// Many problems in one launch: CTA b belongs to the problem whose block range
-// [blk_begin, blk_begin + gx*gy) holds b.
-template <class TF, class OutT>
-__global__ void __launch_bounds__(kInThreads, 2) input_transform_grouped(const InDesc* __restrict__ descs, int ndesc,
-                                                                       DevErr* err) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    const long long b = blockIdx.x;
+// Problem of a work item (descriptors sorted by blk_begin).
+__device__ __forceinline__ const InDesc& in_desc_of(const InDesc* descs, int ndesc, long long item) {
     int lo = 0, hi = ndesc - 1;
     while (lo < hi) {
         const int mid = (lo + hi + 1) / 2;
-        if (descs[mid].blk_begin <= b) lo = mid; else hi = mid - 1;
+        if (descs[mid].blk_begin <= item) lo = mid; else hi = mid - 1;
     }
-    const InDesc& d = descs[lo];
-    const long long local = b - d.blk_begin;
-    input_body<TF, OutT>(d, static_cast<int>(local % d.gx), static_cast<int>(local / d.gx), smem_raw, err);
+    return descs[lo];
+}
+
+// Warp 0: lane c stages channel c of the item (rows [ylo, yhi), whole width)
+// at byte c*stride + (src & 15) of buf and arrives on bar with its byte count.
+// Bulk copies stop at the last 16-byte boundary of the input tensor; the few
+// elements after it are copied with plain loads before the arrival (whose
+// release orders them before the consumers' reads).
+template <int M, int A>
+__device__ __forceinline__ void in_issue(const InDesc& d, long long local, unsigned char* buf, uint64_t* bar) {
+    const int lane = threadIdx.x & 31;
+    const InItem it = in_item(d, static_cast<int>(local % d.gx), static_cast<int>(local / d.gx), M, A);
+    uint32_t bytes = 0;
+    uintptr_t a16 = 0;
+    unsigned char* dst = buf + static_cast<size_t>(lane) * d.stride_bytes;
+    if (lane < it.nch && it.rows > 0) {
+        const long long plane = static_cast<long long>(d.H) * d.W;
+        const uintptr_t a =
+            reinterpret_cast<uintptr_t>(d.x + (it.n * d.C + it.c0 + lane) * plane + static_cast<long long>(it.ylo) * d.W);
+        const uintptr_t b = a + static_cast<uintptr_t>(it.rows) * d.W * 2;
+        const uintptr_t lim = reinterpret_cast<uintptr_t>(d.x_end) & ~uintptr_t(15);
+        a16 = a & ~uintptr_t(15);
+        const uintptr_t b16 = min_uptr((b + 15) & ~uintptr_t(15), lim);
+        if (b16 > a16) bytes = static_cast<uint32_t>(b16 - a16);
+        for (uintptr_t q = (b16 > a16 ? b16 : a16); q < b; q += 2)
+            *reinterpret_cast<uint16_t*>(dst + (q - a16)) = *reinterpret_cast<const uint16_t*>(q);
+    }
+    if (bytes) fence_proxy_async_smem();  // earlier generic reads of this buffer before the async writes
+    mbar_arrive_expect_tx(bar, bytes);
+    if (bytes) bulk_g2s(dst, reinterpret_cast<const void*>(a16), bytes, bar);
+}
+
+// Compute warp cw (of kInComputeWarps) transforms its share of the item:
+// lanes are (tile offset q, channel pair sub) with four pairs per granule
+// row; tiles q, q + Q, q + 2Q, ... of the item for every granule.
+template <class TF, class OutT, bool SCALED>
+__device__ __forceinline__ void in_compute(const InDesc& d, long long local, const unsigned char* buf,
+                                           const unsigned char* zero, int cw) {
+    constexpr int M = TF::M, A = TF::ALPHA;
+    constexpr int Q = kInComputeWarps * 8;  // tiles in flight per granule
+    const int lane = threadIdx.x & 31;
+    const InItem it = in_item(d, static_cast<int>(local % d.gx), static_cast<int>(local / d.gx), M, A);
+    const int W = d.W, tiles_w = d.tiles_w, rows = it.rows;
+    const long long Pp = d.Pp;
+    const long long plane2 = static_cast<long long>(d.H) * d.W * 2;
+    // byte offset of the first staged element of channel (c0 + c): low 4 bits
+    // of its global address (the buffer holds whole 16-byte blocks)
+    const uintptr_t first =
+        reinterpret_cast<uintptr_t>(d.x + (it.n * d.C + it.c0) * (plane2 / 2) + static_cast<long long>(it.ylo) * W);
+    const int ntiles = it.ntb * tiles_w;
+    const int G = (min(d.cb, d.CG * 8 - it.c0) + 7) / 8;
+    const long long estride = static_cast<long long>(d.CG) * Pp * 8;
+    const long long p0 = (it.n * d.tiles_h + it.th0) * tiles_w;  // first tile of the item
+    const int sub = lane & 3;
+    const int q = cw * 8 + (lane >> 2);
+    const int dtr = Q / tiles_w, dtw = Q - dtr * tiles_w;
+    OutT* __restrict__ V = static_cast<OutT*>(d.V);
+    for (int g = 0; g < G; ++g) {
+        const int c = g * 8 + sub * 2;  // channel pair (c, c+1) of the block
+        const bool ok0 = c < it.nch, ok1 = c + 1 < it.nch;
+        const unsigned char* cb0 =
+            buf + static_cast<size_t>(c) * d.stride_bytes + ((first + static_cast<uintptr_t>(c) * plane2) & 15);
+        const unsigned char* cb1 = buf + static_cast<size_t>(c + 1) * d.stride_bytes +
+                                   ((first + static_cast<uintptr_t>(c + 1) * plane2) & 15);
+        OutT* vg = V + (static_cast<long long>(it.c0 / 8 + g) * Pp + p0) * 8 + sub * 2;
+        int tr = q / tiles_w, tw = q - tr * tiles_w;
+        for (int t = q; t < ntiles; t += Q) {
+            const int y0 = (it.th0 + tr) * M - d.pad_h - it.ylo, x0 = tw * M - d.pad_w;
+            // zero padding without per-element masks: a row outside the
+            // staged rows (or a channel past C) reads the zero block, and a
+            // column outside the image takes the zero upper half of the
+            // zero-extended 16-bit loads through the byte-permute selector
+            uint32_t sel[A];
+#pragma unroll
+            for (int j = 0; j < A; ++j) sel[j] = (x0 + j >= 0 && x0 + j < W) ? 0x5410u : 0x3232u;
+            float2 s2 = f2(1.f);
+            if constexpr (SCALED) s2 = f2(d.scale ? d.scale[p0 + t] : 1.f);  // unscaled problems of a group
+            // rows first: r[i][.] = d[i][.] B, then columns: V[.][j] = B^T r[.][j]
+            float2 r[A][A];
+#pragma unroll
+            for (int i = 0; i < A; ++i) {
+                const int yr = y0 + i;
+                const bool rok = yr >= 0 && yr < rows;
+                const int ofs = yr * W * 2 + 2 * x0;
+                const uint16_t* r0 = reinterpret_cast<const uint16_t*>(rok && ok0 ? cb0 + ofs : zero);
+                const uint16_t* r1 = reinterpret_cast<const uint16_t*>(rok && ok1 ? cb1 + ofs : zero);
+                float2 dv[A];
+#pragma unroll
+                for (int j = 0; j < A; ++j) {
+                    const uint32_t h = __byte_perm(r0[j], r1[j], sel[j]);
+                    float2 v = __half22float2(*reinterpret_cast<const __half2*>(&h));
+                    if constexpr (SCALED) v = __fmul2_rn(v, s2);
+                    dv[j] = v;
+                }
+                Bt2<TF>::run(dv, r[i]);
+            }
+            uint32_t pk[A * A];
+#pragma unroll
+            for (int j = 0; j < A; ++j) {
+                float2 col[A], v[A];
+#pragma unroll
+                for (int i = 0; i < A; ++i) col[i] = r[i][j];
+                Bt2<TF>::run(col, v);
+#pragma unroll
+                for (int i = 0; i < A; ++i) pk[i * A + j] = pack2v<OutT>(v[i]);
+            }
+            // element e at dst + e * estride, stored in order with one running pointer
+            OutT* dst = vg + static_cast<long long>(t) * 8;
+#pragma unroll
+            for (int e = 0; e < A * A; ++e) {
+                *reinterpret_cast<uint32_t*>(dst) = pk[e];
+                dst += estride;
+            }
+            tw += dtw;
+            tr += dtr;
+            if (tw >= tiles_w) {
+                tw -= tiles_w;
+                ++tr;
+            }
+        }
+    }
+}
+
+// descs: one problem (kernel parameter) or many (device array sorted by
+// blk_begin); items [0, total) are split round robin over the grid.
+// Warp kInComputeWarps is the producer: it stages item k into buffer k % 2
+// once the compute warps have released that buffer (empty barrier, one
+// arrival per compute warp) and signals the full barrier; the compute warps
+// never wait for one another.
+template <class TF, class OutT, bool SCALED>
+__device__ __forceinline__ void input_body(const InDesc* descs, int ndesc, long long total, int buf_bytes,
+                                           unsigned char* smem_raw, DevErr* err) {
+    constexpr int M = TF::M, A = TF::ALPHA;
+    uint64_t* full = reinterpret_cast<uint64_t*>(smem_raw);
+    uint64_t* empty = full + 2;
+    volatile int* abort_flag = reinterpret_cast<volatile int*>(full + 4);
+    unsigned char* zero = smem_raw + 48;  // 16 zero bytes: the ALPHA elements of a padding row
+    unsigned char* bufs = smem_raw + kInHeader + kInSlack;
+    const int warp = threadIdx.x >> 5;
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < 2; ++i) {
+            mbar_init(&full[i], 32);                // every producer lane arrives
+            mbar_init(&empty[i], kInComputeWarps);  // one arrival per compute warp
+        }
+        *abort_flag = 0;
+        *reinterpret_cast<uint4*>(zero) = make_uint4(0u, 0u, 0u, 0u);
+        fence_barrier_init();
+    }
+    pdl_wait();     // input written, earlier readers of V done
+    pdl_trigger();
+    __syncthreads();
+    if (warp == kInComputeWarps) {
+        int k = 0;
+        for (long long item = blockIdx.x; item < total; item += gridDim.x, ++k) {
+            const int b = k & 1;
+            if (!mbar_wait(&empty[b], ((k >> 1) & 1) ^ 1u, abort_flag, err, ERR_SITE_EMPTY)) break;
+            const InDesc& d = in_desc_of(descs, ndesc, item);
+            in_issue<M, A>(d, item - d.blk_begin, bufs + b * buf_bytes, &full[b]);
+        }
+    } else {
+        int k = 0;
+        for (long long item = blockIdx.x; item < total; item += gridDim.x, ++k) {
+            const int b = k & 1;
+            if (!mbar_wait(&full[b], (k >> 1) & 1, abort_flag, err, ERR_SITE_FULL)) break;
+            const InDesc& d = in_desc_of(descs, ndesc, item);
+            in_compute<TF, OutT, SCALED>(d, item - d.blk_begin, bufs + b * buf_bytes, zero, warp);
+            __syncwarp();
+            if ((threadIdx.x & 31) == 0) mbar_arrive(&empty[b]);
+        }
+    }
+    if (*abort_flag) {
+        // let the copies still in flight land before the CTA retires
+        const unsigned long long t0 = globaltimer_ns();
+        while (globaltimer_ns() - t0 < 2000000ull) {
+        }
+    }
+}
+
+template <class TF, class OutT, bool SCALED>
+__global__ void __launch_bounds__(kInThreads, 2)
+    input_transform_kernel(const __grid_constant__ InDesc d, long long total, int buf_bytes, DevErr* err) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    input_body<TF, OutT, SCALED>(&d, 1, total, buf_bytes, smem_raw, err);
+}
+
+template <class TF, class OutT, bool SCALED>
+__global__ void __launch_bounds__(kInThreads, 2) input_transform_grouped(const InDesc* __restrict__ descs, int ndesc,
+                                                                       long long total, int buf_bytes, DevErr* err) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    input_body<TF, OutT, SCALED>(descs, ndesc, total, buf_bytes, smem_raw, err);
 }
 
 // ---- output transform ----------------------------------------------------------
@@ -387,11 +500,15 @@ __device__ __forceinline__ void output_body(const OutDesc& d, long long bx, int 
 
 template <class TF, class MT>
 __global__ void __launch_bounds__(kOutThreads) output_transform_kernel(const __grid_constant__ OutDesc d) {
+    pdl_wait();     // M written, earlier readers of the output done
+    pdl_trigger();
     output_body<TF, MT>(d, blockIdx.x, blockIdx.y);
 }
 
 template <class TF, class MT>
 __global__ void __launch_bounds__(kOutThreads) output_transform_grouped(const OutDesc* __restrict__ descs, int ndesc) {
+    pdl_wait();
+    pdl_trigger();
     const long long b = blockIdx.x;
     int lo = 0, hi = ndesc - 1;
     while (lo < hi) {
@@ -404,59 +521,95 @@ __global__ void __launch_bounds__(kOutThreads) output_transform_grouped(const Ou
 }
 
 struct InBlocking {
-    int tb, nbh, cb, stride, smem;
+    int tb, nbh, cb, stride, buf;
 };
 
+int sm_count() {
+    static int cached[64] = {0};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) dev = 0;
+    if (!cached[dev]) {
+        int n = 0;
+        if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) n = 148;
+        cached[dev] = n;
+    }
+    return cached[dev];
+}
+
+constexpr int kInBufBudget = 56 * 1024;   // per buffer: two CTAs of two buffers per SM
+constexpr int kSmemPerSm = 233472;        // shared memory of one SM (228 KB)
+
+int in_smem_total(int buf) { return kInHeader + 2 * kInSlack + 2 * buf; }
+int in_ctas_per_sm(int smem) { return std::max(1, std::min(2, kSmemPerSm / (smem + 1024))); }
+
+// Tile-row block tb and channel block cb: the items (image, tile-row block,
+// channel block) are spread over the persistent grid; the choice minimises
+// rounds of items per CTA x rounds of tiles per compute lane x staged rows
+// per output row (halo re-reads).
 InBlocking choose_in_blocking(const Geom& g) {
-    InBlocking b;
     const int M = g.m, A = g.alpha;
-    const int budget = 64 * 1024;
-    b.cb = 32;
-    b.tb = 1;
     auto stride_for = [&](int tb) {
         const int rows = std::min(g.h, tb * M + A - M);
         return (rows * g.w * 2 + 16 + 15) / 16 * 16;
     };
-    while (b.cb > 8 && b.cb * stride_for(1) > budget) b.cb /= 2;
-    for (int tb = 1; tb <= g.tiles_h; ++tb) {
-        if (b.cb * stride_for(tb) > budget || tb * g.tiles_w > 512) break;
-        b.tb = tb;
+    InBlocking best{1, g.tiles_h, 8, stride_for(1), 8 * stride_for(1)};
+    double best_cost = 1e300;
+    const long long slots = static_cast<long long>(sm_count()) * 2;
+    for (int cb = 32; cb >= 8; cb /= 2) {
+        if (cb > 8 && cb * stride_for(1) > kInBufBudget) continue;
+        if (cb > 8 && cb >= 2 * ((g.c + 7) / 8 * 8)) continue;  // no block twice the channel count
+        for (int tb = 1; tb <= g.tiles_h; ++tb) {
+            const int st = stride_for(tb);
+            if ((tb > 1 && cb * st > kInBufBudget) || tb * g.tiles_w > 1024) break;
+            const int nbh = (g.tiles_h + tb - 1) / tb;
+            const long long items = static_cast<long long>(g.n) * nbh * ((g.c + cb - 1) / cb);
+            // per compute lane: granules x rounds of kInComputeWarps*8 tiles
+            const long long lane_rounds = static_cast<long long>(cb / 8) *
+                                          ((static_cast<long long>(tb) * g.tiles_w + kInComputeWarps * 8 - 1) /
+                                           (kInComputeWarps * 8));
+            const double rounds = static_cast<double>((items + slots - 1) / slots);
+            const double cost = rounds * static_cast<double>(lane_rounds) * (static_cast<double>(tb * M + A - M) / (tb * M));
+            if (cost < best_cost * 0.999) {
+                best_cost = cost;
+                best = InBlocking{tb, nbh, cb, st, (cb * st + 15) / 16 * 16};
+            }
+        }
     }
-    b.nbh = (g.tiles_h + b.tb - 1) / b.tb;
-    b.stride = stride_for(b.tb);
-    b.smem = 16 + b.cb * b.stride;
-    return b;
+    return best;
 }
 
-template <class TF, class OutT>
+template <class TF, class OutT, bool SCALED>
 cudaError_t input_launch(const InDesc& d, int smem, DevErr* err, cudaStream_t s) {
-    auto kern = input_transform_kernel<TF, OutT>;
+    auto kern = input_transform_kernel<TF, OutT, SCALED>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e != cudaSuccess) return e;
-    kern<<<dim3(static_cast<unsigned>(d.gx), static_cast<unsigned>(d.gy)), kInThreads, smem, s>>>(d, err);
-    return cudaGetLastError();
+    const long long total = d.gx * d.gy;
+    const long long grid = std::min<long long>(total, static_cast<long long>(sm_count()) * in_ctas_per_sm(smem));
+    return launch_pdl(kern, dim3(static_cast<unsigned>(grid)), dim3(kInThreads), smem, s, d, total,
+                      (smem - kInHeader - 2 * kInSlack) / 2, err);
 }
 
-template <class TF, class OutT>
-cudaError_t input_grouped_launch(const InDesc* descs, int ndesc, long long blocks, int smem, DevErr* err,
+template <class TF, class OutT, bool SCALED>
+cudaError_t input_grouped_launch(const InDesc* descs, int ndesc, long long total, int smem, DevErr* err,
                                  cudaStream_t s) {
-    auto kern = input_transform_grouped<TF, OutT>;
+    auto kern = input_transform_grouped<TF, OutT, SCALED>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e != cudaSuccess) return e;
-    kern<<<static_cast<unsigned>(blocks), kInThreads, smem, s>>>(descs, ndesc, err);
-    return cudaGetLastError();
+    const long long grid = std::min<long long>(total, static_cast<long long>(sm_count()) * in_ctas_per_sm(smem));
+    return launch_pdl(kern, dim3(static_cast<unsigned>(grid)), dim3(kInThreads), smem, s, descs, ndesc, total,
+                      (smem - kInHeader - 2 * kInSlack) / 2, err);
 }
 
 template <class TF, class MT>
 cudaError_t output_launch(const OutDesc& d, cudaStream_t s) {
-    output_transform_kernel<TF, MT><<<dim3(static_cast<unsigned>(d.gx), static_cast<unsigned>(d.gy)), kOutThreads, 0, s>>>(d);
-    return cudaGetLastError();
+    return launch_pdl(output_transform_kernel<TF, MT>, dim3(static_cast<unsigned>(d.gx), static_cast<unsigned>(d.gy)),
+                      dim3(kOutThreads), 0, s, d);
 }
 
 template <class TF, class MT>
 cudaError_t output_grouped_launch(const OutDesc* descs, int ndesc, long long blocks, cudaStream_t s) {
-    output_transform_grouped<TF, MT><<<static_cast<unsigned>(blocks), kOutThreads, 0, s>>>(descs, ndesc);
-    return cudaGetLastError();
+    return launch_pdl(output_transform_grouped<TF, MT>, dim3(static_cast<unsigned>(blocks)), dim3(kOutThreads), 0, s,
+                      descs, ndesc);
 }
 
 template <class TF, class OutT>
@@ -490,13 +643,12 @@ cudaError_t launch_filter_transform(Xform xf, OpType op, const void* weight, voi
 
 cudaError_t launch_tile_scale(const Geom& g, const void* x, float* scale, cudaStream_t stream) {
     const unsigned blocks = static_cast<unsigned>((g.P + 7) / 8);
+    const __half* xh = static_cast<const __half*>(x);
     if (g.m == 2)
-        tile_scale_kernel<2><<<blocks, 256, 0, stream>>>(static_cast<const __half*>(x), scale, g.c, g.h, g.w, g.pad_h,
-                                                         g.pad_w, g.tiles_h, g.tiles_w, g.P);
-    else
-        tile_scale_kernel<4><<<blocks, 256, 0, stream>>>(static_cast<const __half*>(x), scale, g.c, g.h, g.w, g.pad_h,
-                                                         g.pad_w, g.tiles_h, g.tiles_w, g.P);
-    return cudaGetLastError();
+        return launch_pdl(tile_scale_kernel<2>, dim3(blocks), dim3(256), 0, stream, xh, scale, g.c, g.h, g.w, g.pad_h,
+                          g.pad_w, g.tiles_h, g.tiles_w, g.P);
+    return launch_pdl(tile_scale_kernel<4>, dim3(blocks), dim3(256), 0, stream, xh, scale, g.c, g.h, g.w, g.pad_h,
+                      g.pad_w, g.tiles_h, g.tiles_w, g.P);
 }
 
 InDesc make_in_desc(const Geom& g, const void* x, const void* x_end, void* V, const float* scale, int* smem) {
@@ -514,7 +666,7 @@ InDesc make_in_desc(const Geom& g, const void* x, const void* x_end, void* V, co
     d.gx = static_cast<long long>(g.n) * b.nbh;
     d.gy = (g.c + b.cb - 1) / b.cb;
     d.blk_begin = 0;
-    *smem = b.smem;
+    *smem = in_smem_total(b.buf);
     return d;
 }
 
@@ -536,32 +688,46 @@ cudaError_t launch_input_transform(Xform xf, OpType op, const Geom& g, const voi
                                    const float* scale, DevErr* err, cudaStream_t stream) {
     int smem = 0;
     const InDesc d = make_in_desc(g, x, x_end, V, scale, &smem);
-    const bool bf = op == OpType::BF16;
+    const bool bf = op == OpType::BF16, sc = scale != nullptr;
     switch (xf) {
-        case Xform::F2:
-            return bf ? input_launch<F2, __nv_bfloat16>(d, smem, err, stream) : input_launch<F2, __half>(d, smem, err, stream);
+        case Xform::F2:  // never scaled
+            return bf ? input_launch<F2, __nv_bfloat16, false>(d, smem, err, stream)
+                      : input_launch<F2, __half, false>(d, smem, err, stream);
         case Xform::F4:
-            return bf ? input_launch<F4, __nv_bfloat16>(d, smem, err, stream) : input_launch<F4, __half>(d, smem, err, stream);
+            if (sc)
+                return bf ? input_launch<F4, __nv_bfloat16, true>(d, smem, err, stream)
+                          : input_launch<F4, __half, true>(d, smem, err, stream);
+            return bf ? input_launch<F4, __nv_bfloat16, false>(d, smem, err, stream)
+                      : input_launch<F4, __half, false>(d, smem, err, stream);
         case Xform::F4Ref:
-            return bf ? input_launch<F4Ref, __nv_bfloat16>(d, smem, err, stream)
-                      : input_launch<F4Ref, __half>(d, smem, err, stream);
+            if (sc)
+                return bf ? input_launch<F4Ref, __nv_bfloat16, true>(d, smem, err, stream)
+                          : input_launch<F4Ref, __half, true>(d, smem, err, stream);
+            return bf ? input_launch<F4Ref, __nv_bfloat16, false>(d, smem, err, stream)
+                      : input_launch<F4Ref, __half, false>(d, smem, err, stream);
     }
     return cudaErrorInvalidValue;
 }
 
 cudaError_t launch_input_transform_grouped(Xform xf, OpType op, const InDesc* descs, int ndesc, long long blocks,
-                                           int smem, DevErr* err, cudaStream_t stream) {
+                                           int smem, bool scaled, DevErr* err, cudaStream_t stream) {
     const bool bf = op == OpType::BF16;
     switch (xf) {
         case Xform::F2:
-            return bf ? input_grouped_launch<F2, __nv_bfloat16>(descs, ndesc, blocks, smem, err, stream)
-                      : input_grouped_launch<F2, __half>(descs, ndesc, blocks, smem, err, stream);
+            return bf ? input_grouped_launch<F2, __nv_bfloat16, false>(descs, ndesc, blocks, smem, err, stream)
+                      : input_grouped_launch<F2, __half, false>(descs, ndesc, blocks, smem, err, stream);
         case Xform::F4:
-            return bf ? input_grouped_launch<F4, __nv_bfloat16>(descs, ndesc, blocks, smem, err, stream)
-                      : input_grouped_launch<F4, __half>(descs, ndesc, blocks, smem, err, stream);
+            if (scaled)
+                return bf ? input_grouped_launch<F4, __nv_bfloat16, true>(descs, ndesc, blocks, smem, err, stream)
+                          : input_grouped_launch<F4, __half, true>(descs, ndesc, blocks, smem, err, stream);
+            return bf ? input_grouped_launch<F4, __nv_bfloat16, false>(descs, ndesc, blocks, smem, err, stream)
+                      : input_grouped_launch<F4, __half, false>(descs, ndesc, blocks, smem, err, stream);
         case Xform::F4Ref:
-            return bf ? input_grouped_launch<F4Ref, __nv_bfloat16>(descs, ndesc, blocks, smem, err, stream)
-                      : input_grouped_launch<F4Ref, __half>(descs, ndesc, blocks, smem, err, stream);
+            if (scaled)
+                return bf ? input_grouped_launch<F4Ref, __nv_bfloat16, true>(descs, ndesc, blocks, smem, err, stream)
+                          : input_grouped_launch<F4Ref, __half, true>(descs, ndesc, blocks, smem, err, stream);
+            return bf ? input_grouped_launch<F4Ref, __nv_bfloat16, false>(descs, ndesc, blocks, smem, err, stream)
+                      : input_grouped_launch<F4Ref, __half, false>(descs, ndesc, blocks, smem, err, stream);
     }
     return cudaErrorInvalidValue;
 }

@@ -67,9 +67,9 @@ struct InDesc {
     int C, H, W, pad_h, pad_w, tiles_h, tiles_w;
     long long Pp;
     int CG, tb, nbh, cb, stride_bytes;
-    long long gx;         // CTAs along (image, tile-row block)
-    int gy;               // CTAs along channel blocks
-    long long blk_begin;  // first CTA of this problem in a grouped launch
+    long long gx;         // work items along (image, tile-row block)
+    int gy;               // work items along channel blocks (cb <= 32)
+    long long blk_begin;  // first work item of this problem in a grouped launch
 };
 
 struct OutDesc {
@@ -84,12 +84,15 @@ struct OutDesc {
     long long blk_begin;
 };
 
-// Descriptor of one problem's input transform and its dynamic shared memory.
+// Descriptor of one problem's input transform and the dynamic shared memory
+// of its (persistent, double-buffered) launch.
 InDesc make_in_desc(const Geom& g, const void* x, const void* x_end, void* V, const float* scale, int* smem);
 OutDesc make_out_desc(const Geom& g, bool m_fp32, const void* Mw, void* out, const float* scale);
-// Grouped launches: `blocks` = sum of gx*gy; descs device-resident, sorted by blk_begin.
+// Grouped launches: `blocks` = sum of gx*gy work items; descs device-resident,
+// sorted by blk_begin; smem = the largest of the problems' *smem; `scaled` when
+// any problem has a per-tile scale.
 cudaError_t launch_input_transform_grouped(Xform xf, OpType op, const InDesc* descs, int ndesc, long long blocks,
-                                           int smem, DevErr* err, cudaStream_t stream);
+                                           int smem, bool scaled, DevErr* err, cudaStream_t stream);
 cudaError_t launch_output_transform_grouped(Xform xf, bool m_fp32, const OutDesc* descs, int ndesc, long long blocks,
                                             cudaStream_t stream);
 

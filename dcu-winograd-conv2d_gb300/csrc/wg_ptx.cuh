@@ -26,6 +26,12 @@ enum : unsigned int {
 // micro-seconds; a wait this long means the pipeline protocol is broken.
 constexpr unsigned long long kWaitLimitNs = 500000000ull;
 
+// Programmatic dependent launch: wait for the preceding grid on the stream to
+// complete (and its writes to be visible); allow the next grid to be
+// scheduled.  Both are no-ops for a plain launch.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
     return static_cast<uint32_t>(__cvta_generic_to_shared(p));
 }
