@@ -270,25 +270,50 @@ def make_inputs(torch, workload, device, seed):
 
 
 def roofline_for(name, wg, geo, ms, pk, pk_kind):
+    """Roofline of one kernel from its algorithmic work per launch.
+
+    GEMM-shaped kernels have both a FLOP count and a byte count; the bound is
+    the roof their arithmetic intensity puts them under (machine balance =
+    peak FLOP/s / peak bytes/s).  Algorithmic bytes (fp16 operands, M in fp32
+    for F(4x3), fp16 otherwise):
+      input_transform   x read (2*N*C*H*W) + V write (2*E*P*C)
+      gemm_tcgen05      V read (2*E*P*C) + U read (2*E*C*K) + M write (E*P*K*4 or *2)
+      output_transform  M read + y write (2*N*K*OH*OW)
+      fused2x3          x read + U read + y write
+    """
     n, c, h, w, k, m = geo
     oh, ow = h, w  # pad 1
     tiles = n * math.ceil(oh / m) * math.ceil(ow / m)
     E = (m + 2) ** 2
-    if name in ("fused2x3", "gemm_tcgen05"):
-        flops = 2.0 * E * tiles * c * k
-        ach = flops / (ms * 1e-3) / 1e12
-        peak = pk["bf16_tflops"]
-        return {"kernel": name, "bound": "tensor", "achieved": ach, "peak": peak, "unit": "TFLOP/s",
-                "frac": ach / peak, "peak_source": f"{pk_kind} bf16 dense (burst)",
-                "algorithmic_per_launch": f"{flops / 1e9:.2f} GFLOP (2*{E}*P*C*K)"}
-    if name == "input_transform":
-        byts = 2.0 * n * c * h * w + 2.0 * E * tiles * c
+    mb = 4.0 if m == 4 else 2.0
+    x_b, y_b = 2.0 * n * c * h * w, 2.0 * n * k * oh * ow
+    v_b, u_b, m_b = 2.0 * E * tiles * c, 2.0 * E * c * k, mb * E * tiles * k
+    flops = 0.0
+    if name == "gemm_tcgen05":
+        flops, byts, formula = 2.0 * E * tiles * c * k, v_b + u_b + m_b, "V + U + M"
+    elif name == "fused2x3":
+        flops, byts, formula = 2.0 * E * tiles * c * k, x_b + u_b + y_b, "x + U + y"
+    elif name == "input_transform":
+        byts, formula = x_b + v_b, "x + V"
     else:
-        byts = (4.0 if m == 4 else 2.0) * E * tiles * k + 2.0 * n * k * oh * ow
-    ach = byts / (ms * 1e-3) / 1e9
-    peak = pk["hbm_gbs"]
-    return {"kernel": name, "bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
-            "peak_source": f"{pk_kind} HBM copy", "algorithmic_per_launch": f"{byts / 1e6:.1f} MB"}
+        byts, formula = m_b + y_b, "M + y"
+    peak_bw, peak_fl = pk["hbm_gbs"], pk["bf16_tflops"]
+    out = {"kernel": name}
+    if flops and flops / byts > peak_fl * 1e12 / (peak_bw * 1e9):
+        ach = flops / (ms * 1e-3) / 1e12
+        out.update({"bound": "tensor", "achieved": ach, "peak": peak_fl, "unit": "TFLOP/s", "frac": ach / peak_fl,
+                    "peak_source": f"{pk_kind} bf16 dense (burst)"})
+    else:
+        ach = byts / (ms * 1e-3) / 1e9
+        out.update({"bound": "hbm", "achieved": ach, "peak": peak_bw, "unit": "GB/s", "frac": ach / peak_bw,
+                    "peak_source": f"{pk_kind} HBM copy"})
+    out["algorithmic_per_launch"] = f"{byts / 1e6:.1f} MB ({formula})" + (
+        f", {flops / 1e9:.2f} GFLOP (2*{E}*P*C*K)" if flops else "")
+    out["algorithmic_bytes"] = byts
+    if flops:
+        out["tensor_frac"] = flops / (ms * 1e-3) / 1e12 / peak_fl
+    out["launch_us"] = ms * 1e3
+    return out
 
 
 def committed_traffic(kernel, workload):

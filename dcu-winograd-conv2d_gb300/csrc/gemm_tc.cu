@@ -13,7 +13,8 @@
 //   warp 1      allocates TMEM and issues tcgen05.mma (M=128, N=BN, K=16)
 //               from one thread; accumulators double-buffered in TMEM so the
 //               epilogue of one output tile overlaps the main loop of the next;
-//   warps 2-5   epilogue: tcgen05.ld 32 lanes x 16 columns, convert, 16-byte
+//   warps 2-5   epilogue: tcgen05.ld 32 lanes x 32 columns (the next chunk's
+//               load in flight while this one is stored), convert, 16-byte
 //               granule stores of M (a warp writes 512 contiguous bytes).
 // Work items are (problem, e, 128-tile block, BN-channel block), handed out
 // round robin over one global index; a grouped launch covers many problems
@@ -47,37 +48,37 @@ struct GemmCfg {
     static constexpr int kSmem = kStages * kStageBytes + 1024 /*align*/ + 256 /*barriers*/;
 };
 
-// Epilogue stores of 16 accumulator columns (output channels k0..k0+15) of
+// Epilogue stores of 32 accumulator columns (output channels k0..k0+31) of
 // one tile row p into the granule layout.
 template <class MT>
-__device__ __forceinline__ void store16(MT* Mw, const uint32_t (&r)[16], long long P, long long p, int k0, int kg_count,
+__device__ __forceinline__ void store32(MT* Mw, const uint32_t (&r)[32], long long P, long long p, int k0, int kg_count,
                                         int e);
 
-// fp16 M[e][Kp/8][P][8]: two granules
+// fp16 M[e][Kp/8][P][8]: four granules
 template <>
-__device__ __forceinline__ void store16<__half>(__half* Mw, const uint32_t (&r)[16], long long P, long long p, int k0,
+__device__ __forceinline__ void store32<__half>(__half* Mw, const uint32_t (&r)[32], long long P, long long p, int k0,
                                                 int kg_count, int e) {
-    uint32_t h[8];
+    uint32_t h[16];
 #pragma unroll
-    for (int i = 0; i < 8; ++i) {
+    for (int i = 0; i < 16; ++i) {
         __half2 v = __floats2half2_rn(__uint_as_float(r[2 * i]), __uint_as_float(r[2 * i + 1]));
         h[i] = *reinterpret_cast<uint32_t*>(&v);
     }
     const int g0 = k0 / 8;
 #pragma unroll
-    for (int j = 0; j < 2; ++j)
+    for (int j = 0; j < 4; ++j)
         if (g0 + j < kg_count)
             *reinterpret_cast<uint4*>(Mw + ((static_cast<long long>(e) * kg_count + g0 + j) * P + p) * 8) =
                 make_uint4(h[4 * j], h[4 * j + 1], h[4 * j + 2], h[4 * j + 3]);
 }
 
-// fp32 M[e][Kp/4][P][4]: four granules
+// fp32 M[e][Kp/4][P][4]: eight granules
 template <>
-__device__ __forceinline__ void store16<float>(float* Mw, const uint32_t (&r)[16], long long P, long long p, int k0,
+__device__ __forceinline__ void store32<float>(float* Mw, const uint32_t (&r)[32], long long P, long long p, int k0,
                                                int kg_count, int e) {
     const int g0 = k0 / 4;
 #pragma unroll
-    for (int j = 0; j < 4; ++j)
+    for (int j = 0; j < 8; ++j)
         if (g0 + j < kg_count)
             *reinterpret_cast<uint4*>(Mw + ((static_cast<long long>(e) * kg_count + g0 + j) * P + p) * 4) =
                 make_uint4(r[4 * j], r[4 * j + 1], r[4 * j + 2], r[4 * j + 3]);
@@ -233,12 +234,17 @@ __device__ __forceinline__ void gemm_body(const GemmDesc* __restrict__ descs, in
             tc_fence_after();
             const long long p = static_cast<long long>(it.mb) * kBM + row;
             const uint32_t taddr = tmem_base + (static_cast<uint32_t>(quarter * 32) << 16) + static_cast<uint32_t>(acc * BN);
-#pragma unroll 1
-            for (int c0 = 0; c0 < BN; c0 += 16) {
-                uint32_t r[16];
-                tmem_ld_x16(taddr + c0, r);
-                tc_wait_ld();
-                if (p < P) store16<MT>(Mw, r, P, p, it.nb * BN + c0, kg_count, it.e);
+            // 32 columns per load; the load of chunk i+1 is in flight while
+            // chunk i is stored
+            constexpr int kChunks = BN / 32;
+            uint32_t r[2][32];
+            tmem_ld_x32(taddr, r[0]);
+            tc_wait_ld(r[0]);
+#pragma unroll
+            for (int ch = 0; ch < kChunks; ++ch) {
+                if (ch + 1 < kChunks) tmem_ld_x32(taddr + (ch + 1) * 32, r[(ch + 1) & 1]);
+                if (p < P) store32<MT>(Mw, r[ch & 1], P, p, it.nb * BN + ch * 32, kg_count, it.e);
+                if (ch + 1 < kChunks) tc_wait_ld(r[(ch + 1) & 1]);
             }
             tc_fence_before();
             mbar_arrive(&tempty[acc]);
