@@ -307,12 +307,15 @@ int Plan::run(cudaStream_t s) {
     return CONV2D_OK;
 }
 
-// Host input -> device -> host output.  The batch is cut into up to
-// kHostChunks image chunks; chunk i's input copy (copy-in stream), compute
-// (caller stream) and output copy (copy-out stream) are ordered by events, so
-// the copies of one chunk overlap the compute of its neighbours.
+// Host input -> device -> host output.  The batch is cut into image chunks
+// of at least 8 MB of copies each (at most kMaxHostChunks); chunk i's input copy
+// (copy-in stream), compute (caller stream) and output copy (copy-out stream)
+// are ordered by events, so the copies of one chunk overlap the compute of
+// its neighbours and the two copy directions overlap each other.  Smaller
+// chunks shorten the pipeline's fill (first input copy) and drain (last
+// output copy) but run the kernels on fewer tiles; the host link, not the
+// GPU, bounds this call for large inputs.
 int Plan::run_host(const void* host_in, void* host_out, cudaStream_t s) {
-    constexpr int kHostChunks = 4;
     const int n = static_cast<int>(prob.n);
     const long long in_img_b = static_cast<long long>(g.c) * g.h * g.w * 2;
     const long long out_img_b = static_cast<long long>(g.k) * g.oh * g.ow * 2;
@@ -322,7 +325,9 @@ int Plan::run_host(const void* host_in, void* host_out, cudaStream_t s) {
         int st = filter(s);
         if (st) return st;
     }
-    const int chunks = std::min(n, kHostChunks);
+    const long long copy_bytes = static_cast<long long>(n) * (in_img_b + out_img_b);
+    const int chunks = static_cast<int>(
+        std::max(1LL, std::min<long long>({static_cast<long long>(n), kMaxHostChunks, copy_bytes / (8LL << 20)})));
     const int hc = (n + chunks - 1) / chunks;
     const int nch = (n + hc - 1) / hc;
     if (!host_in_stream) {
@@ -345,9 +350,9 @@ int Plan::run_host(const void* host_in, void* host_out, cudaStream_t s) {
         if (ce != cudaSuccess) return cuda_fail(ce, "GEMM plan (host chunks)");
         host_chunk_n = hc;
     }
-    cudaEvent_t* ev_in = host_ev;            // [kHostChunks]
-    cudaEvent_t* ev_done = host_ev + 8;      // [kHostChunks]
-    cudaEvent_t ev_start = host_ev[16], ev_end = host_ev[17];
+    cudaEvent_t* ev_in = host_ev;                     // [kMaxHostChunks]
+    cudaEvent_t* ev_done = host_ev + kMaxHostChunks;  // [kMaxHostChunks]
+    cudaEvent_t ev_start = host_ev[2 * kMaxHostChunks], ev_end = host_ev[2 * kMaxHostChunks + 1];
     // the copies must not overwrite the input before earlier work on s is done
     cudaEventRecord(ev_start, s);
     cudaStreamWaitEvent(host_in_stream, ev_start, 0);

@@ -84,7 +84,9 @@ __device__ __forceinline__ void store32<float>(float* Mw, const uint32_t (&r)[32
                 make_uint4(r[4 * j], r[4 * j + 1], r[4 * j + 2], r[4 * j + 3]);
 }
 
-// Work item t -> problem index (advanced monotonically) and (e, mb, nb).
+// Work item t -> problem index (advanced monotonically) and (e, mb, nb):
+// channel block fastest (the V tile is reused from L2), then tile block, then
+// element, so concurrent CTAs write M in long runs of a few element planes.
 struct Item {
     int e, mb, nb;
 };

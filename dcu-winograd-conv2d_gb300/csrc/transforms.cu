@@ -195,7 +195,9 @@ template <> struct Bt2<F4Ref> {  // points 0, +-1, +-2
 
 template <class T> __device__ __forceinline__ uint32_t pack2v(float2 v) { return pack2<T>(v.x, v.y); }
 
-// Item geometry.
+// Item geometry.  Work item `local` = bx * gy + by: the channel blocks of one
+// (image, tile-row block) are adjacent, so the CTAs in flight stage rows of a
+// few images at a time.
 struct InItem {
     long long n;
     int c0, th0, ntb, ylo, yhi, rows, nch;
@@ -233,7 +235,7 @@ __device__ __forceinline__ const InDesc& in_desc_of(const InDesc* descs, int nde
 template <int M, int A>
 __device__ __forceinline__ void in_issue(const InDesc& d, long long local, unsigned char* buf, uint64_t* bar) {
     const int lane = threadIdx.x & 31;
-    const InItem it = in_item(d, static_cast<int>(local % d.gx), static_cast<int>(local / d.gx), M, A);
+    const InItem it = in_item(d, static_cast<int>(local / d.gy), static_cast<int>(local % d.gy), M, A);
     uint32_t bytes = 0;
     uintptr_t a16 = 0;
     unsigned char* dst = buf + static_cast<size_t>(lane) * d.stride_bytes;
@@ -263,7 +265,7 @@ __device__ __forceinline__ void in_compute(const InDesc& d, long long local, con
     constexpr int M = TF::M, A = TF::ALPHA;
     constexpr int Q = kInComputeWarps * 8;  // tiles in flight per granule
     const int lane = threadIdx.x & 31;
-    const InItem it = in_item(d, static_cast<int>(local % d.gx), static_cast<int>(local / d.gx), M, A);
+    const InItem it = in_item(d, static_cast<int>(local / d.gy), static_cast<int>(local % d.gy), M, A);
     const int W = d.W, tiles_w = d.tiles_w, rows = it.rows;
     const long long Pp = d.Pp;
     const long long plane2 = static_cast<long long>(d.H) * d.W * 2;

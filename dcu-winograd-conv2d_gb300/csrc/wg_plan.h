@@ -60,7 +60,8 @@ struct Plan {
     int host_chunk_n = 0;
     GemmPlan host_gemm_full{}, host_gemm_tail{};
     cudaStream_t host_in_stream = nullptr, host_out_stream = nullptr;
-    cudaEvent_t host_ev[2 * 8 + 2] = {};
+    static constexpr int kMaxHostChunks = 8;
+    cudaEvent_t host_ev[2 * kMaxHostChunks + 2] = {};
 
     ~Plan();
     int build(const problem_t* pr, const conv2d_options_t* opt);

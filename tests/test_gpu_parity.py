@@ -244,12 +244,15 @@ def test_refresh_filter_after_in_place_change(wg):
     assert O.rel_errors(y.cpu().numpy(), r64)[0] <= TOL[2]
 
 
-@pytest.mark.parametrize("algo", [0, 1, 2])
-@pytest.mark.parametrize("n", [1, 2, 7])
-def test_host_buffer_entry_point(wg, algo, n):
+HOST_CASES = [(a, n, 24, 16, 24) for a in (0, 1, 2) for n in (1, 2, 7)] + \
+    [(a, 11, 64, 100, 64) for a in (0, 1, 2)]  # 28.2 MB of copies: 3 chunks of 4, 4, 3 images
+
+
+@pytest.mark.parametrize("algo,n,c,h,k", HOST_CASES)
+def test_host_buffer_entry_point(wg, algo, n, c, h, k):
     """Host in -> device -> host out, with the batch cut into overlapped
-    chunks (uneven for n = 7); equal to the device-buffer call bit for bit."""
-    c, h, k = 24, 16, 24
+    chunks of at least 8 MB of copies (one chunk for the small cases, three
+    uneven ones for the large); equal to the device-buffer call bit for bit."""
     x, wt = O.uniform_inputs(13 + n, n, c, h, h, k)
     xt = torch.empty((n, c, h, h), dtype=torch.float16, device="cuda")
     wtt = torch.from_numpy(wt).cuda()
