@@ -201,6 +201,19 @@ def cpu_sample(O, x16, w16, n_img, threads):
     return time.perf_counter() - t0, flops, "port", threads
 
 
+def replica_throughput(local_ms, flops_per_step, steps, world, dist, device):
+    """Replicas only: every rank runs the same workload on its own GPU with no
+    data-path exchange.  The job's time is the slowest rank's (MAX over ranks)
+    and `value` counts the work of all ranks: world * flops * steps / time."""
+    import torch
+    total_ms = float(local_ms)
+    if dist is not None and world > 1:
+        tt = torch.tensor([total_ms], device=device)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        total_ms = float(tt.item())
+    return total_ms, world * flops_per_step * steps / (total_ms * 1e-3) / 1e12
+
+
 def reference_arm(args):
     """--impl reference: the reference's CPU implementation of the path on the
     host cores, same workload/metric; each step is a bounded sample."""
@@ -395,14 +408,9 @@ def our_arm(args):
     if dist:
         dist.barrier()
     clocks = sampler.stop()
-    total_ms = t_start.elapsed_time(t_end)
-    if dist:
-        tt = torch.tensor([total_ms], device=device)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        total_ms = float(tt.item())
     per_step = [a.elapsed_time(b) for a, b in evs]
+    total_ms, value = replica_throughput(t_start.elapsed_time(t_end), flops, args.steps, world, dist, device)
     ms_per_step = total_ms / args.steps
-    value = world * flops * args.steps / (total_ms * 1e-3) / 1e12
 
     # per-kernel durations (CUDA events between the launches of one call)
     names = ops[0].kernel_names()
