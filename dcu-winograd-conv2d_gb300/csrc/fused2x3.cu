@@ -8,9 +8,10 @@
 //     chunks of 16, 16 wave64 MMAC GEMMs);
 //   * the input rows a chunk needs are staged with cp.async.bulk (one
 //     contiguous copy per channel and image), double-buffered one chunk ahead;
-//   * warps 0-7 (lanes over consecutive tiles) run B^T d B in fp32 from shared
-//     memory and write the 16 Winograd-domain tiles into shared memory in the
-//     tcgen05 canonical K-major layout;
+//   * warps 0-7 (lanes over consecutive tiles) run B^T d B from shared memory
+//     (packed fp16 on channel pairs for fp16 operands, fp32 for bf16) and
+//     write the 16 Winograd-domain tiles into shared memory in the tcgen05
+//     canonical K-major layout;
 //   * the transformed filter U (made once per weight set) arrives by one 4-D
 //     TMA per chunk;
 //   * warp 8 issues the 16 tcgen05.mma (M=128, N=32, K=16) per chunk from one
@@ -46,7 +47,9 @@ constexpr int kStages = 2;
 constexpr int kMaxSeg = 16;                              // images one CTA's tiles may span
 constexpr int kProducers = 256;
 constexpr int kThreads = kProducers + 64;  // + MMA warp + staging-loader warp
-constexpr int kSmemFixed = kStages * kStageBytes + 1024 /*align*/ + 512 /*barriers, segment table*/;
+// + 256 bytes after the staging buffers: loads of padding columns (pad <= 64)
+// past the last staged row stay inside the CTA's shared memory
+constexpr int kSmemFixed = kStages * kStageBytes + 1024 /*align*/ + 512 /*barriers, segment table, zero block*/ + 256;
 
 template <bool BF16> struct OpT;
 template <> struct OpT<false> {
@@ -89,6 +92,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
     SegTable* seg = reinterpret_cast<SegTable*>(bars + 10);
     unsigned char* stg = smem + kStages * kStageBytes + 512;  // nbuf x 16 channels x stg_ch_bytes
+    unsigned char* zero = smem + kStages * kStageBytes + 496;  // 16 zero bytes: a padding row
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int n_blk = blockIdx.x % n_blocks;
@@ -108,6 +112,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         }
         mbar_init(tfull, 1);
         *abort_flag = 0;
+        *reinterpret_cast<uint4*>(zero) = make_uint4(0u, 0u, 0u, 0u);
         // images covered by this CTA's tiles and the input rows each needs
         const int na = p_first / tpi, nb = p_last / tpi;
         seg->nseg = nb - na + 1;
@@ -233,6 +238,9 @@ __global__ void __launch_bounds__(kThreads, 1)
             cv[i] = (x0 + i >= 0) && (x0 + i < W);
         }
         const long long row0 = static_cast<long long>(y0 - ylo) * W + x0;  // patch origin within the staged rows
+        uint32_t sel[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) sel[j] = cv[j] ? 0x5410u : 0x3232u;
 
         bool ok = true;
         for (int c = 0; c < c_chunks && ok; ++c) {
@@ -247,6 +255,59 @@ __global__ void __launch_bounds__(kThreads, 1)
             uint32_t pk[kElems][4];
 #pragma unroll
             for (int j2 = 0; j2 < 4; ++j2) {
+                if constexpr (!BF16) {
+                    // fp16 operands: the channel pair (jl, jl+1) is transformed
+                    // in packed fp16 (the F(2x3) B^T has only +-1 entries, so
+                    // this is two roundings of sums instead of one; the
+                    // reference's transforms are fp16 as well).  Padding rows
+                    // and channels past C read a zero block; padding columns
+                    // take the zero upper half of the 16-bit loads through the
+                    // byte-permute selector.
+                    const int jl = hsel * 8 + j2 * 2;
+                    const int ch = c * kChunk + jl;
+                    const bool v0 = ch < C, v1 = ch + 1 < C;
+                    const uintptr_t a0 = reinterpret_cast<uintptr_t>(
+                        x + (static_cast<long long>(n) * C + ch) * plane + static_cast<long long>(ylo) * W);
+                    const uintptr_t a1 = a0 + static_cast<uintptr_t>(plane) * 2;
+                    const uintptr_t rb = static_cast<uintptr_t>(yhi - ylo) * W * 2;
+                    if ((!v0 || a0 + rb <= lim) && (!v1 || a1 + rb <= lim)) {
+                        const __half* b0 =
+                            reinterpret_cast<const __half*>(buf + jl * stg_ch_bytes + soff + (a0 & 15)) + row0;
+                        const __half* b1 =
+                            reinterpret_cast<const __half*>(buf + (jl + 1) * stg_ch_bytes + soff + (a1 & 15)) + row0;
+                        __half2 t[4][4];
+#pragma unroll
+                        for (int i = 0; i < 4; ++i) {
+                            const uint16_t* r0 =
+                                reinterpret_cast<const uint16_t*>(rv[i] && v0 ? b0 + i * W : reinterpret_cast<const __half*>(zero));
+                            const uint16_t* r1 =
+                                reinterpret_cast<const uint16_t*>(rv[i] && v1 ? b1 + i * W : reinterpret_cast<const __half*>(zero));
+#pragma unroll
+                            for (int j = 0; j < 4; ++j) {
+                                const uint32_t h = __byte_perm(r0[j], r1[j], sel[j]);
+                                t[i][j] = *reinterpret_cast<const __half2*>(&h);
+                            }
+                        }
+                        // columns: B^T d
+#pragma unroll
+                        for (int j = 0; j < 4; ++j) {
+                            const __half2 d0 = t[0][j], d1 = t[1][j], d2 = t[2][j], d3 = t[3][j];
+                            t[0][j] = __hsub2(d0, d2);
+                            t[1][j] = __hadd2(d1, d2);
+                            t[2][j] = __hsub2(d2, d1);
+                            t[3][j] = __hsub2(d1, d3);
+                        }
+                        // rows: (B^T d) B
+#pragma unroll
+                        for (int i = 0; i < 4; ++i) {
+                            const __half2 q0 = t[i][0], q1 = t[i][1], q2 = t[i][2], q3 = t[i][3];
+                            const __half2 o[4] = {__hsub2(q0, q2), __hadd2(q1, q2), __hsub2(q2, q1), __hsub2(q1, q3)};
+#pragma unroll
+                            for (int j = 0; j < 4; ++j) pk[i * 4 + j][j2] = *reinterpret_cast<const uint32_t*>(&o[j]);
+                        }
+                        continue;
+                    }
+                }
                 float v[2][16];
 #pragma unroll
                 for (int h = 0; h < 2; ++h) {
