@@ -85,23 +85,28 @@ __global__ void __launch_bounds__(kThreads, 1)
     uint64_t* bars = reinterpret_cast<uint64_t*>(smem + kStages * kStageBytes);
     uint64_t* full = bars;             // [2] producers (256) + TMA expect_tx (1)
     uint64_t* empty = bars + 2;        // [2] MMA commit
-    uint64_t* tfull = bars + 4;        // accumulators ready
+    uint64_t* tfull = bars + 4;        // accumulators of the current item ready
     uint64_t* sfull = bars + 5;        // [2] staging copies landed
     uint64_t* sempty = bars + 7;       // [2] staging buffer read by all producers
-    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 9);
+    uint64_t* tempty = bars + 9;       // accumulators drained by the epilogue (256 arrivals)
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 10);
     volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
-    SegTable* seg = reinterpret_cast<SegTable*>(bars + 10);
+    SegTable* segs = reinterpret_cast<SegTable*>(bars + 11);  // [2], by item parity
+    static_assert(11 * 8 + 2 * sizeof(SegTable) <= 496, "barrier area");
     unsigned char* stg = smem + kStages * kStageBytes + 512;  // nbuf x 16 channels x stg_ch_bytes
     unsigned char* zero = smem + kStages * kStageBytes + 496;  // 16 zero bytes: a padding row
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int n_blk = blockIdx.x % n_blocks;
-    const int m_blk = blockIdx.x / n_blocks;
     const int tpi = tiles_h * tiles_w;
-    const int p_first = m_blk * kTilesPerCta;
-    const int p_last = min(P, p_first + kTilesPerCta) - 1;
     const long long plane = static_cast<long long>(H) * W;
     const uintptr_t lim = reinterpret_cast<uintptr_t>(x_end) & ~uintptr_t(15);
+    // persistent CTA: work items (tile block, 32-channel block) blockIdx.x,
+    // blockIdx.x + gridDim.x, ...; the output-channel block runs fastest so
+    // CTAs working at the same time read the same input rows (L2)
+    const int m_blocks = (P + kTilesPerCta - 1) / kTilesPerCta;
+    const int total_items = m_blocks * n_blocks;
+    const int my_items = blockIdx.x < total_items ? (total_items - 1 - blockIdx.x) / gridDim.x + 1 : 0;
+    const int total_chunks = my_items * c_chunks;
 
     if (tid == 0) {
         for (int i = 0; i < kStages; ++i) {
@@ -111,23 +116,9 @@ __global__ void __launch_bounds__(kThreads, 1)
             mbar_init(&sempty[i], kProducers);
         }
         mbar_init(tfull, 1);
+        mbar_init(tempty, kProducers);
         *abort_flag = 0;
         *reinterpret_cast<uint4*>(zero) = make_uint4(0u, 0u, 0u, 0u);
-        // images covered by this CTA's tiles and the input rows each needs
-        const int na = p_first / tpi, nb = p_last / tpi;
-        seg->nseg = nb - na + 1;
-        seg->n_first = na;
-        int off = 0;
-        for (int s = 0; s <= nb - na; ++s) {
-            const int n = na + s;
-            const int pa = max(p_first, n * tpi) - n * tpi, pb = min(p_last, n * tpi + tpi - 1) - n * tpi;
-            const int tha = pa / tiles_w, thb = pb / tiles_w;
-            const int ylo = max(0, tha * 2 - pad_h), yhi = min(H, thb * 2 - pad_h + 4);
-            seg->ylo[s] = ylo;
-            seg->yhi[s] = max(ylo, yhi);
-            seg->off[s] = off;
-            off += (max(0, yhi - ylo) * W * 2 + 16 + 15) / 16 * 16;
-        }
         fence_barrier_init();
     }
     pdl_wait();     // input written, earlier readers of the output done
@@ -137,228 +128,285 @@ __global__ void __launch_bounds__(kThreads, 1)
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem_base = *tmem_slot;
-    if (seg->nseg > kMaxSeg) {  // host sizing guarantees this never happens
-        if (tid == 0) record_error(err, ERR_SITE_CONFIG);
-        __syncthreads();
-        if (warp == 8) tmem_dealloc(tmem_base, 512);
-        return;
-    }
 
-    // staging of chunk `c` (16 channels) into buffer c % nbuf: loader lane j
-    // copies channel j's rows of every image segment and accounts its own
-    // bytes on the barrier (16 arrivals complete the phase)
-    auto issue_stage = [&](int c, int j) {
-        const int bsel = c % nbuf;
+    // images covered by an item's 128 tiles and the input rows each needs
+    auto make_seg = [&](int item, SegTable* sg) {
+        const int p_first = (item / n_blocks) * kTilesPerCta;
+        const int p_last = min(P, p_first + kTilesPerCta) - 1;
+        const int na = p_first / tpi, nb = p_last / tpi;
+        int nseg = nb - na + 1;
+        if (nseg > kMaxSeg) {  // host sizing guarantees this never happens
+            record_error(err, ERR_SITE_CONFIG);
+            *abort_flag = 1;
+            nseg = kMaxSeg;
+        }
+        sg->nseg = nseg;
+        sg->n_first = na;
+        int off = 0;
+        for (int q = 0; q < nseg; ++q) {
+            const int n = na + q;
+            const int pa = max(p_first, n * tpi) - n * tpi, pb = min(p_last, n * tpi + tpi - 1) - n * tpi;
+            const int tha = pa / tiles_w, thb = pb / tiles_w;
+            const int ylo = max(0, tha * 2 - pad_h), yhi = min(H, thb * 2 - pad_h + 4);
+            sg->ylo[q] = ylo;
+            sg->yhi[q] = max(ylo, yhi);
+            sg->off[q] = off;
+            off += (max(0, yhi - ylo) * W * 2 + 16 + 15) / 16 * 16;
+        }
+    };
+
+    // staging of chunk gc (the CTA's running chunk count: item gc / c_chunks,
+    // 16 channels from (gc % c_chunks) * 16) into buffer gc % nbuf: loader
+    // lane j copies channel j's rows of every image segment and accounts its
+    // own bytes on the barrier (16 arrivals complete the phase).  Lane 0
+    // writes the item's segment table before its first chunk.
+    auto issue_stage = [&](int gc, int j) {
+        const int k = gc / c_chunks, c = gc - k * c_chunks;
+        SegTable* sg = &segs[k & 1];
+        if (c == 0) {
+            if (j == 0) make_seg(blockIdx.x + k * gridDim.x, sg);
+            __syncwarp(0xffffu);
+        }
+        const int bsel = gc % nbuf;
         unsigned char* buf = stg + bsel * (kChunk * stg_ch_bytes) + j * stg_ch_bytes;
         const int ch = c * kChunk + j;
         uint32_t total = 0;
         uintptr_t a16s[kMaxSeg];
         uint32_t lens[kMaxSeg];
-        const int nseg = seg->nseg;
-        for (int s = 0; s < nseg; ++s) {
-            lens[s] = 0;
-            const int rows = seg->yhi[s] - seg->ylo[s];
+        const int nseg = sg->nseg;
+        for (int q = 0; q < nseg; ++q) {
+            lens[q] = 0;
+            const int rows = sg->yhi[q] - sg->ylo[q];
             if (ch >= C || rows <= 0) continue;
             const uintptr_t a = reinterpret_cast<uintptr_t>(
-                x + (static_cast<long long>(seg->n_first + s) * C + ch) * plane + static_cast<long long>(seg->ylo[s]) * W);
+                x + (static_cast<long long>(sg->n_first + q) * C + ch) * plane + static_cast<long long>(sg->ylo[q]) * W);
             const uintptr_t a16 = a & ~uintptr_t(15);
             const uintptr_t b16 = min_uptr((a + static_cast<uintptr_t>(rows) * W * 2 + 15) & ~uintptr_t(15), lim);
             if (b16 <= a16) continue;
-            a16s[s] = a16;
-            lens[s] = static_cast<uint32_t>(b16 - a16);
-            total += lens[s];
+            a16s[q] = a16;
+            lens[q] = static_cast<uint32_t>(b16 - a16);
+            total += lens[q];
         }
         mbar_arrive_expect_tx(&sfull[bsel], total);
-        for (int s = 0; s < nseg; ++s)
-            if (lens[s]) bulk_g2s(buf + seg->off[s], reinterpret_cast<const void*>(a16s[s]), lens[s], &sfull[bsel]);
+        for (int q = 0; q < nseg; ++q)
+            if (lens[q]) bulk_g2s(buf + sg->off[q], reinterpret_cast<const void*>(a16s[q]), lens[q], &sfull[bsel]);
     };
 
     if (warp == 9) {
         if (lane < kChunk) {
-            for (int c = 0; c < nbuf && c < c_chunks; ++c) issue_stage(c, lane);
-            for (int c = 0; c + nbuf < c_chunks; ++c) {
-                // buffer c % nbuf is free once every producer has read chunk c
-                if (!mbar_wait(&sempty[c % nbuf], (c / nbuf) & 1, abort_flag, err, ERR_SITE_EMPTY)) break;
-                issue_stage(c + nbuf, lane);
+            for (int gc = 0; gc < nbuf && gc < total_chunks; ++gc) issue_stage(gc, lane);
+            for (int gc = 0; gc + nbuf < total_chunks; ++gc) {
+                // buffer gc % nbuf is free once every producer has read chunk gc
+                if (!mbar_wait(&sempty[gc % nbuf], (gc / nbuf) & 1, abort_flag, err, ERR_SITE_EMPTY)) break;
+                issue_stage(gc + nbuf, lane);
             }
         }
     } else if (warp == 8) {
         if (lane == 0) {
             tma_prefetch_desc(&tmU);
-            auto issue_tma = [&](int chunk) {
-                const int s = chunk & 1;
+            auto issue_tma = [&](int gc) {
+                const int k = gc / c_chunks, c = gc - k * c_chunks;
+                const int n_blk = (blockIdx.x + k * gridDim.x) % n_blocks;
+                const int s = gc & 1;
                 mbar_arrive_expect_tx(&full[s], kBBytes);
-                tma_load_4d(smem + s * kStageBytes + kABytes, &tmU, &full[s], 0, n_blk * (kOcPerCta / 8), chunk * 2, 0);
+                tma_load_4d(smem + s * kStageBytes + kABytes, &tmU, &full[s], 0, n_blk * (kOcPerCta / 8), c * 2, 0);
             };
-            issue_tma(0);
-            if (c_chunks > 1) issue_tma(1);
-            for (int c = 0; c < c_chunks; ++c) {
-                const int s = c & 1;
-                if (!mbar_wait(&full[s], (c >> 1) & 1, abort_flag, err, ERR_SITE_FULL)) break;
+            if (total_chunks > 0) issue_tma(0);
+            if (total_chunks > 1) issue_tma(1);
+            bool ok = true;
+            for (int k = 0; k < my_items && ok; ++k) {
+                // the previous item's accumulators must be drained first
+                if (!mbar_wait(tempty, (k & 1) ^ 1, abort_flag, err, ERR_SITE_TMEM_EMPTY)) break;
                 tc_fence_after();
-                const uint32_t a_base = smem_u32(smem + s * kStageBytes);
-                const uint32_t b_base = a_base + kABytes;
+                for (int c = 0; c < c_chunks; ++c) {
+                    const int gc = k * c_chunks + c;
+                    const int s = gc & 1;
+                    if (!mbar_wait(&full[s], (gc >> 1) & 1, abort_flag, err, ERR_SITE_FULL)) {
+                        ok = false;
+                        break;
+                    }
+                    tc_fence_after();
+                    const uint32_t a_base = smem_u32(smem + s * kStageBytes);
+                    const uint32_t b_base = a_base + kABytes;
 #pragma unroll
-                for (int e = 0; e < kElems; ++e) {
-                    const uint64_t ad = make_smem_desc(a_base + e * (kTilesPerCta * 16), kAHalf, 128, Swz::None);
-                    const uint64_t bd = make_smem_desc(b_base + e * (2 * kOcPerCta * 16), kOcPerCta * 16, 128, Swz::None);
-                    tc_mma_f16(tmem_base + e * kOcPerCta, ad, bd, kIdesc, c > 0 ? 1u : 0u);
+                    for (int e = 0; e < kElems; ++e) {
+                        const uint64_t ad = make_smem_desc(a_base + e * (kTilesPerCta * 16), kAHalf, 128, Swz::None);
+                        const uint64_t bd =
+                            make_smem_desc(b_base + e * (2 * kOcPerCta * 16), kOcPerCta * 16, 128, Swz::None);
+                        tc_mma_f16(tmem_base + e * kOcPerCta, ad, bd, kIdesc, c > 0 ? 1u : 0u);
+                    }
+                    tc_commit(&empty[s]);
+                    if (gc + 2 < total_chunks) {
+                        // the filter tile of chunk gc+2 reuses this stage: issue it
+                        // as soon as these MMAs retire, a whole chunk ahead of its use
+                        if (!mbar_wait(&empty[s], (gc >> 1) & 1, abort_flag, err, ERR_SITE_EMPTY)) {
+                            ok = false;
+                            break;
+                        }
+                        issue_tma(gc + 2);
+                    }
                 }
-                tc_commit(&empty[s]);
-                if (c + 2 < c_chunks) {
-                    // the filter tile of chunk c+2 reuses this stage: issue it as
-                    // soon as these MMAs retire, a whole chunk ahead of its use
-                    if (!mbar_wait(&empty[s], (c >> 1) & 1, abort_flag, err, ERR_SITE_EMPTY)) break;
-                    issue_tma(c + 2);
-                }
+                if (ok && !*abort_flag) tc_commit(tfull);
             }
-            if (!*abort_flag) tc_commit(tfull);
         }
     } else {
         // ---- producers: one tile and 8 channels of every chunk per thread,
-        //      lanes over consecutive tiles
+        //      lanes over consecutive tiles; then the item's epilogue
         const int r = tid & 127;
         const int hsel = tid >> 7;
-        const int p = p_first + r;
-        const bool pvalid = p < P;
-        int n = 0, th = 0, tw = 0;
-        if (pvalid) {
-            n = p / tpi;
-            const int rem = p - n * tpi;
-            th = rem / tiles_w;
-            tw = rem - th * tiles_w;
-        }
-        const int s_idx = pvalid ? n - seg->n_first : 0;
-        const int ylo = seg->ylo[s_idx], yhi = seg->yhi[s_idx], soff = seg->off[s_idx];
-        const int y0 = th * 2 - pad_h, x0 = tw * 2 - pad_w;
-        bool rv[4], cv[4];
-#pragma unroll
-        for (int i = 0; i < 4; ++i) {
-            rv[i] = pvalid && (y0 + i >= ylo) && (y0 + i < yhi);
-            cv[i] = (x0 + i >= 0) && (x0 + i < W);
-        }
-        const long long row0 = static_cast<long long>(y0 - ylo) * W + x0;  // patch origin within the staged rows
-        uint32_t sel[4];
-#pragma unroll
-        for (int j = 0; j < 4; ++j) sel[j] = cv[j] ? 0x5410u : 0x3232u;
-
         bool ok = true;
-        for (int c = 0; c < c_chunks && ok; ++c) {
-            const int s = c & 1;
-            const int bsel = c % nbuf;
-            const uint32_t bpar = (c / nbuf) & 1;
-            if (!mbar_wait(&sfull[bsel], bpar, abort_flag, err, ERR_SITE_FULL)) {
-                ok = false;
-                break;
+        for (int k = 0; k < my_items && ok; ++k) {
+            const int item = blockIdx.x + k * gridDim.x;
+            const int n_blk = item % n_blocks;
+            const int p_first = (item / n_blocks) * kTilesPerCta;
+            const int p = p_first + r;
+            const bool pvalid = p < P;
+            int n = 0, th = 0, tw = 0;
+            if (pvalid) {
+                n = p / tpi;
+                const int rem = p - n * tpi;
+                th = rem / tiles_w;
+                tw = rem - th * tiles_w;
             }
-            const unsigned char* buf = stg + bsel * (kChunk * stg_ch_bytes);
-            uint32_t pk[kElems][4];
+            int ylo = 0, yhi = 0, soff = 0;
+            const int y0 = th * 2 - pad_h, x0 = tw * 2 - pad_w;
+            bool rv[4], cv[4];
+            uint32_t sel[4];
+            long long row0 = 0;
+            for (int c = 0; c < c_chunks; ++c) {
+                const int gc = k * c_chunks + c;
+                const int s = gc & 1;
+                const int bsel = gc % nbuf;
+                const uint32_t bpar = (gc / nbuf) & 1;
+                if (!mbar_wait(&sfull[bsel], bpar, abort_flag, err, ERR_SITE_FULL)) {
+                    ok = false;
+                    break;
+                }
+                if (c == 0) {
+                    // the item's segment table arrived with its first chunk
+                    const SegTable* sg = &segs[k & 1];
+                    const int s_idx = pvalid ? n - sg->n_first : 0;
+                    ylo = sg->ylo[s_idx];
+                    yhi = sg->yhi[s_idx];
+                    soff = sg->off[s_idx];
 #pragma unroll
-            for (int j2 = 0; j2 < 4; ++j2) {
-                if constexpr (!BF16) {
-                    // fp16 operands: the channel pair (jl, jl+1) is transformed
-                    // in packed fp16 (the F(2x3) B^T has only +-1 entries, so
-                    // this is two roundings of sums instead of one; the
-                    // reference's transforms are fp16 as well).  Padding rows
-                    // and channels past C read a zero block; padding columns
-                    // take the zero upper half of the 16-bit loads through the
-                    // byte-permute selector.
-                    const int jl = hsel * 8 + j2 * 2;
-                    const int ch = c * kChunk + jl;
-                    const bool v0 = ch < C, v1 = ch + 1 < C;
-                    const uintptr_t a0 = reinterpret_cast<uintptr_t>(
-                        x + (static_cast<long long>(n) * C + ch) * plane + static_cast<long long>(ylo) * W);
-                    const uintptr_t a1 = a0 + static_cast<uintptr_t>(plane) * 2;
-                    const uintptr_t rb = static_cast<uintptr_t>(yhi - ylo) * W * 2;
-                    if ((!v0 || a0 + rb <= lim) && (!v1 || a1 + rb <= lim)) {
-                        const __half* b0 =
-                            reinterpret_cast<const __half*>(buf + jl * stg_ch_bytes + soff + (a0 & 15)) + row0;
-                        const __half* b1 =
-                            reinterpret_cast<const __half*>(buf + (jl + 1) * stg_ch_bytes + soff + (a1 & 15)) + row0;
-                        __half2 t[4][4];
+                    for (int i = 0; i < 4; ++i) {
+                        rv[i] = pvalid && (y0 + i >= ylo) && (y0 + i < yhi);
+                        cv[i] = (x0 + i >= 0) && (x0 + i < W);
+                        sel[i] = cv[i] ? 0x5410u : 0x3232u;
+                    }
+                    row0 = static_cast<long long>(y0 - ylo) * W + x0;  // patch origin within the staged rows
+                }
+                const unsigned char* buf = stg + bsel * (kChunk * stg_ch_bytes);
+                uint32_t pk[kElems][4];
 #pragma unroll
-                        for (int i = 0; i < 4; ++i) {
-                            const uint16_t* r0 =
-                                reinterpret_cast<const uint16_t*>(rv[i] && v0 ? b0 + i * W : reinterpret_cast<const __half*>(zero));
-                            const uint16_t* r1 =
-                                reinterpret_cast<const uint16_t*>(rv[i] && v1 ? b1 + i * W : reinterpret_cast<const __half*>(zero));
+                for (int j2 = 0; j2 < 4; ++j2) {
+                    if constexpr (!BF16) {
+                        // fp16 operands: the channel pair (jl, jl+1) is transformed
+                        // in packed fp16 (the F(2x3) B^T has only +-1 entries, so
+                        // this is two roundings of sums instead of one; the
+                        // reference's transforms are fp16 as well).  Padding rows
+                        // and channels past C read a zero block; padding columns
+                        // take the zero upper half of the 16-bit loads through the
+                        // byte-permute selector.
+                        const int jl = hsel * 8 + j2 * 2;
+                        const int ch = c * kChunk + jl;
+                        const bool v0 = ch < C, v1 = ch + 1 < C;
+                        const uintptr_t a0 = reinterpret_cast<uintptr_t>(
+                            x + (static_cast<long long>(n) * C + ch) * plane + static_cast<long long>(ylo) * W);
+                        const uintptr_t a1 = a0 + static_cast<uintptr_t>(plane) * 2;
+                        const uintptr_t rb = static_cast<uintptr_t>(yhi - ylo) * W * 2;
+                        if ((!v0 || a0 + rb <= lim) && (!v1 || a1 + rb <= lim)) {
+                            const __half* b0 =
+                                reinterpret_cast<const __half*>(buf + jl * stg_ch_bytes + soff + (a0 & 15)) + row0;
+                            const __half* b1 =
+                                reinterpret_cast<const __half*>(buf + (jl + 1) * stg_ch_bytes + soff + (a1 & 15)) + row0;
+                            __half2 t[4][4];
+#pragma unroll
+                            for (int i = 0; i < 4; ++i) {
+                                const uint16_t* r0 =
+                                    reinterpret_cast<const uint16_t*>(rv[i] && v0 ? b0 + i * W : reinterpret_cast<const __half*>(zero));
+                                const uint16_t* r1 =
+                                    reinterpret_cast<const uint16_t*>(rv[i] && v1 ? b1 + i * W : reinterpret_cast<const __half*>(zero));
+#pragma unroll
+                                for (int j = 0; j < 4; ++j) {
+                                    const uint32_t h = __byte_perm(r0[j], r1[j], sel[j]);
+                                    t[i][j] = *reinterpret_cast<const __half2*>(&h);
+                                }
+                            }
+                            // columns: B^T d
 #pragma unroll
                             for (int j = 0; j < 4; ++j) {
-                                const uint32_t h = __byte_perm(r0[j], r1[j], sel[j]);
-                                t[i][j] = *reinterpret_cast<const __half2*>(&h);
+                                const __half2 d0 = t[0][j], d1 = t[1][j], d2 = t[2][j], d3 = t[3][j];
+                                t[0][j] = __hsub2(d0, d2);
+                                t[1][j] = __hadd2(d1, d2);
+                                t[2][j] = __hsub2(d2, d1);
+                                t[3][j] = __hsub2(d1, d3);
                             }
-                        }
-                        // columns: B^T d
+                            // rows: (B^T d) B
 #pragma unroll
-                        for (int j = 0; j < 4; ++j) {
-                            const __half2 d0 = t[0][j], d1 = t[1][j], d2 = t[2][j], d3 = t[3][j];
-                            t[0][j] = __hsub2(d0, d2);
-                            t[1][j] = __hadd2(d1, d2);
-                            t[2][j] = __hsub2(d2, d1);
-                            t[3][j] = __hsub2(d1, d3);
-                        }
-                        // rows: (B^T d) B
+                            for (int i = 0; i < 4; ++i) {
+                                const __half2 q0 = t[i][0], q1 = t[i][1], q2 = t[i][2], q3 = t[i][3];
+                                const __half2 o[4] = {__hsub2(q0, q2), __hadd2(q1, q2), __hsub2(q2, q1), __hsub2(q1, q3)};
 #pragma unroll
-                        for (int i = 0; i < 4; ++i) {
-                            const __half2 q0 = t[i][0], q1 = t[i][1], q2 = t[i][2], q3 = t[i][3];
-                            const __half2 o[4] = {__hsub2(q0, q2), __hadd2(q1, q2), __hsub2(q2, q1), __hsub2(q1, q3)};
-#pragma unroll
-                            for (int j = 0; j < 4; ++j) pk[i * 4 + j][j2] = *reinterpret_cast<const uint32_t*>(&o[j]);
+                                for (int j = 0; j < 4; ++j) pk[i * 4 + j][j2] = *reinterpret_cast<const uint32_t*>(&o[j]);
+                            }
+                            continue;
                         }
-                        continue;
                     }
-                }
-                float v[2][16];
+                    float v[2][16];
 #pragma unroll
-                for (int h = 0; h < 2; ++h) {
-                    const int jl = hsel * 8 + j2 * 2 + h;
-                    const int ch = c * kChunk + jl;
-                    const bool chv = ch < C;
-                    const __half* gsrc = x + (static_cast<long long>(n) * C + ch) * plane;
-                    const uintptr_t a = reinterpret_cast<uintptr_t>(gsrc + static_cast<long long>(ylo) * W);
-                    // rows staged whole unless they run into the input's last
-                    // partial 16-byte block (then read from global memory)
-                    const bool staged = a + static_cast<uintptr_t>(yhi - ylo) * W * 2 <= lim;
-                    float d[16];
-                    // staged rows through shared-memory loads; the rare rows
-                    // that run into the input's last partial 16-byte block
-                    // through global loads (separate code, not one pointer)
-                    if (staged) {
-                        const __half* src =
-                            reinterpret_cast<const __half*>(buf + jl * stg_ch_bytes + soff + (a & 15)) + row0;
+                    for (int h = 0; h < 2; ++h) {
+                        const int jl = hsel * 8 + j2 * 2 + h;
+                        const int ch = c * kChunk + jl;
+                        const bool chv = ch < C;
+                        const __half* gsrc = x + (static_cast<long long>(n) * C + ch) * plane;
+                        const uintptr_t a = reinterpret_cast<uintptr_t>(gsrc + static_cast<long long>(ylo) * W);
+                        // rows staged whole unless they run into the input's last
+                        // partial 16-byte block (then read from global memory)
+                        const bool staged = a + static_cast<uintptr_t>(yhi - ylo) * W * 2 <= lim;
+                        float d[16];
+                        // staged rows through shared-memory loads; the rare rows
+                        // that run into the input's last partial 16-byte block
+                        // through global loads (separate code, not one pointer)
+                        if (staged) {
+                            const __half* src =
+                                reinterpret_cast<const __half*>(buf + jl * stg_ch_bytes + soff + (a & 15)) + row0;
 #pragma unroll
-                        for (int i = 0; i < 4; ++i)
+                            for (int i = 0; i < 4; ++i)
 #pragma unroll
-                            for (int j = 0; j < 4; ++j)
-                                d[i * 4 + j] = (chv && rv[i] && cv[j]) ? __half2float(src[i * W + j]) : 0.f;
-                    } else {
-                        const __half* src = gsrc + static_cast<long long>(ylo) * W + row0;
+                                for (int j = 0; j < 4; ++j)
+                                    d[i * 4 + j] = (chv && rv[i] && cv[j]) ? __half2float(src[i * W + j]) : 0.f;
+                        } else {
+                            const __half* src = gsrc + static_cast<long long>(ylo) * W + row0;
 #pragma unroll
-                        for (int i = 0; i < 4; ++i)
+                            for (int i = 0; i < 4; ++i)
 #pragma unroll
-                            for (int j = 0; j < 4; ++j)
-                                d[i * 4 + j] = (chv && rv[i] && cv[j]) ? __half2float(src[i * W + j]) : 0.f;
+                                for (int j = 0; j < 4; ++j)
+                                    d[i * 4 + j] = (chv && rv[i] && cv[j]) ? __half2float(src[i * W + j]) : 0.f;
+                        }
+                        input_tile_transform<F2>(d, v[h]);
                     }
-                    input_tile_transform<F2>(d, v[h]);
+#pragma unroll
+                    for (int e = 0; e < kElems; ++e) pk[e][j2] = OpT<BF16>::pack(v[0][e], v[1][e]);
                 }
+                mbar_arrive(&sempty[bsel]);  // this thread is done reading the staged rows
+                if (!mbar_wait(&empty[s], ((gc >> 1) & 1) ^ 1, abort_flag, err, ERR_SITE_EMPTY)) {
+                    ok = false;
+                    break;
+                }
+                unsigned char* a = smem + s * kStageBytes + hsel * kAHalf + r * 16;
 #pragma unroll
-                for (int e = 0; e < kElems; ++e) pk[e][j2] = OpT<BF16>::pack(v[0][e], v[1][e]);
+                for (int e = 0; e < kElems; ++e)
+                    *reinterpret_cast<uint4*>(a + e * (kTilesPerCta * 16)) =
+                        make_uint4(pk[e][0], pk[e][1], pk[e][2], pk[e][3]);
+                fence_proxy_async_smem();
+                mbar_arrive(&full[s]);
             }
-            mbar_arrive(&sempty[bsel]);  // this thread is done reading the staged rows
-            if (!mbar_wait(&empty[s], ((c >> 1) & 1) ^ 1, abort_flag, err, ERR_SITE_EMPTY)) {
-                ok = false;
-                break;
-            }
-            unsigned char* a = smem + s * kStageBytes + hsel * kAHalf + r * 16;
-#pragma unroll
-            for (int e = 0; e < kElems; ++e)
-                *reinterpret_cast<uint4*>(a + e * (kTilesPerCta * 16)) = make_uint4(pk[e][0], pk[e][1], pk[e][2], pk[e][3]);
-            fence_proxy_async_smem();
-            mbar_arrive(&full[s]);
-        }
+            if (!ok) break;
 
-        // ---- epilogue: A^T m A from TMEM
-        if (ok && mbar_wait(tfull, 0, abort_flag, err, ERR_SITE_TMEM_FULL)) {
+            // ---- epilogue: A^T m A from TMEM
+            if (!mbar_wait(tfull, k & 1, abort_flag, err, ERR_SITE_TMEM_FULL)) break;
             tc_fence_after();
             const int quarter = warp & 3;
             const int chalf = warp >> 2;
@@ -418,6 +466,7 @@ __global__ void __launch_bounds__(kThreads, 1)
                 }
             }
             tc_fence_before();
+            mbar_arrive(tempty);
         }
     }
 
@@ -494,9 +543,15 @@ cudaError_t plan_fused2x3(FusedPlan& fp, OpType op, const Geom& g, const void* U
 cudaError_t launch_fused2x3(const FusedPlan& fp, const Geom& g, const void* x, const void* x_end, void* out,
                             DevErr* err, cudaStream_t stream) {
     if (g.P > 0x7fffffffLL) return cudaErrorInvalidValue;
-    // tile blocks of this launch (a launch may cover a subset of the images)
-    const long long blocks = (g.P + kTilesPerCta - 1) / kTilesPerCta * fp.n_blocks;
-    if (blocks > 0x7fffffffLL) return cudaErrorInvalidValue;
+    // work items of this launch (a launch may cover a subset of the images),
+    // one persistent CTA per SM
+    const long long items = (g.P + kTilesPerCta - 1) / kTilesPerCta * fp.n_blocks;
+    if (items > 0x7fffffffLL) return cudaErrorInvalidValue;
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+        sms <= 0)
+        sms = 148;
+    const long long blocks = std::min<long long>(items, sms);
     auto kern = fp.op == OpType::BF16 ? fused2x3_kernel<true> : fused2x3_kernel<false>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, fp.smem_bytes);
     if (e != cudaSuccess) return e;
