@@ -54,6 +54,10 @@ EXPORTS = [
     "conv2d_server_config_default", "conv2d_server_create", "conv2d_server_add_layer", "conv2d_server_submit",
     "conv2d_server_poll", "conv2d_server_wait_all", "conv2d_server_replay", "conv2d_server_stats",
     "conv2d_server_destroy",
+    "conv2d_plan_save",
+    "conv2d_plan_load",
+    "conv2d_server_save_layers",
+    "conv2d_server_load_layers",
 ]
 
 _lib = None
@@ -124,6 +128,10 @@ def lib():
                                            ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
         L.conv2d_server_stats.argtypes = [vp, vp]
         L.conv2d_server_destroy.argtypes = [vp]
+        L.conv2d_plan_save.argtypes = [vp, ctypes.c_char_p]
+        L.conv2d_plan_load.argtypes = [vp, ctypes.c_char_p]
+        L.conv2d_server_save_layers.argtypes = [vp, ctypes.c_char_p]
+        L.conv2d_server_load_layers.argtypes = [vp, ctypes.c_char_p, ip, ip]
         _lib = L
     return _lib
 
@@ -190,6 +198,14 @@ class Conv2d:
             return ["fused2x3"]
         per = (["tile_scale"] if self.scaling else []) + ["input_transform", "gemm_tcgen05", "output_transform"]
         return per * (self.launches_per_call // len(per))
+
+    def save(self, path: str):
+        """Write the transformed filter (and what it was made for) to a file."""
+        _check(lib().conv2d_plan_save(self.ptr, os.fsencode(path)))
+
+    def load(self, path: str):
+        """Use a saved transformed filter instead of transforming the weights."""
+        _check(lib().conv2d_plan_load(self.ptr, os.fsencode(path)))
 
     def refresh_filter(self, stream: int | None = None):
         _check(lib().conv2d_refresh_filter(self.ptr, ctypes.c_void_p(stream or 0)))
@@ -274,6 +290,15 @@ class Server:
         _check(lib().conv2d_server_add_layer(self.handle, c, k, h, w, p, q, ctypes.c_void_p(weight_ptr),
                                              ctypes.byref(idx)))
         return idx.value
+
+    def save_layers(self, path: str):
+        _check(lib().conv2d_server_save_layers(self.handle, os.fsencode(path)))
+
+    def load_layers(self, path: str):
+        """Register the layers of a saved file; returns their indices."""
+        first, count = ctypes.c_int(-1), ctypes.c_int(0)
+        _check(lib().conv2d_server_load_layers(self.handle, os.fsencode(path), ctypes.byref(first), ctypes.byref(count)))
+        return list(range(first.value, first.value + count.value))
 
     def submit(self, layer, n, in_ptr, out_ptr):
         rid = ctypes.c_longlong()

@@ -23,6 +23,7 @@
 #include <atomic>
 #include <chrono>
 #include <condition_variable>
+#include <cstdio>
 #include <cstring>
 #include <deque>
 #include <map>
@@ -512,6 +513,111 @@ int conv2d_server_stats(conv2d_server_t* server, conv2d_server_stats_t* st) {
     st->max_inflight_batches = sv->max_inflight;
     st->arena_used_bytes = static_cast<long long>(sv->arena.used());
     st->flops = sv->flops_done;
+    return CONV2D_OK;
+}
+
+// ---- resident layers to and from a file (warm restart) ----------------------
+// magic "WGCSRVL1", version, layer count; per layer its geometry, the byte
+// counts of its F(2x3) and F(4x3) filters and an FNV-1a checksum of both;
+// then the filters as they lie in device memory (U[E][Cp/8][Kp][8], fp16).
+
+namespace {
+
+constexpr char kServerMagic[8] = {'W', 'G', 'C', 'S', 'R', 'V', 'L', '1'};
+
+struct LayerRecord {
+    uint32_t c, k, h, w, p, q;
+    uint64_t b2, b4, checksum;
+};
+
+uint64_t fnv1a64(const unsigned char* p, size_t n, uint64_t h = 1469598103934665603ull) {
+    for (size_t i = 0; i < n; ++i) {
+        h ^= p[i];
+        h *= 1099511628211ull;
+    }
+    return h;
+}
+
+}  // namespace
+
+int conv2d_server_save_layers(conv2d_server_t* server, const char* path) {
+    Server* sv = reinterpret_cast<Server*>(server);
+    if (!sv || !path) return set_last_error(CONV2D_ERR_INVALID, "null argument");
+    std::vector<Layer> layers;
+    {
+        std::lock_guard<std::mutex> lk(sv->mu);
+        layers = sv->layers;
+    }
+    std::vector<LayerRecord> recs;
+    std::vector<std::vector<unsigned char>> data;
+    for (const Layer& L : layers) {
+        const uint64_t cp = (L.c + 7) / 8 * 8, kp = (L.k + 7) / 8 * 8;
+        LayerRecord r{L.c, L.k, L.h, L.w, L.p, L.q, 16 * kp * cp * 2, 36 * kp * cp * 2, 0};
+        std::vector<unsigned char> buf(r.b2 + r.b4);
+        if (cudaMemcpy(buf.data(), L.U2, r.b2, cudaMemcpyDeviceToHost) != cudaSuccess ||
+            cudaMemcpy(buf.data() + r.b2, L.U4, r.b4, cudaMemcpyDeviceToHost) != cudaSuccess)
+            return set_last_error(CONV2D_ERR_CUDA, "copy of a resident filter failed");
+        r.checksum = fnv1a64(buf.data(), buf.size());
+        recs.push_back(r);
+        data.push_back(std::move(buf));
+    }
+    FILE* f = std::fopen(path, "wb");
+    if (!f) return set_last_error(CONV2D_ERR_INVALID, "cannot open the layer file for writing");
+    const uint32_t version = 1, count = static_cast<uint32_t>(recs.size());
+    bool ok = std::fwrite(kServerMagic, 8, 1, f) == 1 && std::fwrite(&version, 4, 1, f) == 1 &&
+              std::fwrite(&count, 4, 1, f) == 1 &&
+              (recs.empty() || std::fwrite(recs.data(), sizeof(LayerRecord), recs.size(), f) == recs.size());
+    for (const auto& d : data) ok = ok && std::fwrite(d.data(), 1, d.size(), f) == d.size();
+    if (std::fclose(f) != 0 || !ok) return set_last_error(CONV2D_ERR_INVALID, "layer file write failed");
+    return CONV2D_OK;
+}
+
+int conv2d_server_load_layers(conv2d_server_t* server, const char* path, int* first_layer, int* count) {
+    Server* sv = reinterpret_cast<Server*>(server);
+    if (!sv || !path) return set_last_error(CONV2D_ERR_INVALID, "null argument");
+    FILE* f = std::fopen(path, "rb");
+    if (!f) return set_last_error(CONV2D_ERR_INVALID, "cannot open the layer file");
+    char magic[8];
+    uint32_t version = 0, n = 0;
+    bool ok = std::fread(magic, 8, 1, f) == 1 && std::fread(&version, 4, 1, f) == 1 && std::fread(&n, 4, 1, f) == 1 &&
+              std::memcmp(magic, kServerMagic, 8) == 0 && version == 1 && n < (1u << 20);
+    std::vector<LayerRecord> recs(ok ? n : 0);
+    if (ok && n) ok = std::fread(recs.data(), sizeof(LayerRecord), n, f) == n;
+    std::vector<std::vector<unsigned char>> data;
+    for (uint32_t i = 0; ok && i < n; ++i) {
+        const LayerRecord& r = recs[i];
+        const uint64_t cp = (r.c + 7) / 8 * 8, kp = (r.k + 7) / 8 * 8;
+        problem_t pr{reinterpret_cast<void*>(16), reinterpret_cast<void*>(16), reinterpret_cast<void*>(16), 1, r.c, r.h,
+                     r.w, r.k, 3, 3, 1, 1, r.p, r.q};
+        if (validate_problem(&pr) != CONV2D_OK || r.b2 != 16 * kp * cp * 2 || r.b4 != 36 * kp * cp * 2) {
+            ok = false;
+            break;
+        }
+        std::vector<unsigned char> buf(r.b2 + r.b4);
+        ok = std::fread(buf.data(), 1, buf.size(), f) == buf.size() && fnv1a64(buf.data(), buf.size()) == r.checksum;
+        data.push_back(std::move(buf));
+    }
+    std::fclose(f);
+    if (!ok) return set_last_error(CONV2D_ERR_INVALID, "not a valid layer file (magic, version, sizes or checksum)");
+    int first = -1;
+    for (uint32_t i = 0; i < n; ++i) {
+        const LayerRecord& r = recs[i];
+        void* blk = nullptr;
+        if (cudaMalloc(&blk, r.b2 + r.b4) != cudaSuccess) return set_last_error(CONV2D_ERR_NOMEM, "filter allocation failed");
+        if (cudaMemcpy(blk, data[i].data(), r.b2 + r.b4, cudaMemcpyHostToDevice) != cudaSuccess) {
+            cudaFree(blk);
+            return set_last_error(CONV2D_ERR_CUDA, "copy of a resident filter failed");
+        }
+        Layer L{r.c, r.k, r.h, r.w, r.p, r.q};
+        L.U2 = blk;
+        L.U4 = static_cast<char*>(blk) + r.b2;
+        std::lock_guard<std::mutex> lk(sv->mu);
+        sv->u_blocks.push_back(blk);
+        sv->layers.push_back(L);
+        if (first < 0) first = static_cast<int>(sv->layers.size()) - 1;
+    }
+    if (first_layer) *first_layer = first;
+    if (count) *count = static_cast<int>(n);
     return CONV2D_OK;
 }
 

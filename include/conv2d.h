@@ -233,6 +233,22 @@ int conv2d_server_replay(conv2d_server_t* server, int count, const int* layer, c
 int conv2d_server_stats(conv2d_server_t* server, conv2d_server_stats_t* stats);
 int conv2d_server_destroy(conv2d_server_t* server);
 
+/* ---- Persistence (no counterpart in the reference, which transforms the
+ * filter on every call) ----------------------------------------------------
+ * A plan's Winograd-domain filter U, with the layer (C, K, padding),
+ * transform and operand type it was made for and a checksum, written to a
+ * file; loading it into a plan of the same layer skips the filter transform
+ * (a restarted process pairs this with WG_CONV2D_TUNE_FILE for the autotuner's
+ * choices).  Load fails with CONV2D_ERR_INVALID when the file was made for
+ * another layer, transform or operand type, or is damaged. */
+int conv2d_plan_save(const void* param, const char* path);
+int conv2d_plan_load(const void* param, const char* path);
+/* A server's resident layers (both transformed filters of each) to a file,
+ * and back into a server: the loaded layers get indices first_layer ..
+ * first_layer + count - 1, in the saved order. */
+int conv2d_server_save_layers(conv2d_server_t* server, const char* path);
+int conv2d_server_load_layers(conv2d_server_t* server, const char* path, int* first_layer, int* count);
+
 /* One call with a CUDA event recorded on the stream after every kernel
  * launch; waits, writes each launch's duration (ms, launch order) to
  * kernel_ms and returns the number of launches (negative status on error). */
