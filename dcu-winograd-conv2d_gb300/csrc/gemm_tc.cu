@@ -6,16 +6,17 @@
 // src/winograd_4x3_non_fused.cpp:587-597; kernels in include/hep_sgemm.h) with
 // the operands stored K-major.
 //
-// Design (one persistent CTA per SM, 192 threads):
+// Design (one persistent CTA per SM, 320 threads):
 //   warp 0      TMA producer: 128 tiles x 64 channels of V plus BN x 64 of U
 //               per stage, as 4-D boxes of 8 granules that land in the
 //               canonical no-swizzle K-major layout; S-stage mbarrier ring;
 //   warp 1      allocates TMEM and issues tcgen05.mma (M=128, N=BN, K=16)
 //               from one thread; accumulators double-buffered in TMEM so the
 //               epilogue of one output tile overlaps the main loop of the next;
-//   warps 2-5   epilogue: tcgen05.ld 32 lanes x 32 columns (the next chunk's
-//               load in flight while this one is stored), convert, 16-byte
-//               granule stores of M (a warp writes 512 contiguous bytes).
+//   warps 2-9   epilogue (two warps per TMEM lane quarter, each half of the
+//               columns when BN >= 64): tcgen05.ld 32 lanes x 32 columns (the
+//               next chunk's load in flight while this one is stored), convert,
+//               16-byte granule stores of M (a warp writes 512 contiguous bytes).
 // Work items are (problem, e, 128-tile block, BN-channel block), handed out
 // round robin over one global index; a grouped launch covers many problems
 // (each with its own tensor maps, sizes and output) in one persistent grid.
@@ -103,11 +104,14 @@ __device__ __forceinline__ Item locate(const GemmDesc* __restrict__ descs, int n
     return it;
 }
 
+constexpr int kGemmThreads = 320;  // TMA warp, MMA warp, 8 epilogue warps
+
 template <int BN, bool BF16, class MT>
 __device__ __forceinline__ void gemm_body(const GemmDesc* __restrict__ descs, int ndesc, long long total_tiles,
                                           DevErr* err) {
     using Cfg = GemmCfg<BN>;
     constexpr int S = Cfg::kStages;
+    constexpr int kEpiHalves = BN >= 64 ? 2 : 1;  // epilogue warps per TMEM lane quarter
     constexpr uint32_t kIdesc = make_idesc_f16(kBM, BN, BF16);
 
     extern __shared__ __align__(1024) unsigned char smem_raw[];
@@ -133,7 +137,7 @@ __device__ __forceinline__ void gemm_body(const GemmDesc* __restrict__ descs, in
         }
         for (int i = 0; i < 2; ++i) {
             mbar_init(&tfull[i], 1);
-            mbar_init(&tempty[i], 128);
+            mbar_init(&tempty[i], 128 * kEpiHalves);
         }
         *abort_flag = 0;
         fence_barrier_init();
@@ -219,9 +223,11 @@ __device__ __forceinline__ void gemm_body(const GemmDesc* __restrict__ descs, in
                 }
             }
         }
-    } else {
-        // epilogue warps 2..5: TMEM lane quarter = warp % 4
+    } else if (warp - 2 < 4 * kEpiHalves) {
+        // epilogue warps 2..9: TMEM lane quarter = warp % 4; warps 2-5 store
+        // the first half of the accumulator columns, 6-9 the second (BN >= 64)
         const int quarter = warp & 3;
+        const int half = (warp - 2) >> 2;
         const int row = quarter * 32 + lane;
         int acc = 0;
         uint32_t acc_phase = 0;
@@ -235,17 +241,19 @@ __device__ __forceinline__ void gemm_body(const GemmDesc* __restrict__ descs, in
             if (!mbar_wait(&tfull[acc], acc_phase, abort_flag, err, ERR_SITE_TMEM_FULL)) break;
             tc_fence_after();
             const long long p = static_cast<long long>(it.mb) * kBM + row;
-            const uint32_t taddr = tmem_base + (static_cast<uint32_t>(quarter * 32) << 16) + static_cast<uint32_t>(acc * BN);
+            const int col0 = half * (BN / kEpiHalves);
+            const uint32_t taddr = tmem_base + (static_cast<uint32_t>(quarter * 32) << 16) +
+                                   static_cast<uint32_t>(acc * BN + col0);
             // 32 columns per load; the load of chunk i+1 is in flight while
             // chunk i is stored
-            constexpr int kChunks = BN / 32;
+            constexpr int kChunks = BN / 32 / kEpiHalves;
             uint32_t r[2][32];
             tmem_ld_x32(taddr, r[0]);
             tc_wait_ld(r[0]);
 #pragma unroll
             for (int ch = 0; ch < kChunks; ++ch) {
                 if (ch + 1 < kChunks) tmem_ld_x32(taddr + (ch + 1) * 32, r[(ch + 1) & 1]);
-                if (p < P) store32<MT>(Mw, r[ch & 1], P, p, it.nb * BN + ch * 32, kg_count, it.e);
+                if (p < P) store32<MT>(Mw, r[ch & 1], P, p, it.nb * BN + col0 + ch * 32, kg_count, it.e);
                 if (ch + 1 < kChunks) tc_wait_ld(r[(ch + 1) & 1]);
             }
             tc_fence_before();
@@ -271,12 +279,12 @@ __device__ __forceinline__ void gemm_body(const GemmDesc* __restrict__ descs, in
 }
 
 template <int BN, bool BF16, class MT>
-__global__ void __launch_bounds__(192, 1) wino_gemm_kernel(const __grid_constant__ GemmDesc d, DevErr* err) {
+__global__ void __launch_bounds__(kGemmThreads, 1) wino_gemm_kernel(const __grid_constant__ GemmDesc d, DevErr* err) {
     gemm_body<BN, BF16, MT>(&d, 1, d.tiles, err);
 }
 
 template <int BN, bool BF16, class MT>
-__global__ void __launch_bounds__(192, 1)
+__global__ void __launch_bounds__(kGemmThreads, 1)
     wino_gemm_grouped(const GemmDesc* __restrict__ descs, int ndesc, long long total_tiles, DevErr* err) {
     gemm_body<BN, BF16, MT>(descs, ndesc, total_tiles, err);
 }
@@ -286,7 +294,7 @@ cudaError_t gemm_launch(const GemmDesc& d, int grid, DevErr* err, cudaStream_t s
     auto kern = wino_gemm_kernel<BN, BF16, MT>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, GemmCfg<BN>::kSmem);
     if (e != cudaSuccess) return e;
-    return launch_pdl(kern, dim3(grid), dim3(192), GemmCfg<BN>::kSmem, s, d, err);
+    return launch_pdl(kern, dim3(grid), dim3(kGemmThreads), GemmCfg<BN>::kSmem, s, d, err);
 }
 
 template <int BN, bool BF16, class MT>
@@ -295,7 +303,7 @@ cudaError_t gemm_grouped_launch(const GemmDesc* descs, int ndesc, long long tota
     auto kern = wino_gemm_grouped<BN, BF16, MT>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, GemmCfg<BN>::kSmem);
     if (e != cudaSuccess) return e;
-    return launch_pdl(kern, dim3(grid), dim3(192), GemmCfg<BN>::kSmem, s, descs, ndesc, total, err);
+    return launch_pdl(kern, dim3(grid), dim3(kGemmThreads), GemmCfg<BN>::kSmem, s, descs, ndesc, total, err);
 }
 
 // One template instance per (BN, operand type, M type); `single` selects the
