@@ -38,7 +38,7 @@ class Options(ctypes.Structure):
     """conv2d_options_t."""
     _fields_ = [("algo", ctypes.c_int), ("operand_bf16", ctypes.c_int), ("tile_scaling", ctypes.c_int),
                 ("f4_points", ctypes.c_int), ("filter_policy", ctypes.c_int), ("gemm_bn", ctypes.c_int),
-                ("l2_chunk_bytes", ctypes.c_longlong), ("reserved", ctypes.c_int * 4)]
+                ("l2_chunk_bytes", ctypes.c_longlong), ("io_bf16", ctypes.c_int), ("reserved", ctypes.c_int * 3)]
 
 
 # every symbol include/conv2d.h declares
@@ -171,7 +171,7 @@ class Conv2d:
                                       ctypes.byref(options)))
         self._alive = True
         opts = options if options is not None else default_options()
-        self.scaling = bool(opts.tile_scaling) and self.algo == ALGO_4X3
+        self.scaling = bool(opts.tile_scaling or opts.io_bf16) and self.algo == ALGO_4X3
 
     @property
     def ptr(self):
@@ -395,16 +395,20 @@ def copy_to_host(host_ptr: int, dev_ptr: int, nbytes: int):
 # ---- torch convenience (tests / benchmark) ------------------------------------
 
 def conv2d_torch(x, w, p=1, q=1, options: Options | None = None, stream=None):
-    """Run the operator on CUDA fp16 tensors x [N,C,H,W], w [K,C,3,3]; returns
-    (output tensor, Conv2d handle)."""
+    """Run the operator on CUDA tensors x [N,C,H,W], w [K,C,3,3], both fp16 or
+    both bf16 (then with the bf16 end-to-end option); returns (output tensor,
+    Conv2d handle)."""
     import torch
-    assert x.is_cuda and w.is_cuda and x.dtype == torch.float16 and w.dtype == torch.float16
+    assert x.is_cuda and w.is_cuda and x.dtype == w.dtype and x.dtype in (torch.float16, torch.bfloat16)
     x = x.contiguous()
     w = w.contiguous()
     n, c, h, wd = x.shape
     k = w.shape[0]
     oh, ow = h + 2 * p - 2, wd + 2 * q - 2
-    y = torch.empty((n, k, oh, ow), dtype=torch.float16, device=x.device)
+    if x.dtype == torch.bfloat16:
+        options = options if options is not None else default_options()
+        options.io_bf16 = 1
+    y = torch.empty((n, k, oh, ow), dtype=x.dtype, device=x.device)
     prob = make_problem(x.data_ptr(), w.data_ptr(), y.data_ptr(), n, c, h, wd, k, p, q)
     op = Conv2d(prob, options)
     op._keep = (x, w, y)

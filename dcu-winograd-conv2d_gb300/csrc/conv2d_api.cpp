@@ -106,6 +106,7 @@ int options_default(conv2d_options_t* o) {
     o->gemm_bn = env_int("WG_CONV2D_GEMM_BN", 0);
     const char* l2 = std::getenv("WG_CONV2D_L2_CHUNK_BYTES");
     o->l2_chunk_bytes = (l2 && *l2) ? std::atoll(l2) : 0;
+    o->io_bf16 = env_int("WG_CONV2D_IO_BF16", 0) ? 1 : 0;
     return CONV2D_OK;
 }
 
@@ -172,8 +173,12 @@ int Plan::build(const problem_t* pr, const conv2d_options_t* opt_in) {
     }
     const int m = algo == CONV2D_ALGO_4X3_NON_FUSED ? 4 : 2;
     xf = m == 2 ? Xform::F2 : (opt.f4_points ? Xform::F4Ref : Xform::F4);
-    m_fp32 = (m == 4);
-    scaling = (m == 4) && opt.tile_scaling;
+    // bf16 tensors: bf16 operands for F(2x3) (sums of +-1 multiples stay in
+    // range), fp16 operands with per-tile scaling for F(4x3) (bf16 operands
+    // lose ~10x accuracy there); M in fp32 either way
+    if (opt.io_bf16) op = m == 2 ? OpType::BF16 : OpType::F16;
+    m_fp32 = (m == 4) || opt.io_bf16;
+    scaling = (m == 4) && (opt.tile_scaling || opt.io_bf16);
     g = make_geom(pr->n, pr->c, pr->h, pr->w, pr->k, pr->p, pr->q, m);
     const int E = g.alpha * g.alpha;
     const long long op_bytes = 2;
@@ -221,6 +226,7 @@ int Plan::build(const problem_t* pr, const conv2d_options_t* opt_in) {
 
     if (algo == CONV2D_ALGO_2X3_FUSED) {
         ce = plan_fused2x3(fused, op, g, U);
+        fused.io_bf16 = opt.io_bf16 != 0;
         if (ce != cudaSuccess) return cuda_fail(ce, "fused plan");
         launches = 1;
         info_grid = static_cast<unsigned>(fused.m_blocks * fused.n_blocks);
@@ -248,7 +254,7 @@ int Plan::build(const problem_t* pr, const conv2d_options_t* opt_in) {
 }
 
 int Plan::filter(cudaStream_t s) {
-    cudaError_t ce = launch_filter_transform(xf, op, prob.weight, U, g.k, g.c, g.cp, s);
+    cudaError_t ce = launch_filter_transform(xf, op, prob.weight, U, g.k, g.c, g.cp, s, opt.io_bf16 != 0);
     if (ce != cudaSuccess) return cuda_fail(ce, "filter transform launch");
     filter_ready = true;
     return CONV2D_OK;
@@ -273,17 +279,17 @@ int Plan::run_range(int n0, int nc, const GemmPlan* gp, cudaStream_t s) {
         return CONV2D_OK;
     }
     if (scaling) {
-        ce = launch_tile_scale(gc, xin, scale, s);
+        ce = launch_tile_scale(gc, xin, scale, s, opt.io_bf16 != 0);
         if (ce != cudaSuccess) return cuda_fail(ce, "tile scale launch");
         mark(s);
     }
-    ce = launch_input_transform(xf, op, gc, xin, x_end, V, scale, err, s);
+    ce = launch_input_transform(xf, op, gc, xin, x_end, V, scale, err, s, opt.io_bf16 != 0);
     if (ce != cudaSuccess) return cuda_fail(ce, "input transform launch");
     mark(s);
     ce = launch_gemm(*gp, err, s);
     if (ce != cudaSuccess) return cuda_fail(ce, "GEMM launch");
     mark(s);
-    ce = launch_output_transform(xf, m_fp32, gc, Mw, yout, scale, s);
+    ce = launch_output_transform(xf, m_fp32, gc, Mw, yout, scale, s, opt.io_bf16 != 0);
     if (ce != cudaSuccess) return cuda_fail(ce, "output transform launch");
     mark(s);
     return CONV2D_OK;

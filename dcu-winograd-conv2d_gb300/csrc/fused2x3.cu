@@ -65,13 +65,23 @@ template <> struct OpT<true> {
     }
 };
 
+// The caller's element type (fp16, or bf16 for the end-to-end bf16 option).
+template <bool IOB> __device__ __forceinline__ float io_load(const __half* p) {
+    if constexpr (IOB) return __bfloat162float(*reinterpret_cast<const __nv_bfloat16*>(p));
+    return __half2float(*p);
+}
+template <bool IOB> __device__ __forceinline__ void io_store1(__half* p, float v) {
+    if constexpr (IOB) *reinterpret_cast<__nv_bfloat16*>(p) = __float2bfloat16_rn(v);
+    else *p = __float2half_rn(v);
+}
+
 struct SegTable {
     int nseg;
     int n_first;
     int ylo[kMaxSeg], yhi[kMaxSeg], off[kMaxSeg];
 };
 
-template <bool BF16>
+template <bool BF16, bool IOB>
 __global__ void __launch_bounds__(kThreads, 1)
     fused2x3_kernel(const __half* __restrict__ x, const __half* __restrict__ x_end,
                     const __grid_constant__ CUtensorMap tmU, __half* __restrict__ out, int C, int H, int W, int K,
@@ -376,14 +386,14 @@ __global__ void __launch_bounds__(kThreads, 1)
                             for (int i = 0; i < 4; ++i)
 #pragma unroll
                                 for (int j = 0; j < 4; ++j)
-                                    d[i * 4 + j] = (chv && rv[i] && cv[j]) ? __half2float(src[i * W + j]) : 0.f;
+                                    d[i * 4 + j] = (chv && rv[i] && cv[j]) ? io_load<IOB>(src + i * W + j) : 0.f;
                         } else {
                             const __half* src = gsrc + static_cast<long long>(ylo) * W + row0;
 #pragma unroll
                             for (int i = 0; i < 4; ++i)
 #pragma unroll
                                 for (int j = 0; j < 4; ++j)
-                                    d[i * 4 + j] = (chv && rv[i] && cv[j]) ? __half2float(src[i * W + j]) : 0.f;
+                                    d[i * 4 + j] = (chv && rv[i] && cv[j]) ? io_load<IOB>(src + i * W + j) : 0.f;
                         }
                         input_tile_transform<F2>(d, v[h]);
                     }
@@ -456,10 +466,10 @@ __global__ void __launch_bounds__(kThreads, 1)
                             if (oh0 + a >= OH) continue;
                             __half* dst = o + static_cast<long long>(oh0 + a) * OW + ow0;
                             if (ow0 + 1 < OW && (reinterpret_cast<uintptr_t>(dst) & 3) == 0) {
-                                *reinterpret_cast<__half2*>(dst) = __floats2half2_rn(y[q][a * 2], y[q][a * 2 + 1]);
+                                *reinterpret_cast<uint32_t*>(dst) = OpT<IOB>::pack(y[q][a * 2], y[q][a * 2 + 1]);
                             } else {
-                                dst[0] = __float2half_rn(y[q][a * 2]);
-                                if (ow0 + 1 < OW) dst[1] = __float2half_rn(y[q][a * 2 + 1]);
+                                io_store1<IOB>(dst, y[q][a * 2]);
+                                if (ow0 + 1 < OW) io_store1<IOB>(dst + 1, y[q][a * 2 + 1]);
                             }
                         }
                     }
@@ -512,6 +522,7 @@ int staging_bytes_per_channel(const Geom& g, int* max_segments) {
 
 cudaError_t plan_fused2x3(FusedPlan& fp, OpType op, const Geom& g, const void* U) {
     if (g.m != 2) return cudaErrorInvalidValue;
+    fp.io_bf16 = false;
     int segs = 0;
     fp.stg_ch_bytes = staging_bytes_per_channel(g, &segs);
     // two staging buffers when they fit (copies run a chunk ahead), else one
@@ -552,7 +563,10 @@ cudaError_t launch_fused2x3(const FusedPlan& fp, const Geom& g, const void* x, c
         sms <= 0)
         sms = 148;
     const long long blocks = std::min<long long>(items, sms);
-    auto kern = fp.op == OpType::BF16 ? fused2x3_kernel<true> : fused2x3_kernel<false>;
+    // bf16 tensors run with bf16 operands
+    if (fp.io_bf16 && fp.op != OpType::BF16) return cudaErrorNotSupported;
+    auto kern = fp.io_bf16 ? fused2x3_kernel<true, true>
+                           : (fp.op == OpType::BF16 ? fused2x3_kernel<true, false> : fused2x3_kernel<false, false>);
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, fp.smem_bytes);
     if (e != cudaSuccess) return e;
     return launch_pdl(kern, dim3(static_cast<unsigned>(blocks)), dim3(kThreads), fp.smem_bytes, stream,

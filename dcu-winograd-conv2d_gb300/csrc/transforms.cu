@@ -65,12 +65,27 @@ template <class T> __device__ __forceinline__ T from_f32(float v);
 template <> __device__ __forceinline__ __half from_f32<__half>(float v) { return __float2half_rn(v); }
 template <> __device__ __forceinline__ __nv_bfloat16 from_f32<__nv_bfloat16>(float v) { return __float2bfloat16_rn(v); }
 
+// Element type of the caller's tensors (input, filter, output): fp16, or
+// bf16 for the end-to-end bf16 option.
+template <bool BF> struct IO;
+template <> struct IO<false> {
+    using T = __half;
+    __device__ static float to_f(T v) { return __half2float(v); }
+    // two 16-bit values packed in one word (low = first) to fp32
+    __device__ static float2 pair(uint32_t h) { return __half22float2(*reinterpret_cast<const __half2*>(&h)); }
+};
+template <> struct IO<true> {
+    using T = __nv_bfloat16;
+    __device__ static float to_f(T v) { return __bfloat162float(v); }
+    __device__ static float2 pair(uint32_t h) { return make_float2(__uint_as_float(h << 16), __uint_as_float(h & 0xffff0000u)); }
+};
+
 // ---- filter transform --------------------------------------------------------
 // One thread per (k, c); U[e][c/8][k][c%8].
 
-template <class TF, class OutT>
-__global__ void __launch_bounds__(256) filter_transform_kernel(const __half* __restrict__ w, OutT* __restrict__ U,
-                                                               int K, int C, int Cp, int Kp) {
+template <class TF, class OutT, bool WB>
+__global__ void __launch_bounds__(256) filter_transform_kernel(const typename IO<WB>::T* __restrict__ w,
+                                                               OutT* __restrict__ U, int K, int C, int Cp, int Kp) {
     constexpr int A = TF::ALPHA;
     const long long idx = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (idx >= static_cast<long long>(Kp) * Cp) return;
@@ -79,9 +94,9 @@ __global__ void __launch_bounds__(256) filter_transform_kernel(const __half* __r
 #pragma unroll
     for (int i = 0; i < 9; ++i) g[i] = 0.f;
     if (c < C && k < K) {
-        const __half* src = w + (static_cast<long long>(k) * C + c) * 9;
+        const typename IO<WB>::T* src = w + (static_cast<long long>(k) * C + c) * 9;
 #pragma unroll
-        for (int i = 0; i < 9; ++i) g[i] = __half2float(src[i]);
+        for (int i = 0; i < 9; ++i) g[i] = IO<WB>::to_f(src[i]);
     }
     float u[A * A];
     filter_tile_transform<TF>(g, u);
@@ -97,8 +112,8 @@ __global__ void __launch_bounds__(256) filter_transform_kernel(const __half* __r
 // for both F(4x3) point sets (|V| <= 100 max|d|).  A power of two changes
 // no rounding of normal-range values.
 
-template <int M>
-__global__ void __launch_bounds__(256) tile_scale_kernel(const __half* __restrict__ x, float* __restrict__ scale,
+template <int M, bool XB>
+__global__ void __launch_bounds__(256) tile_scale_kernel(const typename IO<XB>::T* __restrict__ x, float* __restrict__ scale,
                                                          int C, int H, int W, int pad_h, int pad_w, int tiles_h,
                                                          int tiles_w, long long P) {
     constexpr int A = M + 2;
@@ -113,14 +128,14 @@ __global__ void __launch_bounds__(256) tile_scale_kernel(const __half* __restric
     const int y0 = th * M - pad_h, x0 = tw * M - pad_w;
     float amax = 0.f;
     for (int c = lane; c < C; c += 32) {
-        const __half* plane = x + (n * C + c) * static_cast<long long>(H) * W;
+        const typename IO<XB>::T* plane = x + (n * C + c) * static_cast<long long>(H) * W;
         for (int i = 0; i < A; ++i) {
             const int y = y0 + i;
             if (y < 0 || y >= H) continue;
             for (int j = 0; j < A; ++j) {
                 const int xx = x0 + j;
                 if (xx < 0 || xx >= W) continue;
-                amax = fmaxf(amax, fabsf(__half2float(plane[static_cast<long long>(y) * W + xx])));
+                amax = fmaxf(amax, fabsf(IO<XB>::to_f(plane[static_cast<long long>(y) * W + xx])));
             }
         }
     }
@@ -259,7 +274,7 @@ __device__ __forceinline__ void in_issue(const InDesc& d, long long local, unsig
 // Compute warp cw (of kInComputeWarps) transforms its share of the item:
 // lanes are (tile offset q, channel pair sub) with four pairs per granule
 // row; tiles q, q + Q, q + 2Q, ... of the item for every granule.
-template <class TF, class OutT, bool SCALED>
+template <class TF, class OutT, bool SCALED, bool XB>
 __device__ __forceinline__ void in_compute(const InDesc& d, long long local, const unsigned char* buf,
                                            const unsigned char* zero, int cw) {
     constexpr int M = TF::M, A = TF::ALPHA;
@@ -314,7 +329,7 @@ __device__ __forceinline__ void in_compute(const InDesc& d, long long local, con
 #pragma unroll
                 for (int j = 0; j < A; ++j) {
                     const uint32_t h = __byte_perm(r0[j], r1[j], sel[j]);
-                    float2 v = __half22float2(*reinterpret_cast<const __half2*>(&h));
+                    float2 v = IO<XB>::pair(h);
                     if constexpr (SCALED) v = __fmul2_rn(v, s2);
                     dv[j] = v;
                 }
@@ -353,7 +368,7 @@ __device__ __forceinline__ void in_compute(const InDesc& d, long long local, con
 // once the compute warps have released that buffer (empty barrier, one
 // arrival per compute warp) and signals the full barrier; the compute warps
 // never wait for one another.
-template <class TF, class OutT, bool SCALED>
+template <class TF, class OutT, bool SCALED, bool XB>
 __device__ __forceinline__ void input_body(const InDesc* descs, int ndesc, long long total, int buf_bytes,
                                            unsigned char* smem_raw, DevErr* err) {
     constexpr int M = TF::M, A = TF::ALPHA;
@@ -389,7 +404,7 @@ __device__ __forceinline__ void input_body(const InDesc* descs, int ndesc, long 
             const int b = k & 1;
             if (!mbar_wait(&full[b], (k >> 1) & 1, abort_flag, err, ERR_SITE_FULL)) break;
             const InDesc& d = in_desc_of(descs, ndesc, item);
-            in_compute<TF, OutT, SCALED>(d, item - d.blk_begin, bufs + b * buf_bytes, zero, warp);
+            in_compute<TF, OutT, SCALED, XB>(d, item - d.blk_begin, bufs + b * buf_bytes, zero, warp);
             __syncwarp();
             if ((threadIdx.x & 31) == 0) mbar_arrive(&empty[b]);
         }
@@ -402,18 +417,18 @@ __device__ __forceinline__ void input_body(const InDesc* descs, int ndesc, long 
     }
 }
 
-template <class TF, class OutT, bool SCALED>
+template <class TF, class OutT, bool SCALED, bool XB>
 __global__ void __launch_bounds__(kInThreads, 2)
     input_transform_kernel(const __grid_constant__ InDesc d, long long total, int buf_bytes, DevErr* err) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    input_body<TF, OutT, SCALED>(&d, 1, total, buf_bytes, smem_raw, err);
+    input_body<TF, OutT, SCALED, XB>(&d, 1, total, buf_bytes, smem_raw, err);
 }
 
 template <class TF, class OutT, bool SCALED>
 __global__ void __launch_bounds__(kInThreads, 2) input_transform_grouped(const InDesc* __restrict__ descs, int ndesc,
                                                                        long long total, int buf_bytes, DevErr* err) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    input_body<TF, OutT, SCALED>(descs, ndesc, total, buf_bytes, smem_raw, err);
+    input_body<TF, OutT, SCALED, false>(descs, ndesc, total, buf_bytes, smem_raw, err);
 }
 
 // ---- output transform ----------------------------------------------------------
@@ -440,30 +455,29 @@ template <> struct MG<float> {
     }
 };
 
-template <int M>
-__device__ __forceinline__ void store_row(__half* dst, const float* y, int valid, float inv) {
+// One output row of a tile (M values, `valid` of them inside the image) in
+// the caller's element type YT (fp16 or bf16).
+template <int M, class YT>
+__device__ __forceinline__ void store_row(YT* dst, const float* y, int valid, float inv) {
     const uintptr_t a = reinterpret_cast<uintptr_t>(dst);
     if (M == 2 && valid == 2 && (a & 3) == 0) {
-        *reinterpret_cast<__half2*>(dst) = __floats2half2_rn(y[0] * inv, y[1] * inv);
+        *reinterpret_cast<uint32_t*>(dst) = pack2<YT>(y[0] * inv, y[1] * inv);
     } else if (M == 4 && valid == 4 && (a & 7) == 0) {
-        __half2 lo = __floats2half2_rn(y[0] * inv, y[1] * inv), hi = __floats2half2_rn(y[2] * inv, y[3] * inv);
-        uint2 u;
-        u.x = *reinterpret_cast<uint32_t*>(&lo);
-        u.y = *reinterpret_cast<uint32_t*>(&hi);
-        *reinterpret_cast<uint2*>(dst) = u;
+        *reinterpret_cast<uint2*>(dst) = make_uint2(pack2<YT>(y[0] * inv, y[1] * inv), pack2<YT>(y[2] * inv, y[3] * inv));
     } else {
 #pragma unroll
         for (int j = 0; j < M; ++j)
-            if (j < valid) dst[j] = __float2half_rn(y[j] * inv);
+            if (j < valid) dst[j] = from_f32<YT>(y[j] * inv);
     }
 }
 
-template <class TF, class MT>
+template <class TF, class MT, bool YB>
 __device__ __forceinline__ void output_body(const OutDesc& d, long long bx, int g) {
+    using YT = typename IO<YB>::T;
     constexpr int M = TF::M, A = TF::ALPHA;
     constexpr int PG = MG<MT>::kPerGranule, PH = MG<MT>::kPerHalf;
     const MT* __restrict__ Mw = static_cast<const MT*>(d.Mw);
-    __half* __restrict__ out = d.out;
+    YT* __restrict__ out = reinterpret_cast<YT*>(d.out);
     const float* __restrict__ scale = d.scale;
     const int K = d.K, OH = d.OH, OW = d.OW, tiles_h = d.tiles_h, tiles_w = d.tiles_w, KG = d.KG;
     const long long P = d.P;
@@ -493,18 +507,18 @@ __device__ __forceinline__ void output_body(const OutDesc& d, long long bx, int 
 #pragma unroll
         for (int e = 0; e < A * A; ++e) mm[e] = m[e][ch];
         output_tile_transform<TF>(mm, y);
-        __half* o = out + ((n * K + k) * OH + oh0) * static_cast<long long>(OW) + ow0;
+        YT* o = out + ((n * K + k) * OH + oh0) * static_cast<long long>(OW) + ow0;
 #pragma unroll
         for (int i = 0; i < M; ++i)
             if (i < vr) store_row<M>(o + static_cast<long long>(i) * OW, &y[i * M], vc, inv);
     }
 }
 
-template <class TF, class MT>
+template <class TF, class MT, bool YB>
 __global__ void __launch_bounds__(kOutThreads) output_transform_kernel(const __grid_constant__ OutDesc d) {
     pdl_wait();     // M written, earlier readers of the output done
     pdl_trigger();
-    output_body<TF, MT>(d, blockIdx.x, blockIdx.y);
+    output_body<TF, MT, YB>(d, blockIdx.x, blockIdx.y);
 }
 
 template <class TF, class MT>
@@ -519,7 +533,7 @@ __global__ void __launch_bounds__(kOutThreads) output_transform_grouped(const Ou
     }
     const OutDesc& d = descs[lo];
     const long long local = b - d.blk_begin;
-    output_body<TF, MT>(d, local % d.gx, static_cast<int>(local / d.gx));
+    output_body<TF, MT, false>(d, local % d.gx, static_cast<int>(local / d.gx));
 }
 
 struct InBlocking {
@@ -580,9 +594,9 @@ InBlocking choose_in_blocking(const Geom& g) {
     return best;
 }
 
-template <class TF, class OutT, bool SCALED>
+template <class TF, class OutT, bool SCALED, bool XB = false>
 cudaError_t input_launch(const InDesc& d, int smem, DevErr* err, cudaStream_t s) {
-    auto kern = input_transform_kernel<TF, OutT, SCALED>;
+    auto kern = input_transform_kernel<TF, OutT, SCALED, XB>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e != cudaSuccess) return e;
     const long long total = d.gx * d.gy;
@@ -602,9 +616,9 @@ cudaError_t input_grouped_launch(const InDesc* descs, int ndesc, long long total
                       (smem - kInHeader - 2 * kInSlack) / 2, err);
 }
 
-template <class TF, class MT>
+template <class TF, class MT, bool YB = false>
 cudaError_t output_launch(const OutDesc& d, cudaStream_t s) {
-    return launch_pdl(output_transform_kernel<TF, MT>, dim3(static_cast<unsigned>(d.gx), static_cast<unsigned>(d.gy)),
+    return launch_pdl(output_transform_kernel<TF, MT, YB>, dim3(static_cast<unsigned>(d.gx), static_cast<unsigned>(d.gy)),
                       dim3(kOutThreads), 0, s, d);
 }
 
@@ -615,42 +629,54 @@ cudaError_t output_grouped_launch(const OutDesc* descs, int ndesc, long long blo
 }
 
 template <class TF, class OutT>
-cudaError_t filter_launch(const void* w, void* U, int K, int C, int Cp, cudaStream_t s) {
+cudaError_t filter_launch(const void* w, void* U, int K, int C, int Cp, cudaStream_t s, bool wb) {
     const int Kp = (K + 7) / 8 * 8;
     const long long total = static_cast<long long>(Kp) * Cp;
     const unsigned blocks = static_cast<unsigned>((total + 255) / 256);
-    filter_transform_kernel<TF, OutT><<<blocks, 256, 0, s>>>(static_cast<const __half*>(w), static_cast<OutT*>(U), K, C,
-                                                            Cp, Kp);
+    if (wb)
+        filter_transform_kernel<TF, OutT, true><<<blocks, 256, 0, s>>>(static_cast<const __nv_bfloat16*>(w),
+                                                                      static_cast<OutT*>(U), K, C, Cp, Kp);
+    else
+        filter_transform_kernel<TF, OutT, false><<<blocks, 256, 0, s>>>(static_cast<const __half*>(w),
+                                                                       static_cast<OutT*>(U), K, C, Cp, Kp);
     return cudaGetLastError();
 }
 
 }  // namespace
 
 cudaError_t launch_filter_transform(Xform xf, OpType op, const void* weight, void* U, int K, int C, int Cp,
-                                    cudaStream_t stream) {
+                                    cudaStream_t stream, bool w_bf16) {
     const bool bf = op == OpType::BF16;
     switch (xf) {
         case Xform::F2:
-            return bf ? filter_launch<F2, __nv_bfloat16>(weight, U, K, C, Cp, stream)
-                      : filter_launch<F2, __half>(weight, U, K, C, Cp, stream);
+            return bf ? filter_launch<F2, __nv_bfloat16>(weight, U, K, C, Cp, stream, w_bf16)
+                      : filter_launch<F2, __half>(weight, U, K, C, Cp, stream, w_bf16);
         case Xform::F4:
-            return bf ? filter_launch<F4, __nv_bfloat16>(weight, U, K, C, Cp, stream)
-                      : filter_launch<F4, __half>(weight, U, K, C, Cp, stream);
+            return bf ? filter_launch<F4, __nv_bfloat16>(weight, U, K, C, Cp, stream, w_bf16)
+                      : filter_launch<F4, __half>(weight, U, K, C, Cp, stream, w_bf16);
         case Xform::F4Ref:
-            return bf ? filter_launch<F4Ref, __nv_bfloat16>(weight, U, K, C, Cp, stream)
-                      : filter_launch<F4Ref, __half>(weight, U, K, C, Cp, stream);
+            return bf ? filter_launch<F4Ref, __nv_bfloat16>(weight, U, K, C, Cp, stream, w_bf16)
+                      : filter_launch<F4Ref, __half>(weight, U, K, C, Cp, stream, w_bf16);
     }
     return cudaErrorInvalidValue;
 }
 
-cudaError_t launch_tile_scale(const Geom& g, const void* x, float* scale, cudaStream_t stream) {
+cudaError_t launch_tile_scale(const Geom& g, const void* x, float* scale, cudaStream_t stream, bool x_bf16) {
     const unsigned blocks = static_cast<unsigned>((g.P + 7) / 8);
+    if (x_bf16) {
+        const __nv_bfloat16* xb = static_cast<const __nv_bfloat16*>(x);
+        if (g.m == 2)
+            return launch_pdl(tile_scale_kernel<2, true>, dim3(blocks), dim3(256), 0, stream, xb, scale, g.c, g.h, g.w,
+                              g.pad_h, g.pad_w, g.tiles_h, g.tiles_w, g.P);
+        return launch_pdl(tile_scale_kernel<4, true>, dim3(blocks), dim3(256), 0, stream, xb, scale, g.c, g.h, g.w,
+                          g.pad_h, g.pad_w, g.tiles_h, g.tiles_w, g.P);
+    }
     const __half* xh = static_cast<const __half*>(x);
     if (g.m == 2)
-        return launch_pdl(tile_scale_kernel<2>, dim3(blocks), dim3(256), 0, stream, xh, scale, g.c, g.h, g.w, g.pad_h,
-                          g.pad_w, g.tiles_h, g.tiles_w, g.P);
-    return launch_pdl(tile_scale_kernel<4>, dim3(blocks), dim3(256), 0, stream, xh, scale, g.c, g.h, g.w, g.pad_h,
-                      g.pad_w, g.tiles_h, g.tiles_w, g.P);
+        return launch_pdl(tile_scale_kernel<2, false>, dim3(blocks), dim3(256), 0, stream, xh, scale, g.c, g.h, g.w,
+                          g.pad_h, g.pad_w, g.tiles_h, g.tiles_w, g.P);
+    return launch_pdl(tile_scale_kernel<4, false>, dim3(blocks), dim3(256), 0, stream, xh, scale, g.c, g.h, g.w,
+                      g.pad_h, g.pad_w, g.tiles_h, g.tiles_w, g.P);
 }
 
 InDesc make_in_desc(const Geom& g, const void* x, const void* x_end, void* V, const float* scale, int* smem) {
@@ -687,10 +713,18 @@ OutDesc make_out_desc(const Geom& g, bool m_fp32, const void* Mw, void* out, con
 }
 
 cudaError_t launch_input_transform(Xform xf, OpType op, const Geom& g, const void* x, const void* x_end, void* V,
-                                   const float* scale, DevErr* err, cudaStream_t stream) {
+                                   const float* scale, DevErr* err, cudaStream_t stream, bool x_bf16) {
     int smem = 0;
     const InDesc d = make_in_desc(g, x, x_end, V, scale, &smem);
     const bool bf = op == OpType::BF16, sc = scale != nullptr;
+    if (x_bf16) {
+        // bf16 tensors: F(2x3) with bf16 operands, F(4x3) with fp16 operands
+        // and per-tile scaling (the plan arranges these pairings)
+        if (xf == Xform::F2 && bf && !sc) return input_launch<F2, __nv_bfloat16, false, true>(d, smem, err, stream);
+        if (xf == Xform::F4 && !bf && sc) return input_launch<F4, __half, true, true>(d, smem, err, stream);
+        if (xf == Xform::F4Ref && !bf && sc) return input_launch<F4Ref, __half, true, true>(d, smem, err, stream);
+        return cudaErrorNotSupported;
+    }
     switch (xf) {
         case Xform::F2:  // never scaled
             return bf ? input_launch<F2, __nv_bfloat16, false>(d, smem, err, stream)
@@ -735,8 +769,17 @@ cudaError_t launch_input_transform_grouped(Xform xf, OpType op, const InDesc* de
 }
 
 cudaError_t launch_output_transform(Xform xf, bool m_fp32, const Geom& g, const void* Mw, void* out,
-                                    const float* scale, cudaStream_t stream) {
+                                    const float* scale, cudaStream_t stream, bool y_bf16) {
     const OutDesc d = make_out_desc(g, m_fp32, Mw, out, scale);
+    if (y_bf16) {  // bf16 tensors: M is fp32 for both transforms
+        if (!m_fp32) return cudaErrorNotSupported;
+        switch (xf) {
+            case Xform::F2: return output_launch<F2, float, true>(d, stream);
+            case Xform::F4: return output_launch<F4, float, true>(d, stream);
+            case Xform::F4Ref: return output_launch<F4Ref, float, true>(d, stream);
+        }
+        return cudaErrorInvalidValue;
+    }
     switch (xf) {
         case Xform::F2:
             return m_fp32 ? output_launch<F2, float>(d, stream) : output_launch<F2, __half>(d, stream);

@@ -45,17 +45,17 @@ inline long long round_rows(long long P) { return (P + 7) / 8 * 8; }
 // U[e][Cp/8][Kp][8] = G g G^T, from KCRS fp16 weights; fp32 arithmetic, result
 // in the operand type; zero for c >= C or k >= K.
 cudaError_t launch_filter_transform(Xform xf, OpType op, const void* weight, void* U, int K, int C, int Cp,
-                                    cudaStream_t stream);
+                                    cudaStream_t stream, bool w_bf16 = false);
 
 // Per-tile power-of-two scale (F(4x3) scaling option): scale[p] = 2^-floor(log2 max|d|)
 // over the tile's input patch in every channel; 1 for an all-zero patch.
-cudaError_t launch_tile_scale(const Geom& g, const void* x, float* scale, cudaStream_t stream);
+cudaError_t launch_tile_scale(const Geom& g, const void* x, float* scale, cudaStream_t stream, bool x_bf16 = false);
 
 // V[e][Cp/8][round_rows(P)][8] = B^T d B for the g.n images starting at x (x may point
 // into a larger tensor that ends at x_end; the full tensor must start on a
 // 16-byte boundary).  scale may be null.
 cudaError_t launch_input_transform(Xform xf, OpType op, const Geom& g, const void* x, const void* x_end, void* V,
-                                   const float* scale, DevErr* err, cudaStream_t stream);
+                                   const float* scale, DevErr* err, cudaStream_t stream, bool x_bf16 = false);
 
 // Per-problem descriptors of the transform kernels (device-resident arrays of
 // them drive the grouped launches that run many problems at once).
@@ -99,7 +99,7 @@ cudaError_t launch_output_transform_grouped(Xform xf, bool m_fp32, const OutDesc
 // out[N][K][OH][OW] = A^T M A from M[e][Kp/8][P][8] (fp16, m_fp32 false) or
 // M[e][Kp/4][P][4] (fp32); divides by scale[p] when scale is not null.
 cudaError_t launch_output_transform(Xform xf, bool m_fp32, const Geom& g, const void* Mw, void* out,
-                                    const float* scale, cudaStream_t stream);
+                                    const float* scale, cudaStream_t stream, bool y_bf16 = false);
 
 // ---- tcgen05 batched GEMM: M_e[P][K] = V_e[P][Cp] * U_e[K][Cp]^T -----------
 // (operands and result in the 16-byte granule layouts above)
@@ -143,6 +143,7 @@ struct FusedPlan {
     int nbuf;            // staging buffers (2 = copies one chunk ahead)
     int smem_bytes;
     OpType op;
+    bool io_bf16;        // input and output tensors bf16 (operands then bf16 too)
 };
 
 // cudaErrorNotSupported when the staged rows of one CTA do not fit in shared

@@ -97,7 +97,9 @@ typedef struct
     int filter_policy;   /* 0: transform the filter on the first call, then reuse; 1: every call */
     int gemm_bn;         /* GEMM output-channel tile: 0 = automatic, else 32/64/128/256 */
     long long l2_chunk_bytes; /* non-fused: process images in chunks whose V+M fit this many bytes (0 = one pass) */
-    int reserved[4];
+    int io_bf16;         /* 1: input, filter and output tensors are bf16 (end to end); F(2x3) then uses bf16
+                            operands, F(4x3) fp16 operands with per-tile scaling, both an fp32 M */
+    int reserved[3];
 } conv2d_options_t;
 
 /* reference include/conv2d.h:39-42 */

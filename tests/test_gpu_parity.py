@@ -286,3 +286,49 @@ def test_autotune_choice_is_cached_and_correct(wg):
     torch.cuda.synchronize()
     _, r64 = O.conv2d_direct(x, wt, nthreads=8)
     assert O.rel_errors(y.cpu().numpy(), r64)[0] <= TOL[algo_m(op.algo)]
+
+
+def _to_bf16_bits(a):
+    """float32 -> bf16 bit patterns, round to nearest even."""
+    u = np.ascontiguousarray(a, dtype=np.float32).view(np.uint32).astype(np.uint64)
+    return ((u + 0x7FFF + ((u >> 16) & 1)) >> 16).astype(np.uint16)
+
+
+def _bf16_to_f64(b):
+    return (b.astype(np.uint32) << 16).view(np.float32).astype(np.float64)
+
+
+def _direct64(x, w, p=1):
+    n, c, h, ww = x.shape
+    xp = np.pad(x, ((0, 0), (0, 0), (p, p), (p, p)))
+    out = np.zeros((n, w.shape[0], h + 2 * p - 2, ww + 2 * p - 2))
+    for r in range(3):
+        for s_ in range(3):
+            out += np.einsum("nchw,kc->nkhw", xp[:, :, r:r + out.shape[2], s_:s_ + out.shape[3]], w[:, :, r, s_])
+    return out
+
+
+# bf16 tensors: F(2x3) and fused run bf16 operands (max error 2.0e-2 at C=512 in
+# the precision study), F(4x3) fp16 operands with per-tile scaling; the bf16
+# output rounding adds up to 2^-9 relative
+BF16_TOL = {0: 2.5e-2, 1: 4e-2, 2: 4e-2}
+
+
+@pytest.mark.parametrize("algo", [0, 1, 2])
+@pytest.mark.parametrize("shape", [(2, 24, 16, 16, 32), (1, 40, 13, 11, 20), (3, 96, 28, 28, 64)])
+def test_bf16_end_to_end(wg, algo, shape):
+    """bf16 input, filter and output tensors against the FP64 direct
+    convolution of the same bf16 values."""
+    n, c, h, w, k = shape
+    rng = np.random.default_rng(101 + algo)
+    xb = _to_bf16_bits(rng.uniform(-1, 1, (n, c, h, w)))
+    wb = _to_bf16_bits(rng.standard_normal((k, c, 3, 3)) / np.sqrt(9 * c))
+    x = torch.from_numpy(xb.view(np.int16)).cuda().view(torch.bfloat16)
+    wt = torch.from_numpy(wb.view(np.int16)).cuda().view(torch.bfloat16)
+    y, op = wg.conv2d_torch(x, wt, 1, 1, opts_for(wg, algo))
+    torch.cuda.synchronize()
+    assert y.dtype == torch.bfloat16 and op.algo == algo
+    got = _bf16_to_f64(y.view(torch.int16).cpu().numpy().view(np.uint16))
+    ref = _direct64(_bf16_to_f64(xb), _bf16_to_f64(wb))
+    assert O.rel_errors(got, ref)[0] <= BF16_TOL[algo]
+    op.destroy()
