@@ -365,6 +365,8 @@ def our_arm(args):
         opts.gemm_bn = args.gemm_bn
     if args.l2_chunk is not None:
         opts.l2_chunk_bytes = args.l2_chunk
+    if args.nhwc:
+        opts.layout_nhwc = 1
     in_bytes = 2 * n * c * h * w
     out_bytes = 2 * n * k * h * w
     nsets = max(2, math.ceil(3 * L2_BYTES / (in_bytes + out_bytes)))
@@ -373,7 +375,9 @@ def our_arm(args):
     x0, wt = make_inputs(torch, args.workload, device, seed=1234 + rank)
     for i in range(nsets):
         x = x0 if i == 0 else x0.roll(i, dims=0).contiguous()
-        y = torch.empty((n, k, h, w), dtype=torch.float16, device=device)
+        if args.nhwc:  # the same values, channels last
+            x = x.permute(0, 2, 3, 1).contiguous()
+        y = torch.empty((n, h, w, k) if args.nhwc else (n, k, h, w), dtype=torch.float16, device=device)
         prob = wg.make_problem(x.data_ptr(), wt.data_ptr(), y.data_ptr(), n, c, h, w, k)
         xs.append(x)
         ys.append(y)
@@ -435,9 +439,9 @@ def our_arm(args):
     # end to end through the host-buffer entry point
     e2e = None
     if not args.no_e2e:
-        hin = torch.empty((n, c, h, w), dtype=torch.float16).pin_memory()
-        hin.copy_(x0.cpu())
-        hout = torch.empty((n, k, h, w), dtype=torch.float16).pin_memory()
+        hin = torch.empty(tuple(xs[0].shape), dtype=torch.float16).pin_memory()
+        hin.copy_(xs[0].cpu())
+        hout = torch.empty(tuple(ys[0].shape), dtype=torch.float16).pin_memory()
         e_steps = max(3, min(args.steps, 20))
         for i in range(2):
             ops[0].host(hin.data_ptr(), hout.data_ptr(), sptr)
@@ -470,9 +474,13 @@ def our_arm(args):
 
     cudnn = None
     if args.cudnn:
-        cms = time_cudnn(torch, xs[0], wt, args.steps, args.warmup)
+        if args.nhwc:  # cuDNN's channels-last kernels on the same values
+            cx, cw = x0.contiguous(memory_format=torch.channels_last), wt.contiguous(memory_format=torch.channels_last)
+        else:
+            cx, cw = xs[0], wt
+        cms = time_cudnn(torch, cx, cw, args.steps, args.warmup)
         cudnn = {"value": flops / (cms * 1e-3) / 1e12, "unit": "TFLOP/s", "ms_per_step": cms,
-                 "path": "torch.nn.functional.conv2d fp16 NCHW, cudnn.benchmark"}
+                 "path": f"torch.nn.functional.conv2d fp16 {'NHWC' if args.nhwc else 'NCHW'}, cudnn.benchmark"}
     lat = sorted(per_step)
     line = {
         "metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": world, "steps": args.steps,
@@ -482,6 +490,7 @@ def our_arm(args):
                    "algo": wg.ALGO_NAMES[algo], "selection": args.algo, "accumulate": "fp32",
                    "input": f"{xdist}, filter {wdist}",
                    "l2": f"{nsets} rotating input/output sets ({nsets * (in_bytes + out_bytes) / 2**20:.0f} MiB) > L2",
+                   "layout": "NHWC" if args.nhwc else "NCHW",
                    "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
         "latency_us": {"p50": lat[len(lat) // 2] * 1e3, "p99": lat[min(len(lat) - 1, int(0.99 * len(lat)))] * 1e3},
         "kernel_ms": kernel_ms,
@@ -806,6 +815,7 @@ def main():
     ap.add_argument("--precision", action="store_true", help="F(4x3) precision study instead of timing")
     ap.add_argument("--suite", action="store_true", help="contest shapes through the drop-in API, with cuDNN")
     ap.add_argument("--cudnn", action="store_true", help="also time cuDNN (torch conv2d) on the workload")
+    ap.add_argument("--nhwc", action="store_true", help="channels-last input and output tensors")
     ap.add_argument("--images", type=int, default=4, help="images of the precision study")
     args = ap.parse_args()
     if args.warmup < 3:

@@ -38,7 +38,8 @@ class Options(ctypes.Structure):
     """conv2d_options_t."""
     _fields_ = [("algo", ctypes.c_int), ("operand_bf16", ctypes.c_int), ("tile_scaling", ctypes.c_int),
                 ("f4_points", ctypes.c_int), ("filter_policy", ctypes.c_int), ("gemm_bn", ctypes.c_int),
-                ("l2_chunk_bytes", ctypes.c_longlong), ("io_bf16", ctypes.c_int), ("reserved", ctypes.c_int * 3)]
+                ("l2_chunk_bytes", ctypes.c_longlong), ("io_bf16", ctypes.c_int), ("layout_nhwc", ctypes.c_int),
+                ("reserved", ctypes.c_int * 2)]
 
 
 # every symbol include/conv2d.h declares

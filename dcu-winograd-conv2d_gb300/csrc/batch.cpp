@@ -106,7 +106,8 @@ int batch_create(const problem_t* problems, int count, const conv2d_options_t* o
     else
         options_default(&opt);
     opt.l2_chunk_bytes = 0;
-    if (opt.io_bf16) return batch_fail(CONV2D_ERR_UNSUPPORTED, "grouped batches take fp16 tensors");
+    if (opt.io_bf16 || opt.layout_nhwc)
+        return batch_fail(CONV2D_ERR_UNSUPPORTED, "grouped batches take fp16 NCHW tensors");
     std::unique_ptr<Batch> b(new Batch());
     for (int i = 0; i < count; ++i) {
         std::unique_ptr<Plan> p(new Plan());

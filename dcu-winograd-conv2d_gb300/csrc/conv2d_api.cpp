@@ -107,6 +107,7 @@ int options_default(conv2d_options_t* o) {
     const char* l2 = std::getenv("WG_CONV2D_L2_CHUNK_BYTES");
     o->l2_chunk_bytes = (l2 && *l2) ? std::atoll(l2) : 0;
     o->io_bf16 = env_int("WG_CONV2D_IO_BF16", 0) ? 1 : 0;
+    o->layout_nhwc = env_int("WG_CONV2D_NHWC", 0) ? 1 : 0;
     return CONV2D_OK;
 }
 
@@ -163,6 +164,12 @@ int Plan::build(const problem_t* pr, const conv2d_options_t* opt_in) {
     if (algo < 0 || algo > 2) return fail(CONV2D_ERR_INVALID, "bad algorithm");
 
     op = opt.operand_bf16 ? OpType::BF16 : OpType::F16;
+    nhwc = opt.layout_nhwc != 0;
+    if (nhwc) {
+        if (opt.io_bf16 || opt.tile_scaling)
+            return fail(CONV2D_ERR_UNSUPPORTED, "NHWC tensors are fp16 without per-tile scaling");
+        if (algo == CONV2D_ALGO_2X3_FUSED) algo = CONV2D_ALGO_2X3_NON_FUSED;  // the fused kernel reads NCHW
+    }
     if (algo == CONV2D_ALGO_2X3_FUSED) {
         // the fused kernel stages the input rows of 128 tiles in shared memory;
         // for very wide images they do not fit and F(2x3) runs non-fused
@@ -182,7 +189,7 @@ int Plan::build(const problem_t* pr, const conv2d_options_t* opt_in) {
     g = make_geom(pr->n, pr->c, pr->h, pr->w, pr->k, pr->p, pr->q, m);
     const int E = g.alpha * g.alpha;
     const long long op_bytes = 2;
-    if (algo != CONV2D_ALGO_2X3_FUSED) {
+    if (algo != CONV2D_ALGO_2X3_FUSED && !nhwc) {
         // the input transform stages whole input rows of 8 channels, twice
         int in_smem = 0;
         make_in_desc(g, pr->in, pr->in, nullptr, nullptr, &in_smem);
@@ -233,20 +240,27 @@ int Plan::build(const problem_t* pr, const conv2d_options_t* opt_in) {
         info_threads = 320;
         info_smem = fused.smem_bytes;
     } else {
+        if (nhwc) {
+            ce = make_nhwc_in_desc(nh_in, g, pr->in, V, &nh_smem);
+            if (ce == cudaErrorNotSupported)
+                return fail(CONV2D_ERR_UNSUPPORTED,
+                            "NHWC needs C a multiple of 8 and rows within one TMA box (about 250 columns)");
+            if (ce != cudaSuccess) return cuda_fail(ce, "NHWC tensor map");
+        }
         const int bn = opt.gemm_bn ? opt.gemm_bn : default_bn(g.k);
-        ce = plan_gemm(gemm_full, op, E, Pc, g.k, g.kp, g.cp, V, U, Mw, m_fp32, bn, num_sms);
+        ce = plan_gemm(gemm_full, op, E, Pc, g.k, g.kp, g.cp, V, U, Mw, m_fp32, bn, num_sms, nhwc);
         if (ce != cudaSuccess) return cuda_fail(ce, "GEMM plan (tensor maps)");
         n_chunks = (static_cast<int>(pr->n) + chunk_n - 1) / chunk_n;
         const int tail_n = static_cast<int>(pr->n) - (n_chunks - 1) * chunk_n;
         has_tail = tail_n != chunk_n;
         if (has_tail) {
             const long long Pt = static_cast<long long>(tail_n) * g.tiles_h * g.tiles_w;
-            ce = plan_gemm(gemm_tail, op, E, Pt, g.k, g.kp, g.cp, V, U, Mw, m_fp32, bn, num_sms);
+            ce = plan_gemm(gemm_tail, op, E, Pt, g.k, g.kp, g.cp, V, U, Mw, m_fp32, bn, num_sms, nhwc);
             if (ce != cudaSuccess) return cuda_fail(ce, "GEMM plan (tail)");
         }
         launches = n_chunks * (3 + (scaling ? 1 : 0));
         info_grid = static_cast<unsigned>(gemm_full.grid);
-        info_threads = 192;
+        info_threads = 320;
         info_smem = gemm_full.smem_bytes;
     }
     filter_ready = false;
@@ -275,6 +289,20 @@ int Plan::run_range(int n0, int nc, const GemmPlan* gp, cudaStream_t s) {
     if (algo == CONV2D_ALGO_2X3_FUSED) {
         ce = launch_fused2x3(fused, gc, xin, x_end, yout, err, s);
         if (ce != cudaSuccess) return cuda_fail(ce, "fused F(2x3) launch");
+        mark(s);
+        return CONV2D_OK;
+    }
+    if (nhwc) {
+        NhwcInDesc d = nh_in;        // V of this launch holds its nc images' tiles
+        d.Pp = round_rows(gc.P);
+        ce = launch_nhwc_input_transform(xf, op, d, nh_smem, n0, nc, err, s);
+        if (ce != cudaSuccess) return cuda_fail(ce, "NHWC input transform launch");
+        mark(s);
+        ce = launch_gemm(*gp, err, s);
+        if (ce != cudaSuccess) return cuda_fail(ce, "GEMM launch");
+        mark(s);
+        ce = launch_nhwc_output_transform(xf, m_fp32, make_nhwc_out_desc(gc, Mw, yout), s);
+        if (ce != cudaSuccess) return cuda_fail(ce, "NHWC output transform launch");
         mark(s);
         return CONV2D_OK;
     }
@@ -349,10 +377,10 @@ int Plan::run_host(const void* host_in, void* host_out, cudaStream_t s) {
         const int bn = gemm_full.bn;
         const int tail = n - (nch - 1) * hc;
         cudaError_t ce = plan_gemm(host_gemm_full, op, E, static_cast<long long>(hc) * g.tiles_h * g.tiles_w, g.k, g.kp,
-                                   g.cp, V, U, Mw, m_fp32, bn, num_sms);
+                                   g.cp, V, U, Mw, m_fp32, bn, num_sms, nhwc);
         if (ce == cudaSuccess)
             ce = plan_gemm(host_gemm_tail, op, E, static_cast<long long>(tail) * g.tiles_h * g.tiles_w, g.k, g.kp, g.cp,
-                           V, U, Mw, m_fp32, bn, num_sms);
+                           V, U, Mw, m_fp32, bn, num_sms, nhwc);
         if (ce != cudaSuccess) return cuda_fail(ce, "GEMM plan (host chunks)");
         host_chunk_n = hc;
     }

@@ -47,6 +47,9 @@ struct GemmCfg {
     static constexpr int kStages = std::min(8, (200 * 1024) / kStageBytes);
     static constexpr int kTmemCols = (2 * BN < 32) ? 32 : 2 * BN;  // two accumulators
     static constexpr int kSmem = kStages * kStageBytes + 1024 /*align*/ + 256 /*barriers*/;
+    // + the row-major epilogue's transpose blocks (32x32 fp32 per epilogue
+    // warp), only in launches that write row-major M
+    static constexpr int kSmemRow = kSmem + 8 * 32 * 32 * 4;
 };
 
 // Epilogue stores of 32 accumulator columns (output channels k0..k0+31) of
@@ -83,6 +86,21 @@ __device__ __forceinline__ void store32<float>(float* Mw, const uint32_t (&r)[32
         if (g0 + j < kg_count)
             *reinterpret_cast<uint4*>(Mw + ((static_cast<long long>(e) * kg_count + g0 + j) * P + p) * 4) =
                 make_uint4(r[4 * j], r[4 * j + 1], r[4 * j + 2], r[4 * j + 3]);
+}
+
+// Row-major M[e][P][Kp] (the NHWC output path): 4 consecutive columns of
+// row p (one 16-byte store for fp32, 8 bytes for fp16); Kp is a multiple of 8.
+template <class MT>
+__device__ __forceinline__ void store4_row(MT* Mw, const uint32_t (&v)[4], long long P, long long p, int k0, int kp,
+                                           int e) {
+    MT* dst = Mw + (static_cast<long long>(e) * P + p) * kp + k0;
+    if constexpr (sizeof(MT) == 4) {
+        *reinterpret_cast<uint4*>(dst) = make_uint4(v[0], v[1], v[2], v[3]);
+    } else {
+        __half2 a = __floats2half2_rn(__uint_as_float(v[0]), __uint_as_float(v[1]));
+        __half2 b = __floats2half2_rn(__uint_as_float(v[2]), __uint_as_float(v[3]));
+        *reinterpret_cast<uint2*>(dst) = make_uint2(*reinterpret_cast<uint32_t*>(&a), *reinterpret_cast<uint32_t*>(&b));
+    }
 }
 
 // Work item t -> problem index (advanced monotonically) and (e, mb, nb):
@@ -126,6 +144,7 @@ __device__ __forceinline__ void gemm_body(const GemmDesc* __restrict__ descs, in
     uint64_t* tfull = bars + 2 * S;
     uint64_t* tempty = bars + 2 * S + 2;
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * S + 4);
+    uint32_t* xpose = reinterpret_cast<uint32_t*>(smem + S * Cfg::kStageBytes + 256);  // [8 warps][32][32]
     volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -238,6 +257,7 @@ __device__ __forceinline__ void gemm_body(const GemmDesc* __restrict__ descs, in
             MT* Mw = static_cast<MT*>(d.Mw);
             const long long P = d.P;
             const int kg_count = d.kg_count;
+            const int m_row = d.m_row, kp = d.kp;
             if (!mbar_wait(&tfull[acc], acc_phase, abort_flag, err, ERR_SITE_TMEM_FULL)) break;
             tc_fence_after();
             const long long p = static_cast<long long>(it.mb) * kBM + row;
@@ -253,7 +273,29 @@ __device__ __forceinline__ void gemm_body(const GemmDesc* __restrict__ descs, in
 #pragma unroll
             for (int ch = 0; ch < kChunks; ++ch) {
                 if (ch + 1 < kChunks) tmem_ld_x32(taddr + (ch + 1) * 32, r[(ch + 1) & 1]);
-                if (p < P) store32<MT>(Mw, r[ch & 1], P, p, it.nb * BN + col0 + ch * 32, kg_count, it.e);
+                if (m_row) {
+                    // row-major M: transpose the warp's 32 rows x 32 columns
+                    // through shared memory (XOR-swizzled, conflict-free) so
+                    // that 8 lanes write one row's 128 contiguous bytes
+                    uint32_t* xp = xpose + (warp - 2) * 1024;
+#pragma unroll
+                    for (int c = 0; c < 32; ++c) xp[lane * 32 + (c ^ lane)] = r[ch & 1][c];
+                    __syncwarp();
+                    const int k0 = it.nb * BN + col0 + ch * 32 + (lane & 7) * 4;
+#pragma unroll
+                    for (int i = 0; i < 8; ++i) {
+                        const int row_w = 4 * i + (lane >> 3);  // row within the warp's 32
+                        const int c0 = (lane & 7) * 4;
+                        uint32_t v[4];
+#pragma unroll
+                        for (int j = 0; j < 4; ++j) v[j] = xp[row_w * 32 + ((c0 + j) ^ row_w)];
+                        const long long pr = static_cast<long long>(it.mb) * kBM + quarter * 32 + row_w;
+                        if (pr < P && k0 < kp) store4_row<MT>(Mw, v, P, pr, k0, kp, it.e);
+                    }
+                    __syncwarp();
+                } else if (p < P) {
+                    store32<MT>(Mw, r[ch & 1], P, p, it.nb * BN + col0 + ch * 32, kg_count, it.e);
+                }
                 if (ch + 1 < kChunks) tc_wait_ld(r[(ch + 1) & 1]);
             }
             tc_fence_before();
@@ -292,16 +334,18 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
 template <int BN, bool BF16, class MT>
 cudaError_t gemm_launch(const GemmDesc& d, int grid, DevErr* err, cudaStream_t s) {
     auto kern = wino_gemm_kernel<BN, BF16, MT>;
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, GemmCfg<BN>::kSmem);
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, GemmCfg<BN>::kSmemRow);
     if (e != cudaSuccess) return e;
-    return launch_pdl(kern, dim3(grid), dim3(kGemmThreads), GemmCfg<BN>::kSmem, s, d, err);
+    return launch_pdl(kern, dim3(grid), dim3(kGemmThreads), d.m_row ? GemmCfg<BN>::kSmemRow : GemmCfg<BN>::kSmem, s, d,
+                      err);
 }
 
 template <int BN, bool BF16, class MT>
 cudaError_t gemm_grouped_launch(const GemmDesc* descs, int ndesc, long long total, int grid, DevErr* err,
                                 cudaStream_t s) {
     auto kern = wino_gemm_grouped<BN, BF16, MT>;
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, GemmCfg<BN>::kSmem);
+    // grouped problems write granule-layout M
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, GemmCfg<BN>::kSmemRow);
     if (e != cudaSuccess) return e;
     return launch_pdl(kern, dim3(grid), dim3(kGemmThreads), GemmCfg<BN>::kSmem, s, descs, ndesc, total, err);
 }
@@ -363,12 +407,14 @@ int gemm_smem_bytes(int bn) {
 }
 
 cudaError_t make_gemm_desc(GemmDesc& d, OpType op, int E, long long P, int K, int Kp, int Cp, const void* V,
-                           const void* U, void* Mw, bool m_fp32, int bn) {
+                           const void* U, void* Mw, bool m_fp32, int bn, bool m_row) {
     if (bn != 32 && bn != 64 && bn != 128 && bn != 256) return cudaErrorInvalidValue;
     if (P <= 0 || P > 0x7fffffffLL || Cp % 8 != 0 || Kp % 8 != 0) return cudaErrorInvalidValue;
     d.Mw = Mw;
     d.P = static_cast<int>(P);
     d.kg_count = m_fp32 ? Kp / 4 : Kp / 8;
+    d.m_row = m_row ? 1 : 0;
+    d.kp = Kp;
     d.m_blocks = static_cast<int>((P + kBM - 1) / kBM);
     d.n_blocks = (K + bn - 1) / bn;
     d.k_blocks = (Cp + kBK - 1) / kBK;
@@ -403,8 +449,8 @@ cudaError_t make_gemm_desc(GemmDesc& d, OpType op, int E, long long P, int K, in
 }
 
 cudaError_t plan_gemm(GemmPlan& gp, OpType op, int E, long long P, int K, int Kp, int Cp, const void* V,
-                      const void* U, void* Mw, bool m_fp32, int bn, int num_sms) {
-    cudaError_t e = make_gemm_desc(gp.desc, op, E, P, K, Kp, Cp, V, U, Mw, m_fp32, bn);
+                      const void* U, void* Mw, bool m_fp32, int bn, int num_sms, bool m_row) {
+    cudaError_t e = make_gemm_desc(gp.desc, op, E, P, K, Kp, Cp, V, U, Mw, m_fp32, bn, m_row);
     if (e != cudaSuccess) return e;
     gp.op = op;
     gp.bn = bn;

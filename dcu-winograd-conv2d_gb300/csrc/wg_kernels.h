@@ -110,6 +110,8 @@ struct alignas(64) GemmDesc {
     CUtensorMap tmB;     // U
     void* Mw;
     int P, kg_count, m_blocks, n_blocks, k_blocks, E;
+    int m_row;           // 1: M[e][P][Kp] (rows of output channels, NHWC output path)
+    int kp;
     long long tile_begin;
     long long tiles;     // E * m_blocks * n_blocks
 };
@@ -125,15 +127,45 @@ struct GemmPlan {
 
 // Builds the tensor maps; V, U, M must stay at these addresses.
 cudaError_t make_gemm_desc(GemmDesc& d, OpType op, int E, long long P, int K, int Kp, int Cp, const void* V,
-                           const void* U, void* Mw, bool m_fp32, int bn);
+                           const void* U, void* Mw, bool m_fp32, int bn, bool m_row = false);
 cudaError_t plan_gemm(GemmPlan& gp, OpType op, int E, long long P, int K, int Kp, int Cp, const void* V,
-                      const void* U, void* Mw, bool m_fp32, int bn, int num_sms);
+                      const void* U, void* Mw, bool m_fp32, int bn, int num_sms, bool m_row = false);
 cudaError_t launch_gemm(const GemmPlan& gp, DevErr* err, cudaStream_t stream);
 // Many problems (same BN, operand and M types) in one persistent launch; descs
 // device-resident (64-byte aligned), sorted by tile_begin.
 cudaError_t launch_gemm_grouped(const GemmDesc* descs, int ndesc, long long total_tiles, OpType op, bool m_fp32, int bn,
                                 int grid, DevErr* err, cudaStream_t stream);
 int gemm_smem_bytes(int bn);
+
+// ---- NHWC (channels-last) input and output transforms ---------------------
+// Input x[N][H][W][C] fp16 through one TMA box per work item (zero fill for
+// the padding); writes the same V as launch_input_transform.
+struct alignas(64) NhwcInDesc {
+    CUtensorMap tmX;
+    void* V;
+    int C, H, W, pad_h, pad_w, tiles_h, tiles_w;
+    long long Pp;
+    int CG, tb, nbh, cb, bw, rows;
+    long long gx;         // work items along (image, tile-row block)
+    int gy;               // work items along channel blocks
+};
+// cudaErrorNotSupported when C is not a multiple of 8 (TMA strides), the
+// padded row width exceeds one TMA box (256) or two boxes do not fit in
+// shared memory.
+cudaError_t make_nhwc_in_desc(NhwcInDesc& d, const Geom& g, const void* x, void* V, int* smem);
+// images [n_base, n_base + n_images) of the tensor; V holds their tiles from 0
+cudaError_t launch_nhwc_input_transform(Xform xf, OpType op, const NhwcInDesc& d, int smem, int n_base, int n_images,
+                                        DevErr* err, cudaStream_t stream);
+// Output y[N][OH][OW][K] fp16 from row-major M[E][P][Kp] (fp32 for F(4x3)).
+struct NhwcOutDesc {
+    const void* Mw;
+    __half* out;
+    int K, Kp, OH, OW, tiles_h, tiles_w;
+    long long P;
+    int tpt, tpc;         // threads per tile, tiles per CTA
+};
+NhwcOutDesc make_nhwc_out_desc(const Geom& g, const void* Mw, void* out);
+cudaError_t launch_nhwc_output_transform(Xform xf, bool m_fp32, const NhwcOutDesc& d, cudaStream_t stream);
 
 // ---- fused F(2x3): input transform + tcgen05 GEMM + output transform ------
 struct FusedPlan {

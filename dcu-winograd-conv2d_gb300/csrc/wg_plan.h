@@ -48,6 +48,9 @@ struct Plan {
     DevErr* err = nullptr;
     GemmPlan gemm_full{}, gemm_tail{};
     FusedPlan fused{};
+    bool nhwc = false;   // channels-last input and output
+    NhwcInDesc nh_in{};
+    int nh_smem = 0;
     bool filter_ready = false;
     int launches = 0;
     unsigned info_grid = 0, info_threads = 0;

@@ -99,7 +99,9 @@ typedef struct
     long long l2_chunk_bytes; /* non-fused: process images in chunks whose V+M fit this many bytes (0 = one pass) */
     int io_bf16;         /* 1: input, filter and output tensors are bf16 (end to end); F(2x3) then uses bf16
                             operands, F(4x3) fp16 operands with per-tile scaling, both an fp32 M */
-    int reserved[3];
+    int layout_nhwc;     /* 1: input and output tensors are NHWC (channels last; filter stays KCRS);
+                            non-fused F(2x3)/F(4x3), fp16 tensors, images up to ~250 columns */
+    int reserved[2];
 } conv2d_options_t;
 
 /* reference include/conv2d.h:39-42 */

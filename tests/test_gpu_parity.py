@@ -332,3 +332,59 @@ def test_bf16_end_to_end(wg, algo, shape):
     ref = _direct64(_bf16_to_f64(xb), _bf16_to_f64(wb))
     assert O.rel_errors(got, ref)[0] <= BF16_TOL[algo]
     op.destroy()
+
+
+NHWC_SHAPES = [(2, 24, 16, 16, 32, 1), (1, 16, 13, 11, 27, 1), (3, 40, 9, 30, 36, 2), (2, 64, 28, 28, 64, 0)]
+
+
+@pytest.mark.parametrize("algo", [0, 1, 2])
+@pytest.mark.parametrize("shape", NHWC_SHAPES)
+def test_nhwc_matches_nchw_bit_for_bit(wg, algo, shape):
+    """Channels-last input and output (filter KCRS): the same V, M and output
+    arithmetic as the NCHW path, so the result is the NCHW result transposed,
+    bit for bit (the fused selection runs F(2x3) non-fused for NHWC)."""
+    n, c, h, w, k, pad = shape
+    x, wt = O.uniform_inputs(41 + algo, n, c, h, w, k)
+    y_nchw, op1 = run(wg, x, wt, pad, pad, opts_for(wg, 1 if algo == 2 else algo))
+    xt = torch.from_numpy(np.ascontiguousarray(x.transpose(0, 2, 3, 1))).cuda()
+    wtt = torch.from_numpy(wt).cuda()
+    oh, ow = h + 2 * pad - 2, w + 2 * pad - 2
+    y = torch.full((n, oh, ow, k), float("nan"), dtype=torch.float16, device="cuda")
+    prob = wg.make_problem(xt.data_ptr(), wtt.data_ptr(), y.data_ptr(), n, c, h, w, k, pad, pad)
+    op = wg.Conv2d(prob, opts_for(wg, algo, layout_nhwc=1))
+    op(torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    assert op.check_device()[0] == wg.OK
+    got = y.cpu().numpy().transpose(0, 3, 1, 2)
+    assert np.array_equal(got.view(np.uint16), y_nchw.view(np.uint16))
+    _, r64 = O.conv2d_direct(x, wt, pad, pad)
+    assert O.rel_errors(got, r64)[0] <= TOL[algo_m(algo)]
+    op.destroy()
+
+
+def test_nhwc_host_buffers_in_chunks(wg):
+    """NHWC through the host-buffer entry point, cut into 3 image chunks."""
+    n, c, h, w, k = 11, 64, 100, 100, 64
+    x, wt = O.uniform_inputs(77, n, c, h, w, k)
+    xh = np.ascontiguousarray(x.transpose(0, 2, 3, 1))
+    xt = torch.empty((n, h, w, c), dtype=torch.float16, device="cuda")
+    wtt = torch.from_numpy(wt).cuda()
+    y = torch.empty((n, h, w, k), dtype=torch.float16, device="cuda")
+    prob = wg.make_problem(xt.data_ptr(), wtt.data_ptr(), y.data_ptr(), n, c, h, w, k)
+    op = wg.Conv2d(prob, opts_for(wg, 1, layout_nhwc=1))
+    hin = torch.from_numpy(xh).pin_memory()
+    hout = torch.empty((n, h, w, k), dtype=torch.float16).pin_memory()
+    op.host(hin.data_ptr(), hout.data_ptr(), torch.cuda.current_stream().cuda_stream)
+    dev, _ = run(wg, x, wt, 1, 1, opts_for(wg, 1))
+    assert np.array_equal(hout.numpy().transpose(0, 3, 1, 2).view(np.uint16), dev.view(np.uint16))
+    op.destroy()
+
+
+def test_nhwc_refuses_channels_not_a_multiple_of_8(wg):
+    x = torch.zeros((1, 12, 12, 20), dtype=torch.float16, device="cuda")
+    w = torch.zeros((8, 20, 3, 3), dtype=torch.float16, device="cuda")
+    y = torch.zeros((1, 12, 12, 8), dtype=torch.float16, device="cuda")
+    prob = wg.make_problem(x.data_ptr(), w.data_ptr(), y.data_ptr(), 1, 20, 12, 12, 8)
+    with pytest.raises(wg.Conv2dError) as ei:
+        wg.Conv2d(prob, opts_for(wg, 1, layout_nhwc=1))
+    assert ei.value.status == wg.ERR_UNSUPPORTED
