@@ -514,11 +514,14 @@ __device__ __forceinline__ void output_body(const OutDesc& d, long long bx, int 
     }
 }
 
+// Block b = tile block * gy + granule: the granules of one block of tiles run
+// together (the 36 element planes of those tiles are read once, close in time).
 template <class TF, class MT, bool YB>
 __global__ void __launch_bounds__(kOutThreads) output_transform_kernel(const __grid_constant__ OutDesc d) {
     pdl_wait();     // M written, earlier readers of the output done
     pdl_trigger();
-    output_body<TF, MT, YB>(d, blockIdx.x, blockIdx.y);
+    const long long b = blockIdx.x;
+    output_body<TF, MT, YB>(d, b / d.gy, static_cast<int>(b % d.gy));
 }
 
 template <class TF, class MT>
@@ -533,7 +536,7 @@ __global__ void __launch_bounds__(kOutThreads) output_transform_grouped(const Ou
     }
     const OutDesc& d = descs[lo];
     const long long local = b - d.blk_begin;
-    output_body<TF, MT, false>(d, local % d.gx, static_cast<int>(local / d.gx));
+    output_body<TF, MT, false>(d, local / d.gy, static_cast<int>(local % d.gy));
 }
 
 struct InBlocking {
@@ -618,8 +621,9 @@ cudaError_t input_grouped_launch(const InDesc* descs, int ndesc, long long total
 
 template <class TF, class MT, bool YB = false>
 cudaError_t output_launch(const OutDesc& d, cudaStream_t s) {
-    return launch_pdl(output_transform_kernel<TF, MT, YB>, dim3(static_cast<unsigned>(d.gx), static_cast<unsigned>(d.gy)),
-                      dim3(kOutThreads), 0, s, d);
+    if (d.gx * d.gy > 0x7fffffffLL) return cudaErrorInvalidValue;
+    return launch_pdl(output_transform_kernel<TF, MT, YB>, dim3(static_cast<unsigned>(d.gx * d.gy)), dim3(kOutThreads), 0, s,
+                      d);
 }
 
 template <class TF, class MT>
