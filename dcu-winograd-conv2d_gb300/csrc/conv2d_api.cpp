@@ -317,7 +317,7 @@ int Plan::run_range(int n0, int nc, const GemmPlan* gp, cudaStream_t s) {
     ce = launch_gemm(*gp, err, s);
     if (ce != cudaSuccess) return cuda_fail(ce, "GEMM launch");
     mark(s);
-    ce = launch_output_transform(xf, m_fp32, gc, Mw, yout, scale, s, opt.io_bf16 != 0);
+    ce = launch_output_transform(xf, m_fp32, gc, Mw, yout, scale, err, s, opt.io_bf16 != 0);
     if (ce != cudaSuccess) return cuda_fail(ce, "output transform launch");
     mark(s);
     return CONV2D_OK;

@@ -102,7 +102,7 @@ extern "C" int conv2d_fp16_noalloc(const problem_t* problem, void* stream) {
     if (launch_filter_transform(Xform::F2, OpType::F16, problem->weight, U, g.k, g.c, g.cp, s) != cudaSuccess ||
         launch_input_transform(Xform::F2, OpType::F16, g, problem->in, x_end, V, nullptr, err, s) != cudaSuccess ||
         launch_gemm(gp, err, s) != cudaSuccess ||
-        launch_output_transform(Xform::F2, false, g, Mw, problem->out, nullptr, s) != cudaSuccess)
+        launch_output_transform(Xform::F2, false, g, Mw, problem->out, nullptr, err, s) != cudaSuccess)
         return noalloc_fail(CONV2D_ERR_CUDA, "kernel launch failed");
     return CONV2D_OK;
 }

@@ -524,6 +524,106 @@ __global__ void __launch_bounds__(kOutThreads) output_transform_kernel(const __g
     output_body<TF, MT, YB>(d, b / d.gy, static_cast<int>(b % d.gy));
 }
 
+// Persistent variant for one problem: a work item is (64 tiles, one granule);
+// warp 4 stages the item's E granule rows (E runs of up to 1 KB, contiguous
+// in M[e][g][P][.]) with cp.async.bulk into one half of a double buffer while
+// warps 0-3 transform the previous item from shared memory (thread = tile x
+// half granule, as in output_body).
+constexpr int kOsTiles = 64;
+constexpr int kOsThreads = 32 * 5;
+
+template <class TF> constexpr int os_smem_bytes() { return 128 + 2 * TF::ALPHA * TF::ALPHA * kOsTiles * 16; }
+
+template <class TF, class MT, bool YB>
+__global__ void __launch_bounds__(kOsThreads, 3)
+    output_transform_staged(const __grid_constant__ OutDesc d, long long total, DevErr* err) {
+    using YT = typename IO<YB>::T;
+    constexpr int M = TF::M, A = TF::ALPHA, E = A * A;
+    constexpr int PG = MG<MT>::kPerGranule, PH = MG<MT>::kPerHalf;
+    constexpr int kItemBytes = E * kOsTiles * 16;
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    uint64_t* full = reinterpret_cast<uint64_t*>(smem_raw);
+    uint64_t* empty = full + 2;
+    volatile int* abort_flag = reinterpret_cast<volatile int*>(full + 4);
+    unsigned char* bufs = smem_raw + 128;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < 2; ++i) {
+            mbar_init(&full[i], 32);
+            mbar_init(&empty[i], 4);
+        }
+        *abort_flag = 0;
+        fence_barrier_init();
+    }
+    pdl_wait();     // M written, earlier readers of the output done
+    pdl_trigger();
+    __syncthreads();
+    const long long P = d.P;
+    const int KG = d.KG;
+    if (warp == 4) {
+        const unsigned char* Mb = static_cast<const unsigned char*>(d.Mw);
+        int k = 0;
+        for (long long item = blockIdx.x; item < total; item += gridDim.x, ++k) {
+            const int b = k & 1;
+            if (!mbar_wait(&empty[b], ((k >> 1) & 1) ^ 1u, abort_flag, err, ERR_SITE_EMPTY)) break;
+            const long long p0 = (item / KG) * kOsTiles;
+            const int g = static_cast<int>(item % KG);
+            const uint32_t bytes = static_cast<uint32_t>(min(static_cast<long long>(kOsTiles), P - p0)) * 16u;
+            uint32_t mine = 0;
+            for (int e = lane; e < E; e += 32) mine += bytes;
+            if (mine) fence_proxy_async_smem();  // earlier reads of this buffer before the async writes
+            mbar_arrive_expect_tx(&full[b], mine);
+            for (int e = lane; e < E; e += 32)
+                bulk_g2s(bufs + b * kItemBytes + e * (kOsTiles * 16),
+                         Mb + ((static_cast<long long>(e) * KG + g) * P + p0) * 16, bytes, &full[b]);
+        }
+    } else {
+        const int t = threadIdx.x >> 1, hh = threadIdx.x & 1;
+        const int K = d.K, OH = d.OH, OW = d.OW, tiles_h = d.tiles_h, tiles_w = d.tiles_w;
+        YT* __restrict__ out = reinterpret_cast<YT*>(d.out);
+        int k = 0;
+        for (long long item = blockIdx.x; item < total; item += gridDim.x, ++k) {
+            const int b = k & 1;
+            if (!mbar_wait(&full[b], (k >> 1) & 1, abort_flag, err, ERR_SITE_FULL)) break;
+            const long long p = (item / KG) * kOsTiles + t;
+            const int g = static_cast<int>(item % KG);
+            if (p < P) {
+                const int tw = static_cast<int>(p % tiles_w);
+                const long long r = p / tiles_w;
+                const int th = static_cast<int>(r % tiles_h);
+                const long long n = r / tiles_h;
+                const int oh0 = th * M, ow0 = tw * M;
+                const int vr = min(M, OH - oh0), vc = min(M, OW - ow0);
+                const float inv = d.scale ? 1.f / d.scale[p] : 1.f;  // exact: scale is a power of two
+                const unsigned char* src = bufs + b * kItemBytes + t * 16 + hh * 8;
+                float m[E][PH];
+#pragma unroll
+                for (int e = 0; e < E; ++e) MG<MT>::load(reinterpret_cast<const MT*>(src + e * (kOsTiles * 16)), m[e]);
+#pragma unroll
+                for (int ch = 0; ch < PH; ++ch) {
+                    const int kc = g * PG + hh * PH + ch;
+                    if (kc >= K) break;
+                    float mm[E], y[M * M];
+#pragma unroll
+                    for (int e = 0; e < E; ++e) mm[e] = m[e][ch];
+                    output_tile_transform<TF>(mm, y);
+                    YT* o = out + ((n * K + kc) * OH + oh0) * static_cast<long long>(OW) + ow0;
+#pragma unroll
+                    for (int i = 0; i < M; ++i)
+                        if (i < vr) store_row<M>(o + static_cast<long long>(i) * OW, &y[i * M], vc, inv);
+                }
+            }
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&empty[b]);
+        }
+    }
+    if (*abort_flag) {
+        const unsigned long long t0 = globaltimer_ns();
+        while (globaltimer_ns() - t0 < 2000000ull) {
+        }
+    }
+}
+
 template <class TF, class MT>
 __global__ void __launch_bounds__(kOutThreads) output_transform_grouped(const OutDesc* __restrict__ descs, int ndesc) {
     pdl_wait();
@@ -620,10 +720,16 @@ cudaError_t input_grouped_launch(const InDesc* descs, int ndesc, long long total
 }
 
 template <class TF, class MT, bool YB = false>
-cudaError_t output_launch(const OutDesc& d, cudaStream_t s) {
-    if (d.gx * d.gy > 0x7fffffffLL) return cudaErrorInvalidValue;
-    return launch_pdl(output_transform_kernel<TF, MT, YB>, dim3(static_cast<unsigned>(d.gx * d.gy)), dim3(kOutThreads), 0, s,
-                      d);
+cudaError_t output_launch(const OutDesc& d, DevErr* err, cudaStream_t s) {
+    const long long total = (d.P + kOsTiles - 1) / kOsTiles * d.KG;
+    if (total <= 0) return cudaSuccess;
+    auto kern = output_transform_staged<TF, MT, YB>;
+    constexpr int smem = os_smem_bytes<TF>();
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return e;
+    const int per_sm = std::max(1, std::min(4, 233472 / (smem + 1024)));
+    const long long grid = std::min<long long>(total, static_cast<long long>(sm_count()) * per_sm);
+    return launch_pdl(kern, dim3(static_cast<unsigned>(grid)), dim3(kOsThreads), smem, s, d, total, err);
 }
 
 template <class TF, class MT>
@@ -773,24 +879,24 @@ cudaError_t launch_input_transform_grouped(Xform xf, OpType op, const InDesc* de
 }
 
 cudaError_t launch_output_transform(Xform xf, bool m_fp32, const Geom& g, const void* Mw, void* out,
-                                    const float* scale, cudaStream_t stream, bool y_bf16) {
+                                    const float* scale, DevErr* err, cudaStream_t stream, bool y_bf16) {
     const OutDesc d = make_out_desc(g, m_fp32, Mw, out, scale);
     if (y_bf16) {  // bf16 tensors: M is fp32 for both transforms
         if (!m_fp32) return cudaErrorNotSupported;
         switch (xf) {
-            case Xform::F2: return output_launch<F2, float, true>(d, stream);
-            case Xform::F4: return output_launch<F4, float, true>(d, stream);
-            case Xform::F4Ref: return output_launch<F4Ref, float, true>(d, stream);
+            case Xform::F2: return output_launch<F2, float, true>(d, err, stream);
+            case Xform::F4: return output_launch<F4, float, true>(d, err, stream);
+            case Xform::F4Ref: return output_launch<F4Ref, float, true>(d, err, stream);
         }
         return cudaErrorInvalidValue;
     }
     switch (xf) {
         case Xform::F2:
-            return m_fp32 ? output_launch<F2, float>(d, stream) : output_launch<F2, __half>(d, stream);
+            return m_fp32 ? output_launch<F2, float>(d, err, stream) : output_launch<F2, __half>(d, err, stream);
         case Xform::F4:
-            return m_fp32 ? output_launch<F4, float>(d, stream) : output_launch<F4, __half>(d, stream);
+            return m_fp32 ? output_launch<F4, float>(d, err, stream) : output_launch<F4, __half>(d, err, stream);
         case Xform::F4Ref:
-            return m_fp32 ? output_launch<F4Ref, float>(d, stream) : output_launch<F4Ref, __half>(d, stream);
+            return m_fp32 ? output_launch<F4Ref, float>(d, err, stream) : output_launch<F4Ref, __half>(d, err, stream);
     }
     return cudaErrorInvalidValue;
 }

@@ -99,7 +99,7 @@ cudaError_t launch_output_transform_grouped(Xform xf, bool m_fp32, const OutDesc
 // out[N][K][OH][OW] = A^T M A from M[e][Kp/8][P][8] (fp16, m_fp32 false) or
 // M[e][Kp/4][P][4] (fp32); divides by scale[p] when scale is not null.
 cudaError_t launch_output_transform(Xform xf, bool m_fp32, const Geom& g, const void* Mw, void* out,
-                                    const float* scale, cudaStream_t stream, bool y_bf16 = false);
+                                    const float* scale, DevErr* err, cudaStream_t stream, bool y_bf16 = false);
 
 // ---- tcgen05 batched GEMM: M_e[P][K] = V_e[P][Cp] * U_e[K][Cp]^T -----------
 // (operands and result in the 16-byte granule layouts above)
