@@ -81,7 +81,7 @@ struct Batch {
             if ((e = launch_gemm_grouped(g.descs, g.n, g.tiles, g.op, g.m_fp32, g.bn, g.grid, err, s)) != cudaSuccess)
                 return e;
         for (const OutGroup& g : out_groups)
-            if ((e = launch_output_transform_grouped(g.xf, g.m_fp32, g.descs, g.n, g.blocks, s)) != cudaSuccess) return e;
+            if ((e = launch_output_transform_grouped(g.xf, g.m_fp32, g.descs, g.n, g.blocks, err, s)) != cudaSuccess) return e;
         for (int i : fused) {
             Plan& p = *plans[i];
             const void* x_end =

@@ -271,10 +271,10 @@ struct Server {
                                         g.bn, static_cast<int>(std::min<long long>(g.tiles, num_sms)), err, s);
         if (!out2.empty() && e == cudaSuccess)
             e = launch_output_transform_grouped(Xform::F2, false, reinterpret_cast<const OutDesc*>(d + o_out2),
-                                                static_cast<int>(out2.size()), blk_out2, s);
+                                                static_cast<int>(out2.size()), blk_out2, err, s);
         if (!out4.empty() && e == cudaSuccess)
             e = launch_output_transform_grouped(Xform::F4, true, reinterpret_cast<const OutDesc*>(d + o_out4),
-                                                static_cast<int>(out4.size()), blk_out4, s);
+                                                static_cast<int>(out4.size()), blk_out4, err, s);
         if (e == cudaSuccess) e = cudaEventRecord(slot.done, s);
         if (e != cudaSuccess) return set_last_error(CONV2D_ERR_CUDA, cudaGetErrorString(e));
         return CONV2D_OK;

@@ -432,10 +432,6 @@ __global__ void __launch_bounds__(kInThreads, 2) input_transform_grouped(const I
 }
 
 // ---- output transform ----------------------------------------------------------
-// One thread per (tile, 16-byte granule of M); lanes over consecutive tiles,
-// so both the M reads and the NCHW row writes of a warp are contiguous.
-
-constexpr int kOutThreads = 128;
 
 template <class MT> struct MG;  // 8-byte half granule: 4 fp16 or 2 fp32 channels
 template <> struct MG<__half> {
@@ -471,72 +467,32 @@ __device__ __forceinline__ void store_row(YT* dst, const float* y, int valid, fl
     }
 }
 
-template <class TF, class MT, bool YB>
-__device__ __forceinline__ void output_body(const OutDesc& d, long long bx, int g) {
-    using YT = typename IO<YB>::T;
-    constexpr int M = TF::M, A = TF::ALPHA;
-    constexpr int PG = MG<MT>::kPerGranule, PH = MG<MT>::kPerHalf;
-    const MT* __restrict__ Mw = static_cast<const MT*>(d.Mw);
-    YT* __restrict__ out = reinterpret_cast<YT*>(d.out);
-    const float* __restrict__ scale = d.scale;
-    const int K = d.K, OH = d.OH, OW = d.OW, tiles_h = d.tiles_h, tiles_w = d.tiles_w, KG = d.KG;
-    const long long P = d.P;
-    // thread = (tile, half granule): two consecutive lanes read the two halves
-    // of one 16-byte granule row, so a warp reads 256 contiguous bytes
-    const long long task = bx * kOutThreads + threadIdx.x;
-    const int hh = static_cast<int>(task & 1);
-    const long long p = task >> 1;
-    if (p >= P) return;
-    const int tw = static_cast<int>(p % tiles_w);
-    const long long r = p / tiles_w;
-    const int th = static_cast<int>(r % tiles_h);
-    const long long n = r / tiles_h;
-    const int oh0 = th * M, ow0 = tw * M;
-    const int vr = min(M, OH - oh0), vc = min(M, OW - ow0);
-    const float inv = scale ? 1.f / scale[p] : 1.f;  // exact: scale is a power of two
-    const MT* src = Mw + (static_cast<long long>(g) * P + p) * PG + hh * PH;
-    const long long estride = static_cast<long long>(KG) * P * PG;
-    float m[A * A][PH];
-#pragma unroll
-    for (int e = 0; e < A * A; ++e) MG<MT>::load(src + e * estride, m[e]);
-#pragma unroll
-    for (int ch = 0; ch < PH; ++ch) {
-        const int k = g * PG + hh * PH + ch;
-        if (k >= K) break;
-        float mm[A * A], y[M * M];
-#pragma unroll
-        for (int e = 0; e < A * A; ++e) mm[e] = m[e][ch];
-        output_tile_transform<TF>(mm, y);
-        YT* o = out + ((n * K + k) * OH + oh0) * static_cast<long long>(OW) + ow0;
-#pragma unroll
-        for (int i = 0; i < M; ++i)
-            if (i < vr) store_row<M>(o + static_cast<long long>(i) * OW, &y[i * M], vc, inv);
-    }
-}
-
-// Block b = tile block * gy + granule: the granules of one block of tiles run
-// together (the 36 element planes of those tiles are read once, close in time).
-template <class TF, class MT, bool YB>
-__global__ void __launch_bounds__(kOutThreads) output_transform_kernel(const __grid_constant__ OutDesc d) {
-    pdl_wait();     // M written, earlier readers of the output done
-    pdl_trigger();
-    const long long b = blockIdx.x;
-    output_body<TF, MT, YB>(d, b / d.gy, static_cast<int>(b % d.gy));
-}
-
-// Persistent variant for one problem: a work item is (64 tiles, one granule);
-// warp 4 stages the item's E granule rows (E runs of up to 1 KB, contiguous
-// in M[e][g][P][.]) with cp.async.bulk into one half of a double buffer while
-// warps 0-3 transform the previous item from shared memory (thread = tile x
-// half granule, as in output_body).
+// Persistent CTAs; a work item is (64 tiles, one granule); warp 4 stages the
+// item's E granule rows (E runs of up to 1 KB, contiguous in M[e][g][P][.])
+// with cp.async.bulk into one half of a double buffer while warps 0-3
+// transform the previous item from shared memory: thread = (tile, half
+// granule), so two lanes read the two halves of one 16-byte row and a warp
+// reads 256 contiguous bytes of shared memory per element, and the NCHW row
+// writes of a warp are contiguous across tiles.
 constexpr int kOsTiles = 64;
 constexpr int kOsThreads = 32 * 5;
 
 template <class TF> constexpr int os_smem_bytes() { return 128 + 2 * TF::ALPHA * TF::ALPHA * kOsTiles * 16; }
 
+// Problem of a work item (descriptors sorted by blk_begin).
+__device__ __forceinline__ const OutDesc& out_desc_of(const OutDesc* descs, int ndesc, long long item) {
+    int lo = 0, hi = ndesc - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) / 2;
+        if (descs[mid].blk_begin <= item) lo = mid; else hi = mid - 1;
+    }
+    return descs[lo];
+}
+
+// descs: one problem (kernel parameter) or many (device array sorted by
+// blk_begin, items = ceil(P/64) * KG per problem, granule fastest).
 template <class TF, class MT, bool YB>
-__global__ void __launch_bounds__(kOsThreads, 3)
-    output_transform_staged(const __grid_constant__ OutDesc d, long long total, DevErr* err) {
+__device__ __forceinline__ void output_staged_body(const OutDesc* descs, int ndesc, long long total, DevErr* err) {
     using YT = typename IO<YB>::T;
     constexpr int M = TF::M, A = TF::ALPHA, E = A * A;
     constexpr int PG = MG<MT>::kPerGranule, PH = MG<MT>::kPerHalf;
@@ -558,14 +514,16 @@ __global__ void __launch_bounds__(kOsThreads, 3)
     pdl_wait();     // M written, earlier readers of the output done
     pdl_trigger();
     __syncthreads();
-    const long long P = d.P;
-    const int KG = d.KG;
     if (warp == 4) {
-        const unsigned char* Mb = static_cast<const unsigned char*>(d.Mw);
         int k = 0;
-        for (long long item = blockIdx.x; item < total; item += gridDim.x, ++k) {
+        for (long long gitem = blockIdx.x; gitem < total; gitem += gridDim.x, ++k) {
             const int b = k & 1;
             if (!mbar_wait(&empty[b], ((k >> 1) & 1) ^ 1u, abort_flag, err, ERR_SITE_EMPTY)) break;
+            const OutDesc& d = out_desc_of(descs, ndesc, gitem);
+            const long long item = gitem - d.blk_begin;
+            const long long P = d.P;
+            const int KG = d.KG;
+            const unsigned char* Mb = static_cast<const unsigned char*>(d.Mw);
             const long long p0 = (item / KG) * kOsTiles;
             const int g = static_cast<int>(item % KG);
             const uint32_t bytes = static_cast<uint32_t>(min(static_cast<long long>(kOsTiles), P - p0)) * 16u;
@@ -579,12 +537,16 @@ __global__ void __launch_bounds__(kOsThreads, 3)
         }
     } else {
         const int t = threadIdx.x >> 1, hh = threadIdx.x & 1;
-        const int K = d.K, OH = d.OH, OW = d.OW, tiles_h = d.tiles_h, tiles_w = d.tiles_w;
-        YT* __restrict__ out = reinterpret_cast<YT*>(d.out);
         int k = 0;
-        for (long long item = blockIdx.x; item < total; item += gridDim.x, ++k) {
+        for (long long gitem = blockIdx.x; gitem < total; gitem += gridDim.x, ++k) {
             const int b = k & 1;
             if (!mbar_wait(&full[b], (k >> 1) & 1, abort_flag, err, ERR_SITE_FULL)) break;
+            const OutDesc& d = out_desc_of(descs, ndesc, gitem);
+            const long long item = gitem - d.blk_begin;
+            const long long P = d.P;
+            const int KG = d.KG;
+            const int K = d.K, OH = d.OH, OW = d.OW, tiles_h = d.tiles_h, tiles_w = d.tiles_w;
+            YT* __restrict__ out = reinterpret_cast<YT*>(d.out);
             const long long p = (item / KG) * kOsTiles + t;
             const int g = static_cast<int>(item % KG);
             if (p < P) {
@@ -624,20 +586,18 @@ __global__ void __launch_bounds__(kOsThreads, 3)
     }
 }
 
-template <class TF, class MT>
-__global__ void __launch_bounds__(kOutThreads) output_transform_grouped(const OutDesc* __restrict__ descs, int ndesc) {
-    pdl_wait();
-    pdl_trigger();
-    const long long b = blockIdx.x;
-    int lo = 0, hi = ndesc - 1;
-    while (lo < hi) {
-        const int mid = (lo + hi + 1) / 2;
-        if (descs[mid].blk_begin <= b) lo = mid; else hi = mid - 1;
-    }
-    const OutDesc& d = descs[lo];
-    const long long local = b - d.blk_begin;
-    output_body<TF, MT, false>(d, local / d.gy, static_cast<int>(local % d.gy));
+template <class TF, class MT, bool YB>
+__global__ void __launch_bounds__(kOsThreads, 3)
+    output_transform_staged(const __grid_constant__ OutDesc d, long long total, DevErr* err) {
+    output_staged_body<TF, MT, YB>(&d, 1, total, err);
 }
+
+template <class TF, class MT>
+__global__ void __launch_bounds__(kOsThreads, 3)
+    output_transform_staged_grouped(const OutDesc* __restrict__ descs, int ndesc, long long total, DevErr* err) {
+    output_staged_body<TF, MT, false>(descs, ndesc, total, err);
+}
+
 
 struct InBlocking {
     int tb, nbh, cb, stride, buf;
@@ -733,9 +693,15 @@ cudaError_t output_launch(const OutDesc& d, DevErr* err, cudaStream_t s) {
 }
 
 template <class TF, class MT>
-cudaError_t output_grouped_launch(const OutDesc* descs, int ndesc, long long blocks, cudaStream_t s) {
-    return launch_pdl(output_transform_grouped<TF, MT>, dim3(static_cast<unsigned>(blocks)), dim3(kOutThreads), 0, s,
-                      descs, ndesc);
+cudaError_t output_grouped_launch(const OutDesc* descs, int ndesc, long long blocks, DevErr* err, cudaStream_t s) {
+    if (blocks <= 0) return cudaSuccess;
+    auto kern = output_transform_staged_grouped<TF, MT>;
+    constexpr int smem = os_smem_bytes<TF>();
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return e;
+    const int per_sm = std::max(1, std::min(4, 233472 / (smem + 1024)));
+    const long long grid = std::min<long long>(blocks, static_cast<long long>(sm_count()) * per_sm);
+    return launch_pdl(kern, dim3(static_cast<unsigned>(grid)), dim3(kOsThreads), smem, s, descs, ndesc, blocks, err);
 }
 
 template <class TF, class OutT>
@@ -816,7 +782,7 @@ OutDesc make_out_desc(const Geom& g, bool m_fp32, const void* Mw, void* out, con
     d.K = g.k; d.OH = g.oh; d.OW = g.ow; d.tiles_h = g.tiles_h; d.tiles_w = g.tiles_w;
     d.P = g.P;
     d.KG = m_fp32 ? g.kp / 4 : g.kp / 8;
-    d.gx = (2 * g.P + kOutThreads - 1) / kOutThreads;
+    d.gx = (g.P + kOsTiles - 1) / kOsTiles;
     d.gy = d.KG;
     d.blk_begin = 0;
     return d;
@@ -902,17 +868,17 @@ cudaError_t launch_output_transform(Xform xf, bool m_fp32, const Geom& g, const 
 }
 
 cudaError_t launch_output_transform_grouped(Xform xf, bool m_fp32, const OutDesc* descs, int ndesc, long long blocks,
-                                            cudaStream_t stream) {
+                                            DevErr* err, cudaStream_t stream) {
     switch (xf) {
         case Xform::F2:
-            return m_fp32 ? output_grouped_launch<F2, float>(descs, ndesc, blocks, stream)
-                          : output_grouped_launch<F2, __half>(descs, ndesc, blocks, stream);
+            return m_fp32 ? output_grouped_launch<F2, float>(descs, ndesc, blocks, err, stream)
+                          : output_grouped_launch<F2, __half>(descs, ndesc, blocks, err, stream);
         case Xform::F4:
-            return m_fp32 ? output_grouped_launch<F4, float>(descs, ndesc, blocks, stream)
-                          : output_grouped_launch<F4, __half>(descs, ndesc, blocks, stream);
+            return m_fp32 ? output_grouped_launch<F4, float>(descs, ndesc, blocks, err, stream)
+                          : output_grouped_launch<F4, __half>(descs, ndesc, blocks, err, stream);
         case Xform::F4Ref:
-            return m_fp32 ? output_grouped_launch<F4Ref, float>(descs, ndesc, blocks, stream)
-                          : output_grouped_launch<F4Ref, __half>(descs, ndesc, blocks, stream);
+            return m_fp32 ? output_grouped_launch<F4Ref, float>(descs, ndesc, blocks, err, stream)
+                          : output_grouped_launch<F4Ref, __half>(descs, ndesc, blocks, err, stream);
     }
     return cudaErrorInvalidValue;
 }

@@ -79,8 +79,8 @@ struct OutDesc {
     int K, OH, OW, tiles_h, tiles_w;
     long long P;
     int KG;
-    long long gx;         // CTAs along tiles
-    int gy;               // CTAs along granules
+    long long gx;         // work items along blocks of 64 tiles
+    int gy;               // work items along granules
     long long blk_begin;
 };
 
@@ -94,7 +94,7 @@ OutDesc make_out_desc(const Geom& g, bool m_fp32, const void* Mw, void* out, con
 cudaError_t launch_input_transform_grouped(Xform xf, OpType op, const InDesc* descs, int ndesc, long long blocks,
                                            int smem, bool scaled, DevErr* err, cudaStream_t stream);
 cudaError_t launch_output_transform_grouped(Xform xf, bool m_fp32, const OutDesc* descs, int ndesc, long long blocks,
-                                            cudaStream_t stream);
+                                            DevErr* err, cudaStream_t stream);
 
 // out[N][K][OH][OW] = A^T M A from M[e][Kp/8][P][8] (fp16, m_fp32 false) or
 // M[e][Kp/4][P][4] (fp32); divides by scale[p] when scale is not null.
