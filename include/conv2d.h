@@ -14,9 +14,11 @@
  *
  * All tensor pointers are DEVICE pointers to IEEE binary16 data (the
  * reference's _Float16*, ABI-identical to void*).  Input NCHW, weights KCRS,
- * output N K Oh Ow.  Supported: r = s = 3, u = v = 1, any p, q with a
- * positive output size.  Unsupported descriptors are rejected with a status
- * code (the reference computes garbage for them).
+ * output N K Oh Ow (options: bf16 tensors, channels-last input/output).
+ * Supported: r = s = 3, u = v = 1, padding p, q up to 64 with a positive
+ * output size, dimensions up to 65535, image rows that fit the staged input
+ * transform (about 1,200 columns for F(4x3)).  Unsupported descriptors are
+ * rejected with a status code (the reference computes garbage for them).
  *
  * The reference exports getParamsize/getkernelInfo with C++ linkage; this
  * library exports them both with C linkage (declared here) and with the
