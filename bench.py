@@ -14,7 +14,7 @@ Buffer sets rotate so the bytes touched between two uses of one set exceed
 the 129 MB L2.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload cfg2|cfg1|cfg3|...] [--algo ref|fused|2x3|4x3]
+                    [--workload cfg2|cfg1|cfg3|...] [--algo ref|fused|2x3|4x3|row|auto]
 """
 from __future__ import annotations
 
@@ -56,7 +56,7 @@ WORKLOADS = {
 }
 # reference latencies read from its published chart (Hygon DCU gfx928), microseconds
 PUBLISHED_US = {"final1": 207, "final2": 367, "final3": 724, "final4": 654, "final5": 593, "final6": 133}
-ALGO_ARG = {"ref": -1, "4x3": 0, "2x3": 1, "fused": 2, "auto": 3}
+ALGO_ARG = {"ref": -1, "4x3": 0, "2x3": 1, "fused": 2, "auto": 3, "row": 4}
 SERVE_WORKLOADS = {
     "cfg5": "serving: 16 resident 3x3 pad-1 layers (C,K in {64..512}, H=W in {7..112}), N ~ U{1..64}, "
             "Poisson arrivals swept over multiples of the plain per-request capacity, 40 GiB workspace budget",
@@ -293,6 +293,8 @@ def roofline_for(name, wg, geo, ms, pk, pk_kind):
       gemm_tcgen05      V read (2*E*P*C) + U read (2*E*C*K) + M write (E*P*K*4 or *2)
       output_transform  M read + y write (2*N*K*OH*OW)
       fused2x3          x read + U read + y write
+      row4x3            x read + U1 read (2*18*C*K) + y write; tensor work
+                        2*18*RT*C*K over RT = N*OH*ceil(OW/4) row tiles
     """
     n, c, h, w, k, m = geo
     oh, ow = h, w  # pad 1
@@ -306,6 +308,9 @@ def roofline_for(name, wg, geo, ms, pk, pk_kind):
         flops, byts, formula = 2.0 * E * tiles * c * k, v_b + u_b + m_b, "V + U + M"
     elif name == "fused2x3":
         flops, byts, formula = 2.0 * E * tiles * c * k, x_b + u_b + y_b, "x + U + y"
+    elif name == "row4x3":
+        rt = n * oh * math.ceil(ow / 4)
+        flops, byts, formula = 2.0 * 18 * rt * c * k, x_b + 2.0 * 18 * c * k + y_b, "x + U1 + y"
     elif name == "input_transform":
         byts, formula = x_b + v_b, "x + V"
     else:
@@ -321,7 +326,8 @@ def roofline_for(name, wg, geo, ms, pk, pk_kind):
         out.update({"bound": "hbm", "achieved": ach, "peak": peak_bw, "unit": "GB/s", "frac": ach / peak_bw,
                     "peak_source": f"{pk_kind} HBM copy"})
     out["algorithmic_per_launch"] = f"{byts / 1e6:.1f} MB ({formula})" + (
-        f", {flops / 1e9:.2f} GFLOP (2*{E}*P*C*K)" if flops else "")
+        (f", {flops / 1e9:.2f} GFLOP (2*18*RT*C*K)" if name == "row4x3" else f", {flops / 1e9:.2f} GFLOP (2*{E}*P*C*K)")
+        if flops else "")
     out["algorithmic_bytes"] = byts
     if flops:
         out["tensor_frac"] = flops / (ms * 1e-3) / 1e12 / peak_fl
@@ -428,7 +434,7 @@ def our_arm(args):
     dominant = max(tot, key=tot.get)
     launches_of_dom = len(kt[dominant])
     dom_ms = tot[dominant] / launches_of_dom
-    m = 4 if algo == wg.ALGO_4X3 else 2
+    m = 4 if algo in (wg.ALGO_4X3, wg.ALGO_4X3_ROW) else 2
     pk, pk_kind = peaks()
     roof = roofline_for(dominant, wg, (n, c, h, w, k, m), dom_ms, pk, pk_kind)
     traffic = committed_traffic(dominant, args.workload)

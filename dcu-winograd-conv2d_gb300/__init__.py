@@ -18,8 +18,9 @@ LIB_PATH = os.path.join(HERE, "_build", "libwgconv.so")
 
 # status codes and algorithms (include/conv2d.h)
 OK, ERR_INVALID, ERR_UNSUPPORTED, ERR_NOMEM, ERR_CUDA, ERR_TIMEOUT, ERR_BUSY = range(7)
-ALGO_REFERENCE, ALGO_4X3, ALGO_2X3, ALGO_2X3_FUSED, ALGO_AUTO = -1, 0, 1, 2, 3
-ALGO_NAMES = {ALGO_4X3: "F(4x3) non-fused", ALGO_2X3: "F(2x3) non-fused", ALGO_2X3_FUSED: "F(2x3) fused"}
+ALGO_REFERENCE, ALGO_4X3, ALGO_2X3, ALGO_2X3_FUSED, ALGO_AUTO, ALGO_4X3_ROW = -1, 0, 1, 2, 3, 4
+ALGO_NAMES = {ALGO_4X3: "F(4x3) non-fused", ALGO_2X3: "F(2x3) non-fused", ALGO_2X3_FUSED: "F(2x3) fused",
+              ALGO_4X3_ROW: "row F(4x3) fused"}
 
 
 class Problem(ctypes.Structure):
@@ -197,6 +198,8 @@ class Conv2d:
         """Kernels launched by one call, in launch order."""
         if self.algo == ALGO_2X3_FUSED:
             return ["fused2x3"]
+        if self.algo == ALGO_4X3_ROW:
+            return ["row4x3"]
         per = (["tile_scale"] if self.scaling else []) + ["input_transform", "gemm_tcgen05", "output_transform"]
         return per * (self.launches_per_call // len(per))
 

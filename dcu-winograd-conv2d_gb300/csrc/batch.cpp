@@ -86,7 +86,10 @@ struct Batch {
             Plan& p = *plans[i];
             const void* x_end =
                 static_cast<const uint16_t*>(p.prob.in) + static_cast<long long>(p.prob.n) * p.g.c * p.g.h * p.g.w;
-            if ((e = launch_fused2x3(p.fused, p.g, p.prob.in, x_end, p.prob.out, err, s)) != cudaSuccess) return e;
+            e = p.algo == CONV2D_ALGO_4X3_ROW
+                    ? launch_row4x3(p.row, p.prob.in, x_end, p.prob.out, static_cast<int>(p.prob.n), err, s)
+                    : launch_fused2x3(p.fused, p.g, p.prob.in, x_end, p.prob.out, err, s);
+            if (e != cudaSuccess) return e;
         }
         return cudaSuccess;
     }
@@ -122,7 +125,7 @@ int batch_create(const problem_t* problems, int count, const conv2d_options_t* o
     std::map<std::tuple<int, int, int>, std::vector<int>> gemm_keys;          // (bn, m_fp32, op) -> problems
     for (int i = 0; i < count; ++i) {
         Plan& p = *b->plans[i];
-        if (p.algo == CONV2D_ALGO_2X3_FUSED) {
+        if (p.single_kernel()) {
             b->fused.push_back(i);
             continue;
         }
@@ -286,7 +289,7 @@ int conv2d_batch_info(const conv2d_batch_t* batch, int index, int* algo, int* ge
     if (!b || index < 0 || index >= static_cast<int>(b->plans.size())) return set_last_error(CONV2D_ERR_INVALID, "bad index");
     const Plan& p = *b->plans[index];
     if (algo) *algo = p.algo;
-    if (gemm_bn) *gemm_bn = p.algo == CONV2D_ALGO_2X3_FUSED ? 32 : p.gemm_full.bn;
+    if (gemm_bn) *gemm_bn = p.algo == CONV2D_ALGO_2X3_FUSED ? 32 : p.algo == CONV2D_ALGO_4X3_ROW ? 64 : p.gemm_full.bn;
     return CONV2D_OK;
 }
 

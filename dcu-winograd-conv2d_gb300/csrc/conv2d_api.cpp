@@ -161,7 +161,7 @@ int Plan::build(const problem_t* pr, const conv2d_options_t* opt_in) {
         algo = a;
         if (bn) opt.gemm_bn = bn;
     }
-    if (algo < 0 || algo > 2) return fail(CONV2D_ERR_INVALID, "bad algorithm");
+    if (algo < 0 || (algo > 2 && algo != CONV2D_ALGO_4X3_ROW)) return fail(CONV2D_ERR_INVALID, "bad algorithm");
 
     op = opt.operand_bf16 ? OpType::BF16 : OpType::F16;
     nhwc = opt.layout_nhwc != 0;
@@ -178,18 +178,28 @@ int Plan::build(const problem_t* pr, const conv2d_options_t* opt_in) {
         if (plan_fused2x3(probe, op, g2, nullptr) == cudaErrorNotSupported) algo = CONV2D_ALGO_2X3_NON_FUSED;
         cudaGetLastError();
     }
-    const int m = algo == CONV2D_ALGO_4X3_NON_FUSED ? 4 : 2;
+    if (algo == CONV2D_ALGO_4X3_ROW) {
+        // fp16 NCHW tensors and operands with the {0, +-1, 1/2, -2} points only,
+        // and the staged rows of one output-row block must fit in shared memory;
+        // otherwise F(4x3) runs non-fused
+        const Geom g4 = make_geom(pr->n, pr->c, pr->h, pr->w, pr->k, pr->p, pr->q, 4);
+        if (nhwc || opt.io_bf16 || opt.operand_bf16 || opt.tile_scaling || opt.f4_points ||
+            plan_row4x3(row, g4, nullptr) != cudaSuccess)
+            algo = CONV2D_ALGO_4X3_NON_FUSED;
+        cudaGetLastError();
+    }
+    const int m = (algo == CONV2D_ALGO_4X3_NON_FUSED || algo == CONV2D_ALGO_4X3_ROW) ? 4 : 2;
     xf = m == 2 ? Xform::F2 : (opt.f4_points ? Xform::F4Ref : Xform::F4);
     // bf16 tensors: bf16 operands for F(2x3) (sums of +-1 multiples stay in
     // range), fp16 operands with per-tile scaling for F(4x3) (bf16 operands
     // lose ~10x accuracy there); M in fp32 either way
     if (opt.io_bf16) op = m == 2 ? OpType::BF16 : OpType::F16;
-    m_fp32 = (m == 4) || opt.io_bf16;
-    scaling = (m == 4) && (opt.tile_scaling || opt.io_bf16);
+    m_fp32 = ((m == 4) || opt.io_bf16) && algo != CONV2D_ALGO_4X3_ROW;
+    scaling = (m == 4) && (opt.tile_scaling || opt.io_bf16) && algo != CONV2D_ALGO_4X3_ROW;
     g = make_geom(pr->n, pr->c, pr->h, pr->w, pr->k, pr->p, pr->q, m);
     const int E = g.alpha * g.alpha;
     const long long op_bytes = 2;
-    if (algo != CONV2D_ALGO_2X3_FUSED && !nhwc) {
+    if (!single_kernel() && !nhwc) {
         // the input transform stages whole input rows of 8 channels, twice
         int in_smem = 0;
         make_in_desc(g, pr->in, pr->in, nullptr, nullptr, &in_smem);
@@ -198,7 +208,7 @@ int Plan::build(const problem_t* pr, const conv2d_options_t* opt_in) {
 
     // image chunking keeps V and M of one chunk L2-resident between kernels
     chunk_n = static_cast<int>(pr->n);
-    if (algo != CONV2D_ALGO_2X3_FUSED && opt.l2_chunk_bytes > 0) {
+    if (!single_kernel() && opt.l2_chunk_bytes > 0) {
         const long long per_img = static_cast<long long>(E) * g.tiles_h * g.tiles_w *
                                   (g.cp * op_bytes + g.kp * (m_fp32 ? 4LL : 2LL));
         chunk_n = static_cast<int>(std::max(1LL, std::min<long long>(pr->n, opt.l2_chunk_bytes / std::max(1LL, per_img))));
@@ -207,9 +217,10 @@ int Plan::build(const problem_t* pr, const conv2d_options_t* opt_in) {
 
     // one workspace: U | V | M | scale | device error word (256-byte aligned parts)
     auto al = [](long long b) { return (b + 255) / 256 * 256; };
-    const long long bU = al(static_cast<long long>(E) * g.kp * g.cp * op_bytes);
+    u_bytes = algo == CONV2D_ALGO_4X3_ROW ? row4x3_filter_bytes(row) : static_cast<long long>(E) * g.kp * g.cp * op_bytes;
+    const long long bU = al(u_bytes);
     long long bV = 0, bM = 0, bS = 0;
-    if (algo != CONV2D_ALGO_2X3_FUSED) {
+    if (!single_kernel()) {
         bV = al(static_cast<long long>(E) * round_rows(Pc) * g.cp * op_bytes);
         bM = al(static_cast<long long>(E) * Pc * g.kp * (m_fp32 ? 4 : 2));
         if (scaling) bS = al(Pc * 4);
@@ -239,6 +250,13 @@ int Plan::build(const problem_t* pr, const conv2d_options_t* opt_in) {
         info_grid = static_cast<unsigned>(fused.m_blocks * fused.n_blocks);
         info_threads = 320;
         info_smem = fused.smem_bytes;
+    } else if (algo == CONV2D_ALGO_4X3_ROW) {
+        ce = plan_row4x3(row, g, U);
+        if (ce != cudaSuccess) return cuda_fail(ce, "row F(4x3) plan");
+        launches = 1;
+        info_grid = static_cast<unsigned>(std::min<long long>(row4x3_items(row, static_cast<int>(pr->n)), num_sms));
+        info_threads = 320;
+        info_smem = row.smem_bytes;
     } else {
         if (nhwc) {
             ce = make_nhwc_in_desc(nh_in, g, pr->in, V, &nh_smem);
@@ -268,7 +286,9 @@ int Plan::build(const problem_t* pr, const conv2d_options_t* opt_in) {
 }
 
 int Plan::filter(cudaStream_t s) {
-    cudaError_t ce = launch_filter_transform(xf, op, prob.weight, U, g.k, g.c, g.cp, s, opt.io_bf16 != 0);
+    cudaError_t ce = algo == CONV2D_ALGO_4X3_ROW
+                         ? launch_row4x3_filter(row, prob.weight, U, s)
+                         : launch_filter_transform(xf, op, prob.weight, U, g.k, g.c, g.cp, s, opt.io_bf16 != 0);
     if (ce != cudaSuccess) return cuda_fail(ce, "filter transform launch");
     filter_ready = true;
     return CONV2D_OK;
@@ -289,6 +309,12 @@ int Plan::run_range(int n0, int nc, const GemmPlan* gp, cudaStream_t s) {
     if (algo == CONV2D_ALGO_2X3_FUSED) {
         ce = launch_fused2x3(fused, gc, xin, x_end, yout, err, s);
         if (ce != cudaSuccess) return cuda_fail(ce, "fused F(2x3) launch");
+        mark(s);
+        return CONV2D_OK;
+    }
+    if (algo == CONV2D_ALGO_4X3_ROW) {
+        ce = launch_row4x3(row, xin, x_end, yout, nc, err, s);
+        if (ce != cudaSuccess) return cuda_fail(ce, "row F(4x3) launch");
         mark(s);
         return CONV2D_OK;
     }
@@ -330,7 +356,7 @@ int Plan::run(cudaStream_t s) {
         int st = filter(s);
         if (st) return st;
     }
-    if (algo == CONV2D_ALGO_2X3_FUSED) return run_range(0, static_cast<int>(prob.n), nullptr, s);
+    if (single_kernel()) return run_range(0, static_cast<int>(prob.n), nullptr, s);
     for (int ci = 0; ci < n_chunks; ++ci) {
         const int n0 = ci * chunk_n;
         const int nc = std::min<int>(chunk_n, static_cast<int>(prob.n) - n0);
@@ -372,7 +398,7 @@ int Plan::run_host(const void* host_in, void* host_out, cudaStream_t s) {
             if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess)
                 return fail(CONV2D_ERR_CUDA, "event creation failed");
     }
-    if (algo != CONV2D_ALGO_2X3_FUSED && host_chunk_n != hc) {
+    if (!single_kernel() && host_chunk_n != hc) {
         const int E = g.alpha * g.alpha;
         const int bn = gemm_full.bn;
         const int tail = n - (nch - 1) * hc;

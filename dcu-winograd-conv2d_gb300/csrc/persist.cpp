@@ -52,12 +52,12 @@ PlanFileHeader header_of(const Plan& pl) {
     h.k = pl.prob.k;
     h.p = pl.prob.p;
     h.q = pl.prob.q;
-    h.xform = static_cast<int32_t>(pl.xf);
+    h.xform = static_cast<int32_t>(pl.xf) + (pl.algo == CONV2D_ALGO_4X3_ROW ? 16 : 0);   // row F(4x3): own layout
     h.op = static_cast<int32_t>(pl.op);
     h.e = static_cast<uint32_t>(pl.g.alpha * pl.g.alpha);
     h.cp = static_cast<uint32_t>(pl.g.cp);
     h.kp = static_cast<uint32_t>(pl.g.kp);
-    h.u_bytes = static_cast<uint64_t>(h.e) * h.kp * h.cp * 2;
+    h.u_bytes = static_cast<uint64_t>(pl.u_bytes);
     return h;
 }
 

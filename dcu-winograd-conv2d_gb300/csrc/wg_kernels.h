@@ -184,6 +184,24 @@ cudaError_t plan_fused2x3(FusedPlan& fp, OpType op, const Geom& g, const void* U
 cudaError_t launch_fused2x3(const FusedPlan& fp, const Geom& g, const void* x, const void* x_end, void* out,
                             DevErr* err, cudaStream_t stream);
 
+// ---- row-Winograd F(4x3), fully fused (1-D F(4,3) along the width) --------
+struct RowPlan {
+    CUtensorMap tmU;
+    alignas(8) unsigned char geo[96];  // kernel geometry (row4x3.cu)
+    int cp16, kp64;
+    int smem_bytes;
+};
+// cudaErrorNotSupported for padding above 64, more than 256 output columns or
+// when the stages do not fit in shared memory.  U may be null (a size probe).
+cudaError_t plan_row4x3(RowPlan& rp, const Geom& g, const void* U);
+long long row4x3_filter_bytes(const RowPlan& rp);
+long long row4x3_items(const RowPlan& rp, int n_images);   // CTA work items of n images
+// U1[e*3 + r][Cp16/8][Kp64][8] fp16 from KCRS fp16 weights
+cudaError_t launch_row4x3_filter(const RowPlan& rp, const void* weight, void* U, cudaStream_t stream);
+// images [0, n_images) of the tensor starting at x (which ends at x_end)
+cudaError_t launch_row4x3(const RowPlan& rp, const void* x, const void* x_end, void* out, int n_images, DevErr* err,
+                          cudaStream_t stream);
+
 // Tensor-map encoder from the driver (resolved once through the runtime).
 CUresult encode_tiled(CUtensorMap* map, CUtensorMapDataType dt, cuuint32_t rank, void* addr, const cuuint64_t* dims,
                       const cuuint64_t* strides_bytes, const cuuint32_t* box, CUtensorMapSwizzle swz);

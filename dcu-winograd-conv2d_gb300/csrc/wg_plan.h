@@ -48,6 +48,8 @@ struct Plan {
     DevErr* err = nullptr;
     GemmPlan gemm_full{}, gemm_tail{};
     FusedPlan fused{};
+    RowPlan row{};
+    long long u_bytes = 0;   // bytes of the transformed filter U
     bool nhwc = false;   // channels-last input and output
     NhwcInDesc nh_in{};
     int nh_smem = 0;
@@ -65,6 +67,9 @@ struct Plan {
     cudaStream_t host_in_stream = nullptr, host_out_stream = nullptr;
     static constexpr int kMaxHostChunks = 8;
     cudaEvent_t host_ev[2 * kMaxHostChunks + 2] = {};
+
+    // one kernel per call, no Winograd-domain workspace
+    bool single_kernel() const { return algo == CONV2D_ALGO_2X3_FUSED || algo == CONV2D_ALGO_4X3_ROW; }
 
     ~Plan();
     int build(const problem_t* pr, const conv2d_options_t* opt);

@@ -182,6 +182,14 @@ __device__ __forceinline__ void tc_commit(uint64_t* bar) {
 
 __device__ __forceinline__ void tc_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
+// Ties 8 loaded registers to a preceding tcgen05.wait::ld: an empty volatile
+// asm that rewrites them, ordered after the wait like every volatile asm, so
+// no use of them can be scheduled before the wait.
+__device__ __forceinline__ void tc_hold(uint32_t (&r)[8]) {
+#pragma unroll
+    for (int i = 0; i < 8; ++i) asm volatile("" : "+r"(r[i]));
+}
+
 // 32 lanes x 32-bit, 8 consecutive columns per thread.
 __device__ __forceinline__ void tmem_ld_x8(uint32_t taddr, uint32_t (&r)[8]) {
     asm volatile(

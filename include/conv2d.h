@@ -85,7 +85,9 @@ enum {
     CONV2D_ALGO_4X3_NON_FUSED = 0,
     CONV2D_ALGO_2X3_NON_FUSED = 1,
     CONV2D_ALGO_2X3_FUSED = 2,
-    CONV2D_ALGO_AUTO = 3         /* per-shape autotuner (measures candidates once per shape) */
+    CONV2D_ALGO_AUTO = 3,        /* per-shape autotuner (measures candidates once per shape) */
+    CONV2D_ALGO_4X3_ROW = 4      /* row-Winograd F(4x3), one fused kernel: 1-D F(4,3) along the
+                                    width, the 3 filter rows summed directly; fp16 NCHW tensors */
 };
 
 /* Options for getkernelInfo_ex.  conv2d_options_default() gives the values

@@ -10,7 +10,7 @@ torch = pytest.importorskip("torch")
 
 pytestmark = pytest.mark.gpu
 
-TOL = {0: 2e-2, 1: 1e-2, 2: 1e-2}
+TOL = {0: 2e-2, 1: 1e-2, 2: 1e-2, 4: 2e-2}
 
 SHAPES = [  # n, c, h, w, k, pad
     (2, 64, 14, 14, 64, 1), (1, 128, 28, 28, 256, 1), (3, 32, 7, 7, 48, 1), (2, 256, 12, 12, 128, 1),
@@ -33,7 +33,7 @@ def _make(wg, shapes, seed):
     return probs, keep, host
 
 
-@pytest.mark.parametrize("algo", [-1, 3, 0, 1])
+@pytest.mark.parametrize("algo", [-1, 3, 0, 1, 4])
 def test_batch_grouped_equals_percall_and_oracle(wg, algo):
     if not torch.cuda.is_available():
         pytest.skip("no CUDA device")

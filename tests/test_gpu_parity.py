@@ -29,7 +29,7 @@ TOL4_SMALL_C = 3e-2
 
 def tol_for(m, c):
     return TOL4_SMALL_C if (m == 4 and c < 16) else TOL[m]
-ALGOS = [-1, 0, 1, 2]  # reference selection, F(4x3), F(2x3), F(2x3) fused
+ALGOS = [-1, 0, 1, 2, 4]  # reference selection, F(4x3), F(2x3), F(2x3) fused, row F(4x3) fused
 
 
 @pytest.fixture(scope="module", autouse=True)
@@ -39,7 +39,7 @@ def _cuda():
 
 
 def algo_m(algo):
-    return 4 if algo == 0 else 2
+    return 4 if algo in (0, 4) else 2
 
 
 def run(wg, x16, w16, p=1, q=1, opts=None, stream=None):
@@ -81,7 +81,7 @@ def test_golden_vectors(wg, name, algo):
         assert O.reference_criterion_failures(y, ref) == 0
 
 
-@pytest.mark.parametrize("algo", [0, 1, 2])
+@pytest.mark.parametrize("algo", [0, 1, 2, 4])
 @pytest.mark.parametrize("shape", [
     (1, 3, 7, 7, 5), (2, 5, 14, 14, 27), (1, 16, 28, 28, 4), (3, 8, 13, 9, 12), (1, 70, 10, 10, 33),
     (1, 130, 9, 9, 130), (2, 64, 20, 20, 64), (1, 200, 8, 8, 300), (1, 24, 112, 112, 16), (4, 40, 7, 7, 260),
@@ -151,7 +151,7 @@ def test_transform_kernels_elementwise(wg, algo, variant):
     assert np.abs(y.astype(np.float64) - y_ref).max() <= yscale * 2.0 ** -10
 
 
-@pytest.mark.parametrize("algo", [0, 1, 2])
+@pytest.mark.parametrize("algo", [0, 1, 2, 4])
 def test_repeat_calls_bit_identical(wg, algo):
     x, wt = O.uniform_inputs(3, 2, 48, 30, 30, 40)
     xt = torch.from_numpy(x).cuda()
@@ -244,8 +244,8 @@ def test_refresh_filter_after_in_place_change(wg):
     assert O.rel_errors(y.cpu().numpy(), r64)[0] <= TOL[2]
 
 
-HOST_CASES = [(a, n, 24, 16, 24) for a in (0, 1, 2) for n in (1, 2, 7)] + \
-    [(a, 11, 64, 100, 64) for a in (0, 1, 2)]  # 28.2 MB of copies: 3 chunks of 4, 4, 3 images
+HOST_CASES = [(a, n, 24, 16, 24) for a in (0, 1, 2, 4) for n in (1, 2, 7)] + \
+    [(a, 11, 64, 100, 64) for a in (0, 1, 2, 4)]  # 28.2 MB of copies: 3 chunks of 4, 4, 3 images
 
 
 @pytest.mark.parametrize("algo,n,c,h,k", HOST_CASES)
@@ -388,3 +388,25 @@ def test_nhwc_refuses_channels_not_a_multiple_of_8(wg):
     with pytest.raises(wg.Conv2dError) as ei:
         wg.Conv2d(prob, opts_for(wg, 1, layout_nhwc=1))
     assert ei.value.status == wg.ERR_UNSUPPORTED
+
+
+@pytest.mark.parametrize("algo", [0, 1, 2, 4])
+def test_host_chunks_of_unaligned_images(wg, algo):
+    """Images of 1,202,850 bytes: every host chunk after the first starts off
+    a 16-byte boundary (two chunks of 4 images, 19 MB of copies)."""
+    n, c, h, k = 8, 33, 135, 33
+    x, wt = O.uniform_inputs(77, n, c, h, h, k)
+    xt = torch.empty((n, c, h, h), dtype=torch.float16, device="cuda")
+    wtt = torch.from_numpy(wt).cuda()
+    y = torch.empty((n, k, h, h), dtype=torch.float16, device="cuda")
+    prob = wg.make_problem(xt.data_ptr(), wtt.data_ptr(), y.data_ptr(), n, c, h, h, k)
+    op = wg.Conv2d(prob, opts_for(wg, algo))
+    assert op.algo == algo
+    hin = torch.from_numpy(x).pin_memory()
+    hout = torch.empty((n, k, h, h), dtype=torch.float16).pin_memory()
+    torch.cuda.synchronize()
+    op.host(hin.data_ptr(), hout.data_ptr(), torch.cuda.current_stream().cuda_stream)
+    st, site = op.check_device()
+    assert st == wg.OK, site
+    _, r64 = O.conv2d_direct(x, wt, nthreads=8)
+    assert O.rel_errors(hout.numpy(), r64)[0] <= TOL[algo_m(algo)]

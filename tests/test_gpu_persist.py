@@ -22,7 +22,7 @@ def _plan(wg, x, w_dev, y, algo, bf16=0):
     return wg.Conv2d(prob, wg.default_options(algo=algo, operand_bf16=bf16))
 
 
-@pytest.mark.parametrize("algo", [0, 1, 2])
+@pytest.mark.parametrize("algo", [0, 1, 2, 4])
 def test_saved_filter_reproduces_the_output(wg, tmp_path, algo):
     n, c, h, w, k = 2, 40, 18, 18, 56
     xh, wh = O.uniform_inputs(91, n, c, h, w, k)

@@ -1,0 +1,64 @@
+"""GPU tests of the row-Winograd F(4x3) kernel (algorithm 4): 1-D F(4,3)
+along the width with the three filter rows summed directly, one fused kernel.
+
+Tolerance: max |y - ref| / max(|ref|, rms(ref)) <= 2e-2 against the fp64
+direct convolution, the F(4x3) bound; the 1-D transform's operands grow far
+less than the 2-D ones, so the measured errors sit near 1e-3."""
+import numpy as np
+import pytest
+
+import oracle as O
+
+torch = pytest.importorskip("torch")
+
+pytestmark = pytest.mark.gpu
+
+TOL = 2e-2
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _cuda():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+
+
+def _run(wg, x, wt, p, q, **opts):
+    xt = torch.from_numpy(np.ascontiguousarray(x)).cuda()
+    wtt = torch.from_numpy(np.ascontiguousarray(wt)).cuda()
+    y, op = wg.conv2d_torch(xt, wtt, p, q, wg.default_options(**opts))
+    torch.cuda.synchronize()
+    st, site = op.check_device()
+    assert st == wg.OK, f"device wait gave up at site {site}"
+    return y.cpu().numpy(), op
+
+
+@pytest.mark.parametrize("shape,pad", [
+    ((40, 48, 28, 28, 200), (1, 1)),   # 320 items: persistent CTAs walk several each
+    ((3, 35, 17, 61, 70), (1, 1)),     # channel tails in both dimensions, 16 tiles per row
+    ((2, 24, 30, 250, 40), (1, 1)),    # 63 tiles per row: two output rows per item
+    ((1, 64, 9, 9, 64), (0, 2)),       # asymmetric padding
+])
+def test_row4x3_against_fp64(wg, shape, pad):
+    n, c, h, w, k = shape
+    x, wt = O.uniform_inputs(sum(shape) + pad[0], n, c, h, w, k, filt="normal")
+    y, op = _run(wg, x, wt, pad[0], pad[1], algo=4)
+    assert op.algo == 4
+    _, r64 = O.conv2d_direct(x, wt, p=pad[0], q=pad[1], nthreads=8)
+    mx, mean, _ = O.rel_errors(y, r64)
+    assert mx <= TOL, (shape, pad, mx, mean)
+
+
+@pytest.mark.parametrize("opts", [dict(operand_bf16=1), dict(f4_points=1), dict(tile_scaling=1)])
+def test_row4x3_options_it_does_not_take_run_non_fused(wg, opts):
+    x, wt = O.uniform_inputs(3, 1, 16, 12, 12, 16)
+    _, op = _run(wg, x, wt, 1, 1, algo=4, **opts)
+    assert op.algo == 0
+
+
+def test_row4x3_wide_rows_run_non_fused(wg):
+    # 300 output columns = 75 tiles per row: fewer than two rows per 128-row MMA
+    x, wt = O.uniform_inputs(4, 1, 8, 4, 300, 8)
+    y, op = _run(wg, x, wt, 1, 1, algo=4)
+    assert op.algo == 0
+    _, r64 = O.conv2d_direct(x, wt)
+    assert O.rel_errors(y, r64)[0] <= 3e-2
