@@ -174,6 +174,7 @@ class Conv2d:
         self._alive = True
         opts = options if options is not None else default_options()
         self.scaling = bool(opts.tile_scaling or opts.io_bf16) and self.algo == ALGO_4X3
+        self.nhwc = bool(opts.layout_nhwc)
 
     @property
     def ptr(self):

@@ -2,7 +2,7 @@
 //
 // The reference picks F(2x3) fused / F(2x3) / F(4x3) with fixed size rules
 // (src/conv2d.cpp:125-156).  Here every candidate (algorithm x GEMM channel
-// tile) is planned on scratch output memory and timed on the device the
+// tile, plus the row-Winograd F(4x3) kernel this operator adds) is planned on scratch output memory and timed on the device the
 // first time a shape is seen; the winner is cached per shape and, when
 // WG_CONV2D_TUNE_FILE names a file, persisted there so later processes make
 // the same choice without measuring.  The reference selection wins unless
@@ -132,6 +132,7 @@ int autotune_choose(const problem_t& pr, const conv2d_options_t& opt, int fallba
     };
     std::vector<Cand> cands;
     cands.push_back({CONV2D_ALGO_2X3_FUSED, 0});
+    cands.push_back({CONV2D_ALGO_4X3_ROW, 0});
     const int bn0 = default_bn(static_cast<int>(pr.k));
     for (int a : {CONV2D_ALGO_2X3_NON_FUSED, CONV2D_ALGO_4X3_NON_FUSED}) {
         cands.push_back({a, bn0});

@@ -86,10 +86,13 @@ struct Batch {
             Plan& p = *plans[i];
             const void* x_end =
                 static_cast<const uint16_t*>(p.prob.in) + static_cast<long long>(p.prob.n) * p.g.c * p.g.h * p.g.w;
-            e = p.algo == CONV2D_ALGO_4X3_ROW
-                    ? launch_row4x3(p.row, p.prob.in, x_end, p.prob.out, static_cast<int>(p.prob.n), err, s)
-                    : launch_fused2x3(p.fused, p.g, p.prob.in, x_end, p.prob.out, err, s);
-            if (e != cudaSuccess) return e;
+            if (p.algo == CONV2D_ALGO_4X3_ROW) {
+                if ((e = launch_row4x3(p.row, p.prob.in, x_end, p.prob.out, static_cast<int>(p.prob.n), err, s)) !=
+                    cudaSuccess)
+                    return e;
+            } else if ((e = launch_fused2x3(p.fused, p.g, p.prob.in, x_end, p.prob.out, err, s)) != cudaSuccess) {
+                return e;
+            }
         }
         return cudaSuccess;
     }
@@ -211,8 +214,10 @@ int batch_create(const problem_t* problems, int count, const conv2d_options_t* o
         b->out_groups.push_back({static_cast<Xform>(kr.first.first), kr.first.second != 0,
                                  reinterpret_cast<const OutDesc*>(base + oO) + kr.second.first,
                                  static_cast<int>(kr.second.n), kr.second.total});
+    int single = 0;   // launches of the problems run by their own kernels
+    for (int i : b->fused) single += b->plans[i]->launches;
     b->grouped_launches = static_cast<int>(b->scaled.size() + b->in_groups.size() + b->gemm_groups.size() +
-                                           b->out_groups.size() + b->fused.size());
+                                           b->out_groups.size()) + single;
     if (cudaDeviceSynchronize() != cudaSuccess) return batch_fail(CONV2D_ERR_CUDA, "batch setup failed");
     *out = b.release();
     return CONV2D_OK;

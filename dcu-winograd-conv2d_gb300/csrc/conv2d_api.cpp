@@ -179,12 +179,15 @@ int Plan::build(const problem_t* pr, const conv2d_options_t* opt_in) {
         cudaGetLastError();
     }
     if (algo == CONV2D_ALGO_4X3_ROW) {
-        // fp16 NCHW tensors and operands with the {0, +-1, 1/2, -2} points only,
-        // and the staged rows of one output-row block must fit in shared memory;
-        // otherwise F(4x3) runs non-fused
+        // fp16 tensors and operands with the {0, +-1, 1/2, -2} points only; NCHW
+        // tensors run the channel-planar kernel (the staged rows of one block
+        // of output rows must fit in shared memory), NHWC ones the
+        // channel-interleaved kernel (at most 248 output columns, C a multiple
+        // of 16); otherwise F(4x3) runs non-fused
         const Geom g4 = make_geom(pr->n, pr->c, pr->h, pr->w, pr->k, pr->p, pr->q, 4);
-        if (nhwc || opt.io_bf16 || opt.operand_bf16 || opt.tile_scaling || opt.f4_points ||
-            plan_row4x3(row, g4, nullptr) != cudaSuccess)
+        const cudaError_t pe = nhwc ? (pr->c % 16 == 0 ? plan_row4x3i(row, g4, nullptr, true) : cudaErrorNotSupported)
+                                    : plan_row4x3(row, g4, nullptr);
+        if (opt.io_bf16 || opt.operand_bf16 || opt.tile_scaling || opt.f4_points || pe != cudaSuccess)
             algo = CONV2D_ALGO_4X3_NON_FUSED;
         cudaGetLastError();
     }
@@ -251,7 +254,14 @@ int Plan::build(const problem_t* pr, const conv2d_options_t* opt_in) {
         info_threads = 320;
         info_smem = fused.smem_bytes;
     } else if (algo == CONV2D_ALGO_4X3_ROW) {
-        ce = plan_row4x3(row, g, U);
+        if (nhwc) {
+            ce = plan_row4x3i(row, g, U, true);
+            if (ce == cudaSuccess)
+                ce = bind_row4x3i_input(row, pr->in, static_cast<int>(pr->c), static_cast<int>(pr->h),
+                                        static_cast<int>(pr->w), static_cast<int>(pr->n));
+        } else {
+            ce = plan_row4x3(row, g, U);
+        }
         if (ce != cudaSuccess) return cuda_fail(ce, "row F(4x3) plan");
         launches = 1;
         info_grid = static_cast<unsigned>(std::min<long long>(row4x3_items(row, static_cast<int>(pr->n)), num_sms));
@@ -313,7 +323,7 @@ int Plan::run_range(int n0, int nc, const GemmPlan* gp, cudaStream_t s) {
         return CONV2D_OK;
     }
     if (algo == CONV2D_ALGO_4X3_ROW) {
-        ce = launch_row4x3(row, xin, x_end, yout, nc, err, s);
+        ce = nhwc ? launch_row4x3i(row, yout, n0, nc, err, s) : launch_row4x3(row, xin, x_end, yout, nc, err, s);
         if (ce != cudaSuccess) return cuda_fail(ce, "row F(4x3) launch");
         mark(s);
         return CONV2D_OK;

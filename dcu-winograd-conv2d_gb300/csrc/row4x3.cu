@@ -33,6 +33,8 @@
 #include <cuda_fp16.h>
 
 #include <algorithm>
+#include <cstdio>
+#include <cstdlib>
 
 #include "wg_kernels.h"
 #include "wg_launch.h"
@@ -405,6 +407,314 @@ __global__ void __launch_bounds__(kThreads, 1)
     }
 }
 
+// ---- channel-interleaved variant ---------------------------------------------
+// The input is the caller's NHWC tensor x[n][y][x][C], C a multiple of 16.
+// One 4-D TMA box {16 channels, WB columns, R+2 rows, 1 image} per chunk
+// stages [row][column][16 channels]; its out-of-range parts (padding rows and
+// columns, channels past Cs) arrive as zeros, so the producers need no masks,
+// and each of their loads moves 16 bytes (8 channels of one input value).
+// WB = 4 * tiles_w + 5 (>= the 4 * tiles_w + 2 columns read, 1 mod 4): the
+// staged rows then start 32 bytes apart modulo 128, and a quarter-warp of 4
+// rows x 2 channel granules reads 8 distinct 16-byte bank groups.
+constexpr int kMaxAStages = 4;
+constexpr int kProducersI = 256;                         // 8 warps: transform, then epilogue
+constexpr int kThreadsI = kProducersI + 96;              // + MMA, staging-TMA and filter-TMA warps
+constexpr int kMmaWarpI = kProducersI / 32, kLoaderWarpI = kMmaWarpI + 1, kBWarpI = kMmaWarpI + 2;
+
+struct RowGeoI {    // shared by host and device
+    int C, K, pad_h, pad_w, OH, OW, tiles_w;
+    int R, row_blocks, n_blocks, c_chunks;
+    int wb;         // staged columns
+    int stg_bytes;  // one staging buffer (box bytes rounded to 1024)
+    int box_bytes;  // bytes one staging TMA delivers
+    int nbuf, nbs;  // staging buffers, filter-tile stages
+    int nas;        // transformed-input (A) stages
+    int arows;      // rows of one A granule (>= 128 + 2 * tiles_w)
+    int tb4;        // blocks of 4 tiles per row of tiles
+    int tasks;      // producer task slots per chunk (4 rows x 4 tiles x 2 granules blocks)
+};
+
+__device__ __forceinline__ void bt6x8(const uint4 (&q)[6], uint4 (&o)[6]) {
+#pragma unroll
+    for (int l = 0; l < 4; ++l) {
+        __half2 d[6], v[6];
+#pragma unroll
+        for (int j = 0; j < 6; ++j) {
+            const uint32_t w = l == 0 ? q[j].x : l == 1 ? q[j].y : l == 2 ? q[j].z : q[j].w;
+            d[j] = *reinterpret_cast<const __half2*>(&w);
+        }
+        bt6(d, v);
+#pragma unroll
+        for (int e = 0; e < 6; ++e) {
+            const uint32_t w = *reinterpret_cast<const uint32_t*>(&v[e]);
+            if (l == 0) o[e].x = w;
+            else if (l == 1) o[e].y = w;
+            else if (l == 2) o[e].z = w;
+            else o[e].w = w;
+        }
+    }
+}
+
+template <bool OUT_NHWC>
+__global__ void __launch_bounds__(kThreadsI, 1)
+    row4x3i_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constant__ CUtensorMap tmU,
+                   __half* __restrict__ out, const __grid_constant__ RowGeoI gg, int n_base, int n_images, DevErr* err) {
+    constexpr uint32_t kIdesc = make_idesc_f16(128, kBN, false);
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    unsigned char* smem = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
+    const int a_gran = gg.arows * 16;
+    const int a_bytes = kE * 2 * a_gran;
+    const int nbs = gg.nbs, nbuf = gg.nbuf, nas = gg.nas;
+    // smem: B stages | staging buffers | A stages | barriers (1024-aligned parts first)
+    unsigned char* bstage = smem;
+    unsigned char* stg = smem + nbs * kBBytes;
+    unsigned char* astage = stg + nbuf * gg.stg_bytes;
+    uint64_t* bars = reinterpret_cast<uint64_t*>(astage + nas * a_bytes);
+    uint64_t* afull = bars;                        // [4] producers
+    uint64_t* aempty = bars + 4;                   // [4] MMA commit
+    uint64_t* bfull = bars + 8;                    // [4] filter TMA (expect_tx)
+    uint64_t* bempty = bars + 12;                  // [4] MMA commit
+    uint64_t* sfull = bars + 16;                   // [4] staging TMA (expect_tx)
+    uint64_t* sempty = bars + 20;                  // [4] staging buffer read by all producers
+    uint64_t* tfull = bars + 24;                   // accumulators of the current item ready
+    uint64_t* tempty = bars + 25;                  // accumulators drained
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 26);
+    volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int K = gg.K, R = gg.R, tiles_w = gg.tiles_w, c_chunks = gg.c_chunks;
+    const int total_items = n_images * gg.row_blocks * gg.n_blocks;
+    const int my_items = blockIdx.x < total_items ? (total_items - 1 - blockIdx.x) / gridDim.x + 1 : 0;
+    const int total_chunks = my_items * c_chunks;
+
+    if (tid == 0) {
+        for (int i = 0; i < kMaxAStages; ++i) {
+            mbar_init(&afull[i], kProducersI);
+            mbar_init(&aempty[i], 1);
+        }
+        for (int i = 0; i < kMaxBStages; ++i) {
+            mbar_init(&bfull[i], 1);
+            mbar_init(&bempty[i], 1);
+        }
+        for (int i = 0; i < kMaxBufs; ++i) {
+            mbar_init(&sfull[i], 1);
+            mbar_init(&sempty[i], kProducersI);
+        }
+        mbar_init(tfull, 1);
+        mbar_init(tempty, kProducersI);
+        *abort_flag = 0;
+        fence_barrier_init();
+    }
+    pdl_wait();     // input written, earlier readers of the output done
+    pdl_trigger();
+    if (warp == kMmaWarpI) tmem_alloc(tmem_slot, 512);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem_base = *tmem_slot;
+
+    auto item_of = [&](int k, int& n, int& oh0, int& nb) {
+        const int item = blockIdx.x + k * gridDim.x;
+        nb = item % gg.n_blocks;
+        const int rest = item / gg.n_blocks;
+        oh0 = (rest % gg.row_blocks) * R;
+        n = rest / gg.row_blocks;
+    };
+
+    if (warp == kLoaderWarpI) {
+        // staged input rows: one TMA box per chunk, nbuf chunks ahead
+        if (lane == 0) {
+            tma_prefetch_desc(&tmX);
+            for (int gc = 0; gc < total_chunks; ++gc) {
+                const int sb = gc % nbuf;
+                if (gc >= nbuf && !mbar_wait(&sempty[sb], ((gc / nbuf) & 1) ^ 1, abort_flag, err, ERR_SITE_EMPTY)) break;
+                const int k = gc / c_chunks, c = gc - k * c_chunks;
+                int n, oh0, nb;
+                item_of(k, n, oh0, nb);
+                mbar_arrive_expect_tx(&sfull[sb], static_cast<uint32_t>(gg.box_bytes));
+                tma_load_4d(stg + sb * gg.stg_bytes, &tmX, &sfull[sb], c * kChunk, -gg.pad_w, oh0 - gg.pad_h,
+                            n_base + n);
+            }
+        }
+    } else if (warp == kBWarpI) {
+        if (lane == 0) {
+            tma_prefetch_desc(&tmU);
+            for (int gc = 0; gc < total_chunks; ++gc) {
+                const int sb = gc % nbs;
+                if (gc >= nbs && !mbar_wait(&bempty[sb], ((gc / nbs) & 1) ^ 1, abort_flag, err, ERR_SITE_EMPTY)) break;
+                const int k = gc / c_chunks, c = gc - k * c_chunks;
+                int n, oh0, nb;
+                item_of(k, n, oh0, nb);
+                mbar_arrive_expect_tx(&bfull[sb], kBBytes);
+                tma_load_4d(bstage + sb * kBBytes, &tmU, &bfull[sb], 0, nb * (kBN / 8), c * 2, 0);
+            }
+        }
+    } else if (warp == kMmaWarpI) {
+        if (lane == 0) {
+            bool ok = true;
+            for (int k = 0; k < my_items && ok; ++k) {
+                if (!mbar_wait(tempty, (k & 1) ^ 1, abort_flag, err, ERR_SITE_TMEM_EMPTY)) break;
+                tc_fence_after();
+                for (int c = 0; c < c_chunks; ++c) {
+                    const int gc = k * c_chunks + c;
+                    const int sa = gc % nas, sb = gc % nbs;
+                    if (!mbar_wait(&afull[sa], (gc / nas) & 1, abort_flag, err, ERR_SITE_FULL) ||
+                        !mbar_wait(&bfull[sb], (gc / nbs) & 1, abort_flag, err, ERR_SITE_FULL)) {
+                        ok = false;
+                        break;
+                    }
+                    tc_fence_after();
+                    const uint32_t a_base = smem_u32(astage + sa * a_bytes);
+                    const uint32_t b_base = smem_u32(bstage + sb * kBBytes);
+#pragma unroll
+                    for (int e = 0; e < kE; ++e) {
+#pragma unroll
+                        for (int r = 0; r < kTaps; ++r) {
+                            const uint64_t ad =
+                                make_smem_desc(a_base + e * (2 * a_gran) + r * tiles_w * 16, a_gran, 128, Swz::None);
+                            const uint64_t bd = make_smem_desc(b_base + (e * kTaps + r) * (2 * kBN * 16), kBN * 16, 128,
+                                                               Swz::None);
+                            tc_mma_f16(tmem_base + e * kBN, ad, bd, kIdesc, (c > 0 || r > 0) ? 1u : 0u);
+                        }
+                    }
+                    tc_commit(&aempty[sa]);
+                    tc_commit(&bempty[sb]);
+                }
+                if (ok && !*abort_flag) tc_commit(tfull);
+            }
+        }
+    } else {
+        // ---- producers: task = (row of tiles rho, tile tw, granule g) in
+        //      blocks of 4 rows x 4 tiles x 2 granules (a warp = one block)
+        const int nrow = R + kTaps - 1;
+        bool ok = true;
+        for (int k = 0; k < my_items && ok; ++k) {
+            int n, oh0, nb;
+            item_of(k, n, oh0, nb);
+            for (int c = 0; c < c_chunks; ++c) {
+                const int gc = k * c_chunks + c;
+                const int s = gc % nas;
+                const int sb = gc % nbuf;
+                // the A stage may be rewritten once the MMAs of chunk gc - nas are done
+                if (!mbar_wait(&sfull[sb], (gc / nbuf) & 1, abort_flag, err, ERR_SITE_FULL) ||
+                    !mbar_wait(&aempty[s], ((gc / nas) & 1) ^ 1, abort_flag, err, ERR_SITE_EMPTY)) {
+                    ok = false;
+                    break;
+                }
+                const unsigned char* buf = stg + sb * gg.stg_bytes;
+                unsigned char* A = astage + s * a_bytes;
+                for (int t = tid; t < gg.tasks; t += kProducersI) {
+                    const int g = t & 1, rq = (t >> 1) & 3, tq = (t >> 3) & 3, blk = t >> 5;
+                    const int rb = blk / gg.tb4, tb = blk - rb * gg.tb4;
+                    const int rho = rb * 4 + rq, tw = tb * 4 + tq;
+                    if (rho >= nrow || tw >= tiles_w) continue;
+                    const unsigned char* src = buf + ((rho * gg.wb + tw * 4) * 2 + g) * 16;
+                    uint4 q[6], o[6];
+#pragma unroll
+                    for (int j = 0; j < 6; ++j) q[j] = *reinterpret_cast<const uint4*>(src + j * 32);
+                    bt6x8(q, o);
+                    unsigned char* dst = A + g * a_gran + (rho * tiles_w + tw) * 16;
+#pragma unroll
+                    for (int e = 0; e < 6; ++e) *reinterpret_cast<uint4*>(dst + e * (2 * a_gran)) = o[e];
+                }
+                mbar_arrive(&sempty[sb]);     // staged rows read
+                fence_proxy_async_smem();     // A visible to the tensor core
+                mbar_arrive(&afull[s]);
+            }
+            if (!ok) break;
+
+            // ---- epilogue: the 6 accumulators of each (tile, channel) -> 4 outputs
+            if (!mbar_wait(tfull, k & 1, abort_flag, err, ERR_SITE_TMEM_FULL)) break;
+            tc_fence_after();
+            const int quarter = warp & 3;
+            const int chalf = warp >> 2;                // 32 output channels each
+            const int m = quarter * 32 + lane;          // MMA row = output row i, tile tw
+            const int i = m / tiles_w, tw = m - (m / tiles_w) * tiles_w;
+            const int oh = oh0 + i;
+            const bool mv = i < R && oh < gg.OH;
+            const int ow0 = tw * 4;
+            const int vc = min(4, gg.OW - ow0);
+            const uint32_t lane_base = tmem_base + (static_cast<uint32_t>(quarter * 32) << 16);
+#pragma unroll 1
+            for (int g8 = 0; g8 < 4; ++g8) {
+                const int kl0 = chalf * 32 + g8 * 8;
+                uint32_t acc[6][8];
+#pragma unroll
+                for (int e = 0; e < 6; ++e) tmem_ld_x8(lane_base + e * kBN + kl0, acc[e]);
+                tc_wait_ld();
+#pragma unroll
+                for (int e = 0; e < 6; ++e) tc_hold(acc[e]);
+                const int kk0 = nb * kBN + kl0;
+                if (!mv || kk0 >= K) continue;
+                float yv[8][4];
+#pragma unroll
+                for (int q = 0; q < 8; ++q) {
+                    const float m0 = __uint_as_float(acc[0][q]), m1 = __uint_as_float(acc[1][q]);
+                    const float m2 = __uint_as_float(acc[2][q]), m3 = __uint_as_float(acc[3][q]);
+                    const float m4 = __uint_as_float(acc[4][q]), m5 = __uint_as_float(acc[5][q]);
+                    const float a = m1 + m2, b = m1 - m2;   // A^T of F4 (wg_transforms.cuh)
+                    yv[q][0] = m0 + a + m3 + m4;
+                    yv[q][1] = b + 0.5f * m3 - 2.f * m4;
+                    yv[q][2] = a + 0.25f * m3 + 4.f * m4;
+                    yv[q][3] = b + 0.125f * m3 - 8.f * m4 + m5;
+                }
+                if (OUT_NHWC) {
+                    // y[n][oh][ow][K]: 8 consecutive channels of each output column
+                    __half* o = out + ((static_cast<long long>(n) * gg.OH + oh) * gg.OW + ow0) * K + kk0;
+                    const bool vec = kk0 + 8 <= K && (K & 7) == 0 && (reinterpret_cast<uintptr_t>(out) & 15) == 0;
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) {
+                        if (j >= vc) break;
+                        if (vec) {
+                            uint4 w;
+                            __half2 h0 = __floats2half2_rn(yv[0][j], yv[1][j]), h1 = __floats2half2_rn(yv[2][j], yv[3][j]);
+                            __half2 h2 = __floats2half2_rn(yv[4][j], yv[5][j]), h3 = __floats2half2_rn(yv[6][j], yv[7][j]);
+                            w.x = *reinterpret_cast<uint32_t*>(&h0);
+                            w.y = *reinterpret_cast<uint32_t*>(&h1);
+                            w.z = *reinterpret_cast<uint32_t*>(&h2);
+                            w.w = *reinterpret_cast<uint32_t*>(&h3);
+                            *reinterpret_cast<uint4*>(o + static_cast<long long>(j) * K) = w;
+                        } else {
+#pragma unroll
+                            for (int q = 0; q < 8; ++q)
+                                if (kk0 + q < K) o[static_cast<long long>(j) * K + q] = __float2half_rn(yv[q][j]);
+                        }
+                    }
+                } else {
+#pragma unroll
+                    for (int q = 0; q < 8; ++q) {
+                        const int kk = kk0 + q;
+                        if (kk >= K) break;
+                        __half* o = out + ((static_cast<long long>(n) * K + kk) * gg.OH + oh) * static_cast<long long>(gg.OW) + ow0;
+                        if (vc == 4 && (reinterpret_cast<uintptr_t>(o) & 7) == 0) {
+                            __half2 lo = __floats2half2_rn(yv[q][0], yv[q][1]), hi = __floats2half2_rn(yv[q][2], yv[q][3]);
+                            *reinterpret_cast<uint2*>(o) =
+                                make_uint2(*reinterpret_cast<uint32_t*>(&lo), *reinterpret_cast<uint32_t*>(&hi));
+                        } else {
+#pragma unroll
+                            for (int j = 0; j < 4; ++j)
+                                if (j < vc) o[j] = __float2half_rn(yv[q][j]);
+                        }
+                    }
+                }
+            }
+            tc_fence_before();
+            mbar_arrive(tempty);
+        }
+    }
+
+    __syncthreads();
+    if (*abort_flag) {
+        const unsigned long long t0 = globaltimer_ns();
+        while (globaltimer_ns() - t0 < 2000000ull) {
+        }
+    }
+    if (warp == kMmaWarpI) {
+        tc_fence_after();
+        tmem_dealloc(tmem_base, 512);
+    }
+}
+
 // U1[e*3 + r][Cp16/8][Kp64][8] = G w[k][c][r][.] (1-D F(4,3) filter transform,
 // the G of F4), zero for c >= C or k >= K.
 __global__ void __launch_bounds__(256) row4x3_filter_kernel(const __half* __restrict__ w, __half* __restrict__ U, int K,
@@ -426,6 +736,29 @@ __global__ void __launch_bounds__(256) row4x3_filter_kernel(const __half* __rest
         for (int e = 0; e < kE; ++e)
             U[((static_cast<long long>(e * kTaps + r) * CG + c / 8) * Kp + k) * 8 + (c & 7)] = __float2half_rn(u[e]);
     }
+}
+
+}  // namespace
+
+namespace {
+
+// U1 viewed as 128-byte rows of 8 output channels: a box of 8 rows (64
+// channels) x 2 granules x 18 (element, filter row) per chunk
+cudaError_t encode_u1(RowPlan& rp, const Geom& g, const void* U) {
+    rp.c = g.c;
+    rp.k = g.k;
+    rp.cp16 = (g.c + 15) / 16 * 16;
+    rp.kp64 = (g.k + kBN - 1) / kBN * kBN;
+    if (!U) return cudaSuccess;
+    const cuuint64_t CG = static_cast<cuuint64_t>(rp.cp16 / 8);
+    const cuuint64_t Kr = static_cast<cuuint64_t>(rp.kp64 / 8);
+    cuuint64_t dims[4] = {64, Kr, CG, kE * kTaps};
+    cuuint64_t strides[3] = {128, Kr * 128, CG * Kr * 128};
+    cuuint32_t box[4] = {64, kBN / 8, 2, kE * kTaps};
+    if (encode_tiled(&rp.tmU, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 4, const_cast<void*>(U), dims, strides, box,
+                     CU_TENSOR_MAP_SWIZZLE_NONE) != CUDA_SUCCESS)
+        return cudaErrorInvalidValue;
+    return cudaSuccess;
 }
 
 }  // namespace
@@ -462,35 +795,129 @@ cudaError_t plan_row4x3(RowPlan& rp, const Geom& g, const void* U) {
         }
     }
     if (!rp.smem_bytes) return cudaErrorNotSupported;
-    rp.cp16 = (g.c + 15) / 16 * 16;
-    rp.kp64 = (g.k + kBN - 1) / kBN * kBN;
-    if (U) {
-        // U1 viewed as 128-byte rows of 8 output channels: a box of 8 rows (64
-        // channels) x 2 granules x 18 (element, filter row) per chunk
-        const cuuint64_t CG = static_cast<cuuint64_t>(rp.cp16 / 8);
-        const cuuint64_t Kr = static_cast<cuuint64_t>(rp.kp64 / 8);
-        cuuint64_t dims[4] = {64, Kr, CG, kE * kTaps};
-        cuuint64_t strides[3] = {128, Kr * 128, CG * Kr * 128};
-        cuuint32_t box[4] = {64, kBN / 8, 2, kE * kTaps};
-        if (encode_tiled(&rp.tmU, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 4, const_cast<void*>(U), dims, strides, box,
-                         CU_TENSOR_MAP_SWIZZLE_NONE) != CUDA_SUCCESS)
-            return cudaErrorInvalidValue;
+    rp.interleaved = 0;
+    return encode_u1(rp, g, U);
+}
+
+// channel-interleaved variant: geometry, shared-memory split and the filter map
+cudaError_t plan_row4x3i(RowPlan& rp, const Geom& g, const void* U, bool out_nhwc) {
+    RowGeoI& gg = *reinterpret_cast<RowGeoI*>(rp.geo);
+    static_assert(sizeof(RowGeoI) <= sizeof(rp.geo), "RowPlan geometry storage");
+    gg.C = g.c; gg.K = g.k; gg.pad_h = g.pad_h; gg.pad_w = g.pad_w;
+    gg.OH = g.oh; gg.OW = g.ow;
+    gg.tiles_w = (g.ow + 3) / 4;
+    if (gg.tiles_w > 62) return cudaErrorNotSupported;   // the staged columns are one TMA box (<= 256)
+    const int rmax = 128 / gg.tiles_w;
+    gg.row_blocks = (g.oh + rmax - 1) / rmax;
+    gg.R = (g.oh + gg.row_blocks - 1) / gg.row_blocks;
+    gg.n_blocks = (g.k + kBN - 1) / kBN;
+    gg.c_chunks = (g.c + kChunk - 1) / kChunk;
+    gg.wb = 4 * gg.tiles_w + 5;
+    gg.box_bytes = 2 * kChunk * gg.wb * (gg.R + kTaps - 1);
+    gg.stg_bytes = (gg.box_bytes + 127) / 128 * 128;
+    gg.tb4 = (gg.tiles_w + 3) / 4;
+    gg.tasks = (gg.R + kTaps - 1 + 3) / 4 * gg.tb4 * 32;
+    // A granule rows: 128 + 2 * tiles_w at least; the rows mod 8 set where the
+    // second granule falls in the bank space relative to the first, chosen so
+    // a quarter-warp's stores (4 rows of tiles x 2 granules) hit distinct
+    // 16-byte bank groups where the tile row count allows it
+    const int base = (128 + 2 * gg.tiles_w + 7) / 8 * 8;
+    int best = 0, best_distinct = -1;
+    for (int k = 0; k < 8; ++k) {
+        unsigned used = 0;
+        int distinct = 0;
+        for (int r = 0; r < 4; ++r)
+            for (int gr = 0; gr < 2; ++gr) {
+                const int slot = ((r * gg.tiles_w) + gr * k) & 7;
+                if (!(used & (1u << slot))) ++distinct;
+                used |= 1u << slot;
+            }
+        if (distinct > best_distinct) {
+            best_distinct = distinct;
+            best = k;
+        }
     }
+    gg.arows = base + best;
+    const int a_bytes = kE * 2 * gg.arows * 16;
+    // (A stages, filter-tile stages, staging buffers), deepest first;
+    // WG_CONV2D_ROW_STAGES="a,b,s" asks for one split (if it fits)
+    static const int kPrefs[][3] = {{2, 4, 4}, {2, 4, 3}, {2, 3, 4}, {2, 3, 3}, {2, 4, 2},
+                                    {2, 3, 2}, {2, 2, 3}, {2, 2, 2}, {2, 2, 1}};
+    rp.smem_bytes = 0;
+    int want[3] = {0, 0, 0};
+    if (const char* e = std::getenv("WG_CONV2D_ROW_STAGES"))
+        if (std::sscanf(e, "%d,%d,%d", &want[0], &want[1], &want[2]) != 3 || want[0] < 2 || want[0] > kMaxAStages ||
+            want[1] < 2 || want[1] > kMaxBStages || want[2] < 1 || want[2] > kMaxBufs)
+            want[0] = 0;
+    auto fits = [&](int a, int b, int sb) {
+        const int bytes = b * kBBytes + sb * gg.stg_bytes + a * a_bytes + kHdr + 128;
+        if (bytes > 227 * 1024) return false;
+        gg.nas = a;
+        gg.nbs = b;
+        gg.nbuf = sb;
+        rp.smem_bytes = bytes;
+        return true;
+    };
+    if (!(want[0] && fits(want[0], want[1], want[2])))
+        for (const auto& pf : kPrefs)
+            if (fits(pf[0], pf[1], pf[2])) break;
+    if (!rp.smem_bytes) return cudaErrorNotSupported;
+    rp.interleaved = 1;
+    rp.out_nhwc = out_nhwc ? 1 : 0;
+    rp.cs = (g.c + 15) / 16 * 16;
+    return encode_u1(rp, g, U);
+}
+
+cudaError_t bind_row4x3i_input(RowPlan& rp, const void* x_nhwc, int cs, int h, int w, int n_total) {
+    const RowGeoI& gg = *reinterpret_cast<const RowGeoI*>(rp.geo);
+    cuuint64_t dims[4] = {static_cast<cuuint64_t>(cs), static_cast<cuuint64_t>(w), static_cast<cuuint64_t>(h),
+                          static_cast<cuuint64_t>(n_total)};
+    cuuint64_t strides[3] = {static_cast<cuuint64_t>(cs) * 2, static_cast<cuuint64_t>(w) * cs * 2,
+                             static_cast<cuuint64_t>(h) * w * cs * 2};
+    cuuint32_t box[4] = {kChunk, static_cast<cuuint32_t>(gg.wb), static_cast<cuuint32_t>(gg.R + kTaps - 1), 1};
+    if (encode_tiled(&rp.tmX, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 4, const_cast<void*>(x_nhwc), dims, strides, box,
+                     CU_TENSOR_MAP_SWIZZLE_NONE) != CUDA_SUCCESS)
+        return cudaErrorInvalidValue;
     return cudaSuccess;
+}
+
+cudaError_t launch_row4x3i(const RowPlan& rp, void* out, int n_base, int n_images, DevErr* err, cudaStream_t s) {
+    const RowGeoI& gg = *reinterpret_cast<const RowGeoI*>(rp.geo);
+    const long long items = row4x3_items(rp, n_images);
+    if (items <= 0) return cudaSuccess;
+    if (items > 0x7fffffffLL) return cudaErrorInvalidValue;
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+        sms <= 0)
+        sms = 148;
+    const dim3 grid(static_cast<unsigned>(std::min<long long>(items, sms)));
+    if (rp.out_nhwc) {
+        cudaError_t e = cudaFuncSetAttribute(row4x3i_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, rp.smem_bytes);
+        if (e != cudaSuccess) return e;
+        return launch_pdl(row4x3i_kernel<true>, grid, dim3(kThreadsI), rp.smem_bytes, s, rp.tmX, rp.tmU,
+                          static_cast<__half*>(out), gg, n_base, n_images, err);
+    }
+    cudaError_t e = cudaFuncSetAttribute(row4x3i_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, rp.smem_bytes);
+    if (e != cudaSuccess) return e;
+    return launch_pdl(row4x3i_kernel<false>, grid, dim3(kThreadsI), rp.smem_bytes, s, rp.tmX, rp.tmU,
+                      static_cast<__half*>(out), gg, n_base, n_images, err);
 }
 
 long long row4x3_filter_bytes(const RowPlan& rp) { return static_cast<long long>(kE * kTaps) * rp.kp64 * rp.cp16 * 2; }
 
 long long row4x3_items(const RowPlan& rp, int n_images) {
+    if (rp.interleaved) {
+        const RowGeoI& gi = *reinterpret_cast<const RowGeoI*>(rp.geo);
+        return static_cast<long long>(n_images) * gi.row_blocks * gi.n_blocks;
+    }
     const RowGeo& gg = *reinterpret_cast<const RowGeo*>(rp.geo);
     return static_cast<long long>(n_images) * gg.row_blocks * gg.n_blocks;
 }
 
 cudaError_t launch_row4x3_filter(const RowPlan& rp, const void* weight, void* U, cudaStream_t s) {
-    const RowGeo& gg = *reinterpret_cast<const RowGeo*>(rp.geo);
     const long long total = static_cast<long long>(rp.kp64) * rp.cp16;
     row4x3_filter_kernel<<<static_cast<unsigned>((total + 255) / 256), 256, 0, s>>>(
-        static_cast<const __half*>(weight), static_cast<__half*>(U), gg.K, gg.C, rp.cp16, rp.kp64);
+        static_cast<const __half*>(weight), static_cast<__half*>(U), rp.k, rp.c, rp.cp16, rp.kp64);
     return cudaGetLastError();
 }
 

@@ -186,21 +186,35 @@ cudaError_t launch_fused2x3(const FusedPlan& fp, const Geom& g, const void* x, c
 
 // ---- row-Winograd F(4x3), fully fused (1-D F(4,3) along the width) --------
 struct RowPlan {
-    CUtensorMap tmU;
+    CUtensorMap tmU;                   // U1 filter tiles
+    CUtensorMap tmX;                   // interleaved kernel: the NHWC input rows
     alignas(8) unsigned char geo[96];  // kernel geometry (row4x3.cu)
+    int c, k;
     int cp16, kp64;
     int smem_bytes;
+    int interleaved;                   // 1: channel-interleaved kernel (NHWC rows)
+    int out_nhwc;                      // interleaved kernel: y is NHWC
+    int cs;                            // interleaved kernel: channels of the input pixels (C, a multiple of 16)
 };
-// cudaErrorNotSupported for padding above 64, more than 256 output columns or
-// when the stages do not fit in shared memory.  U may be null (a size probe).
+// Channel-planar kernel over NCHW input.  cudaErrorNotSupported for padding
+// above 64, more than 256 output columns or when the stages do not fit in
+// shared memory.  U may be null (a size probe).
 cudaError_t plan_row4x3(RowPlan& rp, const Geom& g, const void* U);
+// Channel-interleaved kernel over x[n][h][w][cs]; cudaErrorNotSupported for
+// more than 248 output columns.  U may be null (a size probe).
+cudaError_t plan_row4x3i(RowPlan& rp, const Geom& g, const void* U, bool out_nhwc);
+// tensor map of the interleaved kernel's input x[n_total][h][w][cs]
+cudaError_t bind_row4x3i_input(RowPlan& rp, const void* x_nhwc, int cs, int h, int w, int n_total);
 long long row4x3_filter_bytes(const RowPlan& rp);
 long long row4x3_items(const RowPlan& rp, int n_images);   // CTA work items of n images
 // U1[e*3 + r][Cp16/8][Kp64][8] fp16 from KCRS fp16 weights
 cudaError_t launch_row4x3_filter(const RowPlan& rp, const void* weight, void* U, cudaStream_t stream);
-// images [0, n_images) of the tensor starting at x (which ends at x_end)
+// planar kernel: images [0, n_images) of the tensor starting at x (which ends at x_end)
 cudaError_t launch_row4x3(const RowPlan& rp, const void* x, const void* x_end, void* out, int n_images, DevErr* err,
                           cudaStream_t stream);
+// interleaved kernel: images [n_base, n_base + n_images) of the bound input into
+// out (which holds those images)
+cudaError_t launch_row4x3i(const RowPlan& rp, void* out, int n_base, int n_images, DevErr* err, cudaStream_t stream);
 
 // Tensor-map encoder from the driver (resolved once through the runtime).
 CUresult encode_tiled(CUtensorMap* map, CUtensorMapDataType dt, cuuint32_t rank, void* addr, const cuuint64_t* dims,

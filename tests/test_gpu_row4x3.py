@@ -35,7 +35,7 @@ def _run(wg, x, wt, p, q, **opts):
 @pytest.mark.parametrize("shape,pad", [
     ((40, 48, 28, 28, 200), (1, 1)),   # 320 items: persistent CTAs walk several each
     ((3, 35, 17, 61, 70), (1, 1)),     # channel tails in both dimensions, 16 tiles per row
-    ((2, 24, 30, 250, 40), (1, 1)),    # 63 tiles per row: two output rows per item
+    ((2, 24, 30, 246, 40), (1, 1)),    # 62 tiles per row (the widest): two output rows per item
     ((1, 64, 9, 9, 64), (0, 2)),       # asymmetric padding
 ])
 def test_row4x3_against_fp64(wg, shape, pad):
@@ -62,3 +62,43 @@ def test_row4x3_wide_rows_run_non_fused(wg):
     assert op.algo == 0
     _, r64 = O.conv2d_direct(x, wt)
     assert O.rel_errors(y, r64)[0] <= 3e-2
+
+
+@pytest.mark.parametrize("shape,pad", [
+    ((2, 32, 14, 14, 64), 1), ((3, 48, 17, 23, 40), 1), ((1, 16, 30, 120, 72), 0), ((2, 64, 9, 9, 136), 2),
+])
+def test_row4x3_nhwc_matches_nchw_bit_for_bit(wg, shape, pad):
+    """NHWC tensors go straight to the kernel; NCHW ones through the NHWC copy
+    the plan makes, so the two results are the same numbers."""
+    n, c, h, w, k = shape
+    x, wt = O.uniform_inputs(61 + c, n, c, h, w, k, filt="normal")
+    y_nchw, op1 = _run(wg, x, wt, pad, pad, algo=4)
+    assert op1.algo == 4
+    xt = torch.from_numpy(np.ascontiguousarray(x.transpose(0, 2, 3, 1))).cuda()
+    wtt = torch.from_numpy(wt).cuda()
+    oh, ow = h + 2 * pad - 2, w + 2 * pad - 2
+    y = torch.full((n, oh, ow, k), float("nan"), dtype=torch.float16, device="cuda")
+    prob = wg.make_problem(xt.data_ptr(), wtt.data_ptr(), y.data_ptr(), n, c, h, w, k, pad, pad)
+    op = wg.Conv2d(prob, wg.default_options(algo=4, layout_nhwc=1))
+    assert op.algo == 4
+    assert op.kernel_names() == ["row4x3"]
+    op(torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    assert op.check_device()[0] == wg.OK
+    got = y.cpu().numpy().transpose(0, 3, 1, 2)
+    assert np.array_equal(got.view(np.uint16), y_nchw.view(np.uint16))
+    _, r64 = O.conv2d_direct(x, wt, pad, pad, nthreads=8)
+    assert O.rel_errors(got, r64)[0] <= TOL
+    op.destroy()
+
+
+def test_row4x3_nhwc_channels_not_a_multiple_of_16_run_non_fused(wg):
+    n, c, h, w, k = 1, 24, 10, 10, 16
+    x, wt = O.uniform_inputs(8, n, c, h, w, k)
+    xt = torch.from_numpy(np.ascontiguousarray(x.transpose(0, 2, 3, 1))).cuda()
+    wtt = torch.from_numpy(wt).cuda()
+    y = torch.empty((n, h, w, k), dtype=torch.float16, device="cuda")
+    prob = wg.make_problem(xt.data_ptr(), wtt.data_ptr(), y.data_ptr(), n, c, h, w, k)
+    op = wg.Conv2d(prob, wg.default_options(algo=4, layout_nhwc=1))
+    assert op.algo == 0
+    op.destroy()
