@@ -57,6 +57,7 @@ int env_algo(int dflt) {
     if (s == "2x3") return CONV2D_ALGO_2X3_NON_FUSED;
     if (s == "fused" || s == "2x3_fused") return CONV2D_ALGO_2X3_FUSED;
     if (s == "auto") return CONV2D_ALGO_AUTO;
+    if (s == "row" || s == "4x3_row") return CONV2D_ALGO_4X3_ROW;
     return dflt;
 }
 

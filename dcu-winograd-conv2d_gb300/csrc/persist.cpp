@@ -6,8 +6,9 @@
 //
 // File: a fixed header (magic, version, the layer's C, K, padding, the
 // transform, operand type and padded sizes, the byte count and an FNV-1a
-// checksum of the payload) followed by U exactly as it lies in device memory,
-// U[E][Cp/8][Kp][8] in the operand type.
+// checksum of the payload) followed by U exactly as it lies in device memory:
+// U[E][Cp/8][Kp][8] in the operand type, or for the row F(4x3) kernel
+// U1[18][Cp16/8][Kp64][8] fp16 (its own transform code in the header).
 #include <cstdint>
 #include <cstdio>
 #include <cstring>

@@ -142,7 +142,8 @@ int conv2d_refresh_filter(const void* param_ptr, void* stream);
  * release path: include/common.h:174 never runs).  The blob is unusable after. */
 int conv2d_destroy(void* param_ptr);
 
-/* Selected algorithm (CONV2D_ALGO_4X3_NON_FUSED .. CONV2D_ALGO_2X3_FUSED), or -1. */
+/* Selected algorithm (CONV2D_ALGO_4X3_NON_FUSED .. CONV2D_ALGO_2X3_FUSED, or
+ * CONV2D_ALGO_4X3_ROW), or -1. */
 int conv2d_get_algo(const void* param_ptr);
 
 /* Device workspace bytes held by the blob. */
