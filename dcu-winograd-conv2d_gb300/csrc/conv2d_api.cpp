@@ -125,8 +125,12 @@ int default_bn(int K) {
 Plan::~Plan() { release(); }
 
 void Plan::release() {
+    if (host_graph) cudaGraphExecDestroy(host_graph);
+    host_graph = nullptr;
     if (host_in_stream) cudaStreamDestroy(host_in_stream);
     if (host_out_stream) cudaStreamDestroy(host_out_stream);
+    if (host_cap_stream) cudaStreamDestroy(host_cap_stream);
+    host_cap_stream = nullptr;
     for (cudaEvent_t& e : host_ev)
         if (e) cudaEventDestroy(e);
     host_in_stream = host_out_stream = nullptr;
@@ -378,82 +382,150 @@ int Plan::run(cudaStream_t s) {
     return CONV2D_OK;
 }
 
-// Host input -> device -> host output.  The batch is cut into image chunks
-// of at least 8 MB of copies each (at most kMaxHostChunks); chunk i's input copy
-// (copy-in stream), compute (caller stream) and output copy (copy-out stream)
-// are ordered by events, so the copies of one chunk overlap the compute of
-// its neighbours and the two copy directions overlap each other.  Smaller
-// chunks shorten the pipeline's fill (first input copy) and drain (last
-// output copy) but run the kernels on fewer tiles; the host link, not the
-// GPU, bounds this call for large inputs.
+// Host input -> device -> host output.  The batch is cut into equal image
+// chunks; chunk i's input copy (copy-in stream), compute (caller stream) and
+// output copy (copy-out stream) are ordered by events, so the copies of one
+// chunk overlap the compute of its neighbours and the two copy directions
+// overlap each other.  The host link bounds this call for large inputs (on
+// the GB300 measured: 206 GB/s in, 190 GB/s out, 312 GB/s for both at once,
+// whether copy engines or SM loads and stores move the bytes).  Chunks hold at
+// least 6 MB of copies and there are at most 8 of them: on the 32 x 256 x 56^2
+// layer (103 MB of copies) 8 chunks took 402-411 us per call, 6 took 420,
+// 4 took 439, 12 and 16 took 450.  WG_CONV2D_HOST_CHUNKS sets another maximum
+// (1-16).  Each chunk's copies and kernels are queued together, the input
+// copies three chunks ahead.
+namespace {
+
+int host_schedule(int n, long long img_copy_bytes, int* sizes) {
+    const long long total = static_cast<long long>(n) * img_copy_bytes;
+    long long max_chunks = 8;
+    if (const char* e = std::getenv("WG_CONV2D_HOST_CHUNKS")) max_chunks = std::max(1, std::min(std::atoi(e), Plan::kMaxHostChunks));
+    const int chunks = static_cast<int>(
+        std::max(1LL, std::min<long long>({static_cast<long long>(n), max_chunks, total / (6LL << 20)})));
+    const int per = (n + chunks - 1) / chunks;
+    int cnt = 0;
+    for (int done = 0; done < n; done += per) sizes[cnt++] = std::min(per, n - done);
+    return cnt;
+}
+
+}  // namespace
+
+const GemmPlan* Plan::host_gemm_for(int nc) {
+    for (int i = 0; i < n_host_plans; ++i)
+        if (host_plan_n[i] == nc) return &host_gemm[i];
+    if (n_host_plans == kMaxHostPlans) return nullptr;
+    const int E = g.alpha * g.alpha;
+    GemmPlan& gp = host_gemm[n_host_plans];
+    if (plan_gemm(gp, op, E, static_cast<long long>(nc) * g.tiles_h * g.tiles_w, g.k, g.kp, g.cp, V, U, Mw, m_fp32,
+                  gemm_full.bn, num_sms, nhwc) != cudaSuccess)
+        return nullptr;
+    host_plan_n[n_host_plans++] = nc;
+    return &gp;
+}
+
+// The pipeline queues about ten operations per chunk; queued one by one from
+// the host they take longer than the copies they order, so the pipeline for a
+// pair of host buffers is captured once into a CUDA graph (on a stream of the
+// plan, as the caller's stream may be the legacy default stream, which cannot
+// be captured) and replayed on the caller's stream by later calls with the
+// same buffers.  Where capture is unavailable the operations are queued
+// directly.
 int Plan::run_host(const void* host_in, void* host_out, cudaStream_t s) {
-    const int n = static_cast<int>(prob.n);
-    const long long in_img_b = static_cast<long long>(g.c) * g.h * g.w * 2;
-    const long long out_img_b = static_cast<long long>(g.k) * g.oh * g.ow * 2;
     int cur = -1;
     if (cudaGetDevice(&cur) == cudaSuccess && cur != device) cudaSetDevice(device);
     if (!filter_ready || opt.filter_policy == 1) {
         int st = filter(s);
         if (st) return st;
     }
-    const long long copy_bytes = static_cast<long long>(n) * (in_img_b + out_img_b);
-    const int chunks = static_cast<int>(
-        std::max(1LL, std::min<long long>({static_cast<long long>(n), kMaxHostChunks, copy_bytes / (8LL << 20)})));
-    const int hc = (n + chunks - 1) / chunks;
-    const int nch = (n + hc - 1) / hc;
     if (!host_in_stream) {
         if (cudaStreamCreateWithFlags(&host_in_stream, cudaStreamNonBlocking) != cudaSuccess ||
-            cudaStreamCreateWithFlags(&host_out_stream, cudaStreamNonBlocking) != cudaSuccess)
+            cudaStreamCreateWithFlags(&host_out_stream, cudaStreamNonBlocking) != cudaSuccess ||
+            cudaStreamCreateWithFlags(&host_cap_stream, cudaStreamNonBlocking) != cudaSuccess)
             return fail(CONV2D_ERR_CUDA, "copy stream creation failed");
         for (cudaEvent_t& e : host_ev)
             if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess)
                 return fail(CONV2D_ERR_CUDA, "event creation failed");
     }
-    if (!single_kernel() && host_chunk_n != hc) {
-        const int E = g.alpha * g.alpha;
-        const int bn = gemm_full.bn;
-        const int tail = n - (nch - 1) * hc;
-        cudaError_t ce = plan_gemm(host_gemm_full, op, E, static_cast<long long>(hc) * g.tiles_h * g.tiles_w, g.k, g.kp,
-                                   g.cp, V, U, Mw, m_fp32, bn, num_sms, nhwc);
-        if (ce == cudaSuccess)
-            ce = plan_gemm(host_gemm_tail, op, E, static_cast<long long>(tail) * g.tiles_h * g.tiles_w, g.k, g.kp, g.cp,
-                           V, U, Mw, m_fp32, bn, num_sms, nhwc);
-        if (ce != cudaSuccess) return cuda_fail(ce, "GEMM plan (host chunks)");
-        host_chunk_n = hc;
+    if (host_graph && (graph_in != host_in || graph_out != host_out)) {
+        cudaGraphExecDestroy(host_graph);
+        host_graph = nullptr;
     }
+    if (!host_graph && cudaStreamBeginCapture(host_cap_stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+        const int st = enqueue_host(host_in, host_out, host_cap_stream);
+        cudaGraph_t graph = nullptr;
+        const cudaError_t ce = cudaStreamEndCapture(host_cap_stream, &graph);
+        if (st == CONV2D_OK && ce == cudaSuccess && graph &&
+            cudaGraphInstantiate(&host_graph, graph, 0) == cudaSuccess) {
+            graph_in = host_in;
+            graph_out = host_out;
+        } else {
+            host_graph = nullptr;
+        }
+        if (graph) cudaGraphDestroy(graph);
+        cudaGetLastError();   // a failed capture leaves its error; the direct path follows
+    }
+    if (host_graph) {
+        const cudaError_t ce = cudaGraphLaunch(host_graph, s);
+        if (ce != cudaSuccess) return cuda_fail(ce, "host pipeline graph launch");
+    } else {
+        const int st = enqueue_host(host_in, host_out, s);
+        if (st) return st;
+    }
+    const cudaError_t ce = cudaStreamSynchronize(s);
+    if (ce != cudaSuccess) return cuda_fail(ce, "stream sync");
+    return CONV2D_OK;
+}
+
+int Plan::enqueue_host(const void* host_in, void* host_out, cudaStream_t s) {
+    const int n = static_cast<int>(prob.n);
+    const long long in_img_b = static_cast<long long>(g.c) * g.h * g.w * 2;
+    const long long out_img_b = static_cast<long long>(g.k) * g.oh * g.ow * 2;
+    int sizes[kMaxHostChunks];
+    const int nch = host_schedule(n, in_img_b + out_img_b, sizes);
+    // the non-fused workspace holds chunk_n images: a host chunk runs as
+    // ranges of at most that many
+    const int cap = single_kernel() ? n : chunk_n;
     cudaEvent_t* ev_in = host_ev;                     // [kMaxHostChunks]
     cudaEvent_t* ev_done = host_ev + kMaxHostChunks;  // [kMaxHostChunks]
     cudaEvent_t ev_start = host_ev[2 * kMaxHostChunks], ev_end = host_ev[2 * kMaxHostChunks + 1];
     // the copies must not overwrite the input before earlier work on s is done
     cudaEventRecord(ev_start, s);
     cudaStreamWaitEvent(host_in_stream, ev_start, 0);
-    for (int i = 0; i < nch; ++i) {
-        const int n0 = i * hc, nc = std::min(hc, n - n0);
-        cudaError_t ce = cudaMemcpyAsync(static_cast<char*>(prob.in) + n0 * in_img_b,
-                                         static_cast<const char*>(host_in) + n0 * in_img_b, nc * in_img_b,
-                                         cudaMemcpyHostToDevice, host_in_stream);
-        if (ce != cudaSuccess) return cuda_fail(ce, "input copy");
+    cudaStreamWaitEvent(host_out_stream, ev_start, 0);
+    int first[kMaxHostChunks + 1];
+    first[0] = 0;
+    for (int i = 0; i < nch; ++i) first[i + 1] = first[i] + sizes[i];
+    auto copy_in = [&](int i) {
+        const cudaError_t ce = cudaMemcpyAsync(static_cast<char*>(prob.in) + first[i] * in_img_b,
+                                               static_cast<const char*>(host_in) + first[i] * in_img_b,
+                                               sizes[i] * in_img_b, cudaMemcpyHostToDevice, host_in_stream);
         cudaEventRecord(ev_in[i], host_in_stream);
-    }
-    for (int i = 0; i < nch; ++i) {
-        const int n0 = i * hc, nc = std::min(hc, n - n0);
+        return ce;
+    };
+    // input copies are queued three chunks ahead of the chunk being queued
+    constexpr int kAhead = 3;
+    for (int i = 0; i < std::min(kAhead, nch); ++i)
+        if (cudaError_t ce = copy_in(i); ce != cudaSuccess) return cuda_fail(ce, "input copy");
+    for (int i = 0, n0 = 0; i < nch; n0 += sizes[i], ++i) {
+        cudaError_t ce = i + kAhead < nch ? copy_in(i + kAhead) : cudaSuccess;
+        if (ce != cudaSuccess) return cuda_fail(ce, "input copy");
         cudaStreamWaitEvent(s, ev_in[i], 0);
-        const int st = run_range(n0, nc, i == nch - 1 ? &host_gemm_tail : &host_gemm_full, s);
-        if (st) return st;
+        for (int r0 = n0; r0 < n0 + sizes[i]; r0 += cap) {
+            const int nc = std::min(cap, n0 + sizes[i] - r0);
+            const GemmPlan* gp = nullptr;
+            if (!single_kernel() && !(gp = host_gemm_for(nc))) return fail(CONV2D_ERR_CUDA, "GEMM plan (host chunks) failed");
+            const int st = run_range(r0, nc, gp, s);
+            if (st) return st;
+        }
         cudaEventRecord(ev_done[i], s);
-    }
-    for (int i = 0; i < nch; ++i) {
-        const int n0 = i * hc, nc = std::min(hc, n - n0);
         cudaStreamWaitEvent(host_out_stream, ev_done[i], 0);
-        cudaError_t ce = cudaMemcpyAsync(static_cast<char*>(host_out) + n0 * out_img_b,
-                                         static_cast<const char*>(prob.out) + n0 * out_img_b, nc * out_img_b,
-                                         cudaMemcpyDeviceToHost, host_out_stream);
+        ce = cudaMemcpyAsync(static_cast<char*>(host_out) + n0 * out_img_b,
+                             static_cast<const char*>(prob.out) + n0 * out_img_b, sizes[i] * out_img_b,
+                             cudaMemcpyDeviceToHost, host_out_stream);
         if (ce != cudaSuccess) return cuda_fail(ce, "output copy");
     }
     cudaEventRecord(ev_end, host_out_stream);
     cudaStreamWaitEvent(s, ev_end, 0);
-    cudaError_t ce = cudaStreamSynchronize(s);
-    if (ce != cudaSuccess) return cuda_fail(ce, "stream sync");
     return CONV2D_OK;
 }
 

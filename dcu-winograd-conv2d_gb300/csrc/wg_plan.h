@@ -61,11 +61,18 @@ struct Plan {
     // when set, run() records an event on the stream after every launch
     cudaEvent_t* marks = nullptr;
     int n_marks = 0, max_marks = 0;
-    // host-buffer pipeline: image chunks, their GEMM plans, copy streams, events
-    int host_chunk_n = 0;
-    GemmPlan host_gemm_full{}, host_gemm_tail{};
+    // host-buffer pipeline: image chunks, a GEMM plan per chunk size, copy
+    // streams, events
+    static constexpr int kMaxHostPlans = 8;
+    int host_plan_n[kMaxHostPlans] = {};
+    GemmPlan host_gemm[kMaxHostPlans]{};
+    int n_host_plans = 0;
     cudaStream_t host_in_stream = nullptr, host_out_stream = nullptr;
-    static constexpr int kMaxHostChunks = 8;
+    cudaStream_t host_cap_stream = nullptr;   // compute stream of the captured pipeline
+    cudaGraphExec_t host_graph = nullptr;     // the pipeline for (graph_in, graph_out)
+    const void* graph_in = nullptr;
+    void* graph_out = nullptr;
+    static constexpr int kMaxHostChunks = 16;
     cudaEvent_t host_ev[2 * kMaxHostChunks + 2] = {};
 
     // one kernel per call, no Winograd-domain workspace
@@ -79,6 +86,10 @@ struct Plan {
     int run_range(int n0, int nc, const GemmPlan* gp, cudaStream_t s);
     // host input -> device -> host output, copies overlapped with compute
     int run_host(const void* host_in, void* host_out, cudaStream_t s);
+    // queue the host-buffer pipeline with cs as the compute stream
+    int enqueue_host(const void* host_in, void* host_out, cudaStream_t cs);
+    // GEMM plan for a host chunk of nc images (made once per size), or null
+    const GemmPlan* host_gemm_for(int nc);
     void mark(cudaStream_t s);
     void release();
 };

@@ -245,14 +245,14 @@ def test_refresh_filter_after_in_place_change(wg):
 
 
 HOST_CASES = [(a, n, 24, 16, 24) for a in (0, 1, 2, 4) for n in (1, 2, 7)] + \
-    [(a, 11, 64, 100, 64) for a in (0, 1, 2, 4)]  # 28.2 MB of copies: 3 chunks of 4, 4, 3 images
+    [(a, 11, 64, 100, 64) for a in (0, 1, 2, 4)]  # 28.2 MB of copies: 4 chunks of 3, 3, 3, 2 images
 
 
 @pytest.mark.parametrize("algo,n,c,h,k", HOST_CASES)
 def test_host_buffer_entry_point(wg, algo, n, c, h, k):
     """Host in -> device -> host out, with the batch cut into overlapped
-    chunks of at least 8 MB of copies (one chunk for the small cases, three
-    uneven ones for the large); equal to the device-buffer call bit for bit."""
+    chunks of at least 6 MB of copies (one chunk for the small cases, four
+    for the large); equal to the device-buffer call bit for bit."""
     x, wt = O.uniform_inputs(13 + n, n, c, h, h, k)
     xt = torch.empty((n, c, h, h), dtype=torch.float16, device="cuda")
     wtt = torch.from_numpy(wt).cuda()
@@ -393,7 +393,7 @@ def test_nhwc_refuses_channels_not_a_multiple_of_8(wg):
 @pytest.mark.parametrize("algo", [0, 1, 2, 4])
 def test_host_chunks_of_unaligned_images(wg, algo):
     """Images of 1,202,850 bytes: every host chunk after the first starts off
-    a 16-byte boundary (two chunks of 4 images, 19 MB of copies)."""
+    a 16-byte boundary (chunks of 3, 3 and 2 images, 19 MB of copies)."""
     n, c, h, k = 8, 33, 135, 33
     x, wt = O.uniform_inputs(77, n, c, h, h, k)
     xt = torch.empty((n, c, h, h), dtype=torch.float16, device="cuda")
@@ -410,3 +410,24 @@ def test_host_chunks_of_unaligned_images(wg, algo):
     assert st == wg.OK, site
     _, r64 = O.conv2d_direct(x, wt, nthreads=8)
     assert O.rel_errors(hout.numpy(), r64)[0] <= TOL[algo_m(algo)]
+
+
+@pytest.mark.parametrize("algo", [0, 1])
+def test_host_chunks_over_a_smaller_image_chunk_workspace(wg, algo):
+    """With image chunking the non-fused workspace holds one image; every host
+    chunk then runs as ranges of one image, and the result equals the
+    device-buffer call bit for bit."""
+    n, c, h, k = 11, 64, 100, 64
+    x, wt = O.uniform_inputs(5, n, c, h, h, k)
+    xt = torch.empty((n, c, h, h), dtype=torch.float16, device="cuda")
+    wtt = torch.from_numpy(wt).cuda()
+    y = torch.empty((n, k, h, h), dtype=torch.float16, device="cuda")
+    prob = wg.make_problem(xt.data_ptr(), wtt.data_ptr(), y.data_ptr(), n, c, h, h, k)
+    op = wg.Conv2d(prob, opts_for(wg, algo, l2_chunk_bytes=1))
+    hin = torch.from_numpy(x).pin_memory()
+    hout = torch.empty((n, k, h, h), dtype=torch.float16).pin_memory()
+    torch.cuda.synchronize()
+    op.host(hin.data_ptr(), hout.data_ptr(), torch.cuda.current_stream().cuda_stream)
+    assert op.check_device()[0] == wg.OK
+    dev, _ = run(wg, x, wt, 1, 1, opts_for(wg, algo))
+    assert np.array_equal(hout.numpy().view(np.uint16), dev.view(np.uint16))
