@@ -270,7 +270,7 @@ int Plan::build(const problem_t* pr, const conv2d_options_t* opt_in) {
         if (ce != cudaSuccess) return cuda_fail(ce, "row F(4x3) plan");
         launches = 1;
         info_grid = static_cast<unsigned>(std::min<long long>(row4x3_items(row, static_cast<int>(pr->n)), num_sms));
-        info_threads = 320;
+        info_threads = static_cast<unsigned>(row4x3_threads(row));
         info_smem = row.smem_bytes;
     } else {
         if (nhwc) {

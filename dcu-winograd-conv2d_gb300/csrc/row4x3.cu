@@ -903,6 +903,8 @@ cudaError_t launch_row4x3i(const RowPlan& rp, void* out, int n_base, int n_image
                       static_cast<__half*>(out), gg, n_base, n_images, err);
 }
 
+int row4x3_threads(const RowPlan& rp) { return rp.interleaved ? kThreadsI : kThreads; }
+
 long long row4x3_filter_bytes(const RowPlan& rp) { return static_cast<long long>(kE * kTaps) * rp.kp64 * rp.cp16 * 2; }
 
 long long row4x3_items(const RowPlan& rp, int n_images) {

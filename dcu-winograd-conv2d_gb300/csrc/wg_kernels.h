@@ -206,6 +206,7 @@ cudaError_t plan_row4x3i(RowPlan& rp, const Geom& g, const void* U, bool out_nhw
 // tensor map of the interleaved kernel's input x[n_total][h][w][cs]
 cudaError_t bind_row4x3i_input(RowPlan& rp, const void* x_nhwc, int cs, int h, int w, int n_total);
 long long row4x3_filter_bytes(const RowPlan& rp);
+int row4x3_threads(const RowPlan& rp);                      // threads per CTA of the planned kernel
 long long row4x3_items(const RowPlan& rp, int n_images);   // CTA work items of n images
 // U1[e*3 + r][Cp16/8][Kp64][8] fp16 from KCRS fp16 weights
 cudaError_t launch_row4x3_filter(const RowPlan& rp, const void* weight, void* U, cudaStream_t stream);

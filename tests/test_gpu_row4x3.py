@@ -102,3 +102,22 @@ def test_row4x3_nhwc_channels_not_a_multiple_of_16_run_non_fused(wg):
     op = wg.Conv2d(prob, wg.default_options(algo=4, layout_nhwc=1))
     assert op.algo == 0
     op.destroy()
+
+
+def test_row4x3_reports_its_launch_shape(wg):
+    """getkernelInfo describes the kernel that runs: the NCHW kernel has 608
+    threads per CTA (16 producer warps + MMA, staging and filter warps), the
+    NHWC kernel 352, and at most one CTA per SM."""
+    x, wt = O.uniform_inputs(3, 2, 32, 14, 30, 48)
+    y, op = _run(wg, x, wt, 1, 1, algo=4)
+    assert op.algo == 4 and op.info.threadx == 608
+    assert 1 <= op.info.blockx <= torch.cuda.get_device_properties(0).multi_processor_count
+    _, r64 = O.conv2d_direct(x, wt)
+    assert O.rel_errors(y, r64)[0] <= TOL
+    xt = torch.from_numpy(np.ascontiguousarray(x.transpose(0, 2, 3, 1))).cuda()
+    wtt = torch.from_numpy(wt).cuda()
+    yn = torch.empty((2, 14, 30, 48), dtype=torch.float16, device="cuda")
+    opn = wg.Conv2d(wg.make_problem(xt.data_ptr(), wtt.data_ptr(), yn.data_ptr(), 2, 32, 14, 30, 48),
+                    wg.default_options(algo=4, layout_nhwc=1))
+    assert opn.algo == 4 and opn.info.threadx == 352
+    opn.destroy()
