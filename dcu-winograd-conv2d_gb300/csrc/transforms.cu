@@ -164,7 +164,8 @@ __global__ void __launch_bounds__(256) tile_scale_kernel(const typename IO<XB>::
 
 constexpr int kInComputeWarps = 7;
 constexpr int kInThreads = 32 * (kInComputeWarps + 1);  // + one producer warp
-constexpr int kInHeader = 64;   // four mbarriers, an abort flag, 16 zero bytes
+constexpr int kInMaxBufs = 3;   // staging buffers: 3 where two CTAs of them fit an SM, else 2
+constexpr int kInHeader = 96;   // 2 x kInMaxBufs mbarriers, an abort flag, 16 zero bytes
 constexpr int kInSlack = 256;   // bytes before and after the two buffers: reads
                                 // of columns in the padding (masked to zero)
                                 // stay inside the CTA's shared memory
@@ -364,22 +365,22 @@ __device__ __forceinline__ void in_compute(const InDesc& d, long long local, con
 
 // descs: one problem (kernel parameter) or many (device array sorted by
 // blk_begin); items [0, total) are split round robin over the grid.
-// Warp kInComputeWarps is the producer: it stages item k into buffer k % 2
-// once the compute warps have released that buffer (empty barrier, one
-// arrival per compute warp) and signals the full barrier; the compute warps
-// never wait for one another.
+// Warp kInComputeWarps is the producer: it stages item k into buffer
+// k % nbufs once the compute warps have released that buffer (empty barrier,
+// one arrival per compute warp) and signals the full barrier; the compute
+// warps never wait for one another.
 template <class TF, class OutT, bool SCALED, bool XB>
-__device__ __forceinline__ void input_body(const InDesc* descs, int ndesc, long long total, int buf_bytes,
+__device__ __forceinline__ void input_body(const InDesc* descs, int ndesc, long long total, int buf_bytes, int nbufs,
                                            unsigned char* smem_raw, DevErr* err) {
     constexpr int M = TF::M, A = TF::ALPHA;
     uint64_t* full = reinterpret_cast<uint64_t*>(smem_raw);
-    uint64_t* empty = full + 2;
-    volatile int* abort_flag = reinterpret_cast<volatile int*>(full + 4);
-    unsigned char* zero = smem_raw + 48;  // 16 zero bytes: the ALPHA elements of a padding row
+    uint64_t* empty = full + kInMaxBufs;
+    volatile int* abort_flag = reinterpret_cast<volatile int*>(full + 2 * kInMaxBufs);
+    unsigned char* zero = smem_raw + 64;  // 16 zero bytes: the ALPHA elements of a padding row
     unsigned char* bufs = smem_raw + kInHeader + kInSlack;
     const int warp = threadIdx.x >> 5;
     if (threadIdx.x == 0) {
-        for (int i = 0; i < 2; ++i) {
+        for (int i = 0; i < kInMaxBufs; ++i) {
             mbar_init(&full[i], 32);                // every producer lane arrives
             mbar_init(&empty[i], kInComputeWarps);  // one arrival per compute warp
         }
@@ -393,16 +394,16 @@ __device__ __forceinline__ void input_body(const InDesc* descs, int ndesc, long 
     if (warp == kInComputeWarps) {
         int k = 0;
         for (long long item = blockIdx.x; item < total; item += gridDim.x, ++k) {
-            const int b = k & 1;
-            if (!mbar_wait(&empty[b], ((k >> 1) & 1) ^ 1u, abort_flag, err, ERR_SITE_EMPTY)) break;
+            const int b = k % nbufs;
+            if (!mbar_wait(&empty[b], ((k / nbufs) & 1) ^ 1u, abort_flag, err, ERR_SITE_EMPTY)) break;
             const InDesc& d = in_desc_of(descs, ndesc, item);
             in_issue<M, A>(d, item - d.blk_begin, bufs + b * buf_bytes, &full[b]);
         }
     } else {
         int k = 0;
         for (long long item = blockIdx.x; item < total; item += gridDim.x, ++k) {
-            const int b = k & 1;
-            if (!mbar_wait(&full[b], (k >> 1) & 1, abort_flag, err, ERR_SITE_FULL)) break;
+            const int b = k % nbufs;
+            if (!mbar_wait(&full[b], (k / nbufs) & 1, abort_flag, err, ERR_SITE_FULL)) break;
             const InDesc& d = in_desc_of(descs, ndesc, item);
             in_compute<TF, OutT, SCALED, XB>(d, item - d.blk_begin, bufs + b * buf_bytes, zero, warp);
             __syncwarp();
@@ -419,16 +420,16 @@ __device__ __forceinline__ void input_body(const InDesc* descs, int ndesc, long 
 
 template <class TF, class OutT, bool SCALED, bool XB>
 __global__ void __launch_bounds__(kInThreads, 2)
-    input_transform_kernel(const __grid_constant__ InDesc d, long long total, int buf_bytes, DevErr* err) {
+    input_transform_kernel(const __grid_constant__ InDesc d, long long total, int buf_bytes, int nbufs, DevErr* err) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    input_body<TF, OutT, SCALED, XB>(&d, 1, total, buf_bytes, smem_raw, err);
+    input_body<TF, OutT, SCALED, XB>(&d, 1, total, buf_bytes, nbufs, smem_raw, err);
 }
 
 template <class TF, class OutT, bool SCALED>
 __global__ void __launch_bounds__(kInThreads, 2) input_transform_grouped(const InDesc* __restrict__ descs, int ndesc,
                                                                        long long total, int buf_bytes, DevErr* err) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    input_body<TF, OutT, SCALED, false>(descs, ndesc, total, buf_bytes, smem_raw, err);
+    input_body<TF, OutT, SCALED, false>(descs, ndesc, total, buf_bytes, 2, smem_raw, err);
 }
 
 // ---- output transform ----------------------------------------------------------
@@ -618,7 +619,7 @@ int sm_count() {
 constexpr int kInBufBudget = 56 * 1024;   // per buffer: two CTAs of two buffers per SM
 constexpr int kSmemPerSm = 233472;        // shared memory of one SM (228 KB)
 
-int in_smem_total(int buf) { return kInHeader + 2 * kInSlack + 2 * buf; }
+int in_smem_total(int buf) { return kInHeader + 2 * kInSlack + 2 * buf; }   // two buffers
 int in_ctas_per_sm(int smem) { return std::max(1, std::min(2, kSmemPerSm / (smem + 1024))); }
 
 // Tile-row block tb and channel block cb: the items (image, tile-row block,
@@ -660,12 +661,17 @@ InBlocking choose_in_blocking(const Geom& g) {
 template <class TF, class OutT, bool SCALED, bool XB = false>
 cudaError_t input_launch(const InDesc& d, int smem, DevErr* err, cudaStream_t s) {
     auto kern = input_transform_kernel<TF, OutT, SCALED, XB>;
+    // a third staging buffer where two CTAs of three still fit an SM: the
+    // next item's copies then start two items ahead of the arithmetic
+    const int buf = (smem - kInHeader - 2 * kInSlack) / 2;
+    const int smem3 = kInHeader + 2 * kInSlack + 3 * buf;
+    const int nbufs = in_ctas_per_sm(smem3) >= 2 ? 3 : 2;
+    if (nbufs == 3) smem = smem3;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e != cudaSuccess) return e;
     const long long total = d.gx * d.gy;
     const long long grid = std::min<long long>(total, static_cast<long long>(sm_count()) * in_ctas_per_sm(smem));
-    return launch_pdl(kern, dim3(static_cast<unsigned>(grid)), dim3(kInThreads), smem, s, d, total,
-                      (smem - kInHeader - 2 * kInSlack) / 2, err);
+    return launch_pdl(kern, dim3(static_cast<unsigned>(grid)), dim3(kInThreads), smem, s, d, total, buf, nbufs, err);
 }
 
 template <class TF, class OutT, bool SCALED>
