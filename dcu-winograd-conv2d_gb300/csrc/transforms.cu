@@ -156,9 +156,9 @@ __global__ void __launch_bounds__(256) tile_scale_kernel(const typename IO<XB>::
 // ---- input transform -------------------------------------------------------------
 // Persistent CTAs walk a list of work items (image, block of tile rows, block
 // of up to 32 channels).  Each item's input rows are staged in shared memory
-// with one cp.async.bulk per channel, issued by warp 0 one item ahead into the
-// other half of a double buffer, so the copies of item i+1 overlap the
-// arithmetic of item i.  A thread transforms one channel pair of one tile in
+// with one cp.async.bulk per channel, issued by the producer warp one or two
+// items ahead into a ring of two or three buffers, so the copies of the next
+// items overlap the arithmetic of this one.  A thread transforms one channel pair of one tile in
 // packed fp32x2 arithmetic; four lanes complete one 16-byte granule row and a
 // warp of eight consecutive tiles stores 128 contiguous bytes per element.
 
