@@ -243,7 +243,7 @@ __device__ __forceinline__ const InDesc& in_desc_of(const InDesc* descs, int nde
     return descs[lo];
 }
 
-// Warp 0: lane c stages channel c of the item (rows [ylo, yhi), whole width)
+// The producer warp: lane c stages channel c of the item (rows [ylo, yhi), whole width)
 // at byte c*stride + (src & 15) of buf and arrives on bar with its byte count.
 // Bulk copies stop at the last 16-byte boundary of the input tensor; the few
 // elements after it are copied with plain loads before the arrival (whose
