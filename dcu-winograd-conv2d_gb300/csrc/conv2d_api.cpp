@@ -423,13 +423,15 @@ const GemmPlan* Plan::host_gemm_for(int nc) {
     return &gp;
 }
 
-// The pipeline queues about ten operations per chunk; queued one by one from
-// the host they take longer than the copies they order, so the pipeline for a
-// pair of host buffers is captured once into a CUDA graph (on a stream of the
-// plan, as the caller's stream may be the legacy default stream, which cannot
-// be captured) and replayed on the caller's stream by later calls with the
-// same buffers.  Where capture is unavailable the operations are queued
-// directly.
+// The pipeline queues about ten operations per chunk.  With
+// WG_CONV2D_HOST_GRAPH=1 the pipeline for a pair of host buffers is captured
+// once into a CUDA graph (on a stream of the plan, as the caller's stream may
+// be the legacy default stream, which cannot be captured) and replayed on the
+// caller's stream by later calls with the same buffers.  By default the
+// operations are queued directly: at 8 chunks the host queues them faster than
+// the copies run and the first copies start at once, while a graph launch
+// front-loads its set-up (on the 32 x 256 x 56^2 layer: 413-418 us per call
+// queued directly, 434-437 us replayed).
 int Plan::run_host(const void* host_in, void* host_out, cudaStream_t s) {
     int cur = -1;
     if (cudaGetDevice(&cur) == cudaSuccess && cur != device) cudaSetDevice(device);
@@ -450,7 +452,9 @@ int Plan::run_host(const void* host_in, void* host_out, cudaStream_t s) {
         cudaGraphExecDestroy(host_graph);
         host_graph = nullptr;
     }
-    if (!host_graph && cudaStreamBeginCapture(host_cap_stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+    static const bool use_graph = env_int("WG_CONV2D_HOST_GRAPH", 0) != 0;
+    if (use_graph && !host_graph &&
+        cudaStreamBeginCapture(host_cap_stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
         const int st = enqueue_host(host_in, host_out, host_cap_stream);
         cudaGraph_t graph = nullptr;
         const cudaError_t ce = cudaStreamEndCapture(host_cap_stream, &graph);
