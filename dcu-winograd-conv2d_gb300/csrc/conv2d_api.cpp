@@ -452,7 +452,7 @@ int Plan::run_host(const void* host_in, void* host_out, cudaStream_t s) {
         cudaGraphExecDestroy(host_graph);
         host_graph = nullptr;
     }
-    static const bool use_graph = env_int("WG_CONV2D_HOST_GRAPH", 0) != 0;
+    const bool use_graph = env_int("WG_CONV2D_HOST_GRAPH", 0) != 0;
     if (use_graph && !host_graph &&
         cudaStreamBeginCapture(host_cap_stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
         const int st = enqueue_host(host_in, host_out, host_cap_stream);
