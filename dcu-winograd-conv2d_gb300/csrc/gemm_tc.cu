@@ -56,12 +56,12 @@ struct GemmCfg {
 // one tile row p into the granule layout.
 template <class MT>
 __device__ __forceinline__ void store32(MT* Mw, const uint32_t (&r)[32], long long P, long long p, int k0, int kg_count,
-                                        int e);
+                                        int e, uint64_t pol);
 
 // fp16 M[e][Kp/8][P][8]: four granules
 template <>
 __device__ __forceinline__ void store32<__half>(__half* Mw, const uint32_t (&r)[32], long long P, long long p, int k0,
-                                                int kg_count, int e) {
+                                                int kg_count, int e, uint64_t pol) {
     uint32_t h[16];
 #pragma unroll
     for (int i = 0; i < 16; ++i) {
@@ -72,20 +72,20 @@ __device__ __forceinline__ void store32<__half>(__half* Mw, const uint32_t (&r)[
 #pragma unroll
     for (int j = 0; j < 4; ++j)
         if (g0 + j < kg_count)
-            *reinterpret_cast<uint4*>(Mw + ((static_cast<long long>(e) * kg_count + g0 + j) * P + p) * 8) =
-                make_uint4(h[4 * j], h[4 * j + 1], h[4 * j + 2], h[4 * j + 3]);
+            st_hint_v4(Mw + ((static_cast<long long>(e) * kg_count + g0 + j) * P + p) * 8,
+                       make_uint4(h[4 * j], h[4 * j + 1], h[4 * j + 2], h[4 * j + 3]), pol);
 }
 
 // fp32 M[e][Kp/4][P][4]: eight granules
 template <>
 __device__ __forceinline__ void store32<float>(float* Mw, const uint32_t (&r)[32], long long P, long long p, int k0,
-                                               int kg_count, int e) {
+                                               int kg_count, int e, uint64_t pol) {
     const int g0 = k0 / 4;
 #pragma unroll
     for (int j = 0; j < 8; ++j)
         if (g0 + j < kg_count)
-            *reinterpret_cast<uint4*>(Mw + ((static_cast<long long>(e) * kg_count + g0 + j) * P + p) * 4) =
-                make_uint4(r[4 * j], r[4 * j + 1], r[4 * j + 2], r[4 * j + 3]);
+            st_hint_v4(Mw + ((static_cast<long long>(e) * kg_count + g0 + j) * P + p) * 4,
+                       make_uint4(r[4 * j], r[4 * j + 1], r[4 * j + 2], r[4 * j + 3]), pol);
 }
 
 // Row-major M[e][P][Kp] (the NHWC output path): 4 consecutive columns of
@@ -171,6 +171,7 @@ __device__ __forceinline__ void gemm_body(const GemmDesc* __restrict__ descs, in
 
     if (warp == 0) {
         if (lane == 0) {
+            const uint64_t drop = l2_evict_first(), keep_as_is = l2_evict_unchanged();
             int stage = 0;
             uint32_t phase = 0;
             int pi = 0, prefetched = -1;
@@ -189,7 +190,9 @@ __device__ __forceinline__ void gemm_body(const GemmDesc* __restrict__ descs, in
                         break;
                     }
                     mbar_arrive_expect_tx(&full[stage], Cfg::kStageBytes);
-                    tma_load_4d(sA + stage * kTileABytes, &d.tmA, &full[stage], 0, it.mb * (kBM / 8), kb * 8, it.e);
+                    // V: dropped from L2 by its last reader (the last N block)
+                    tma_load_4d_hint(sA + stage * kTileABytes, &d.tmA, &full[stage], 0, it.mb * (kBM / 8), kb * 8, it.e,
+                                     it.nb == d.n_blocks - 1 ? drop : keep_as_is);
                     tma_load_4d(sB + stage * Cfg::kTileB, &d.tmB, &full[stage], 0, it.nb * (BN / 8), kb * 8, it.e);
                     if (++stage == S) {
                         stage = 0;
@@ -246,6 +249,7 @@ __device__ __forceinline__ void gemm_body(const GemmDesc* __restrict__ descs, in
         // epilogue warps 2..9: TMEM lane quarter = warp % 4; warps 2-5 store
         // the first half of the accumulator columns, 6-9 the second (BN >= 64)
         const int quarter = warp & 3;
+        const uint64_t m_pol = l2_evict_first();   // M is larger than L2: do not let it push V out
         const int half = (warp - 2) >> 2;
         const int row = quarter * 32 + lane;
         int acc = 0;
@@ -294,7 +298,7 @@ __device__ __forceinline__ void gemm_body(const GemmDesc* __restrict__ descs, in
                     }
                     __syncwarp();
                 } else if (p < P) {
-                    store32<MT>(Mw, r[ch & 1], P, p, it.nb * BN + col0 + ch * 32, kg_count, it.e);
+                    store32<MT>(Mw, r[ch & 1], P, p, it.nb * BN + col0 + ch * 32, kg_count, it.e, m_pol);
                 }
                 if (ch + 1 < kChunks) tc_wait_ld(r[(ch + 1) & 1]);
             }

@@ -275,7 +275,7 @@ __device__ __forceinline__ void in_issue(const InDesc& d, long long local, unsig
 // Compute warp cw (of kInComputeWarps) transforms its share of the item:
 // lanes are (tile offset q, channel pair sub) with four pairs per granule
 // row; tiles q, q + Q, q + 2Q, ... of the item for every granule.
-template <class TF, class OutT, bool SCALED, bool XB>
+template <class TF, class OutT, bool SCALED, bool XB, bool KEEP>
 __device__ __forceinline__ void in_compute(const InDesc& d, long long local, const unsigned char* buf,
                                            const unsigned char* zero, int cw) {
     constexpr int M = TF::M, A = TF::ALPHA;
@@ -297,6 +297,7 @@ __device__ __forceinline__ void in_compute(const InDesc& d, long long local, con
     const int q = cw * 8 + (lane >> 2);
     const int dtr = Q / tiles_w, dtw = Q - dtr * tiles_w;
     OutT* __restrict__ V = static_cast<OutT*>(d.V);
+    const uint64_t keep = KEEP ? l2_evict_last() : 0;
     for (int g = 0; g < G; ++g) {
         const int c = g * 8 + sub * 2;  // channel pair (c, c+1) of the block
         const bool ok0 = c < it.nch, ok1 = c + 1 < it.nch;
@@ -347,10 +348,15 @@ __device__ __forceinline__ void in_compute(const InDesc& d, long long local, con
                 for (int i = 0; i < A; ++i) pk[i * A + j] = pack2v<OutT>(v[i]);
             }
             // element e at dst + e * estride, stored in order with one running pointer
+            // V is read once by the GEMM that follows: kept in L2 when it fits
+            // (KEEP; plain stores otherwise)
             OutT* dst = vg + static_cast<long long>(t) * 8;
 #pragma unroll
             for (int e = 0; e < A * A; ++e) {
-                *reinterpret_cast<uint32_t*>(dst) = pk[e];
+                if constexpr (KEEP)
+                    st_hint_b32(dst, pk[e], keep);
+                else
+                    *reinterpret_cast<uint32_t*>(dst) = pk[e];
                 dst += estride;
             }
             tw += dtw;
@@ -369,7 +375,7 @@ __device__ __forceinline__ void in_compute(const InDesc& d, long long local, con
 // k % nbufs once the compute warps have released that buffer (empty barrier,
 // one arrival per compute warp) and signals the full barrier; the compute
 // warps never wait for one another.
-template <class TF, class OutT, bool SCALED, bool XB>
+template <class TF, class OutT, bool SCALED, bool XB, bool KEEP>
 __device__ __forceinline__ void input_body(const InDesc* descs, int ndesc, long long total, int buf_bytes, int nbufs,
                                            unsigned char* smem_raw, DevErr* err) {
     constexpr int M = TF::M, A = TF::ALPHA;
@@ -405,7 +411,7 @@ __device__ __forceinline__ void input_body(const InDesc* descs, int ndesc, long 
             const int b = k % nbufs;
             if (!mbar_wait(&full[b], (k / nbufs) & 1, abort_flag, err, ERR_SITE_FULL)) break;
             const InDesc& d = in_desc_of(descs, ndesc, item);
-            in_compute<TF, OutT, SCALED, XB>(d, item - d.blk_begin, bufs + b * buf_bytes, zero, warp);
+            in_compute<TF, OutT, SCALED, XB, KEEP>(d, item - d.blk_begin, bufs + b * buf_bytes, zero, warp);
             __syncwarp();
             if ((threadIdx.x & 31) == 0) mbar_arrive(&empty[b]);
         }
@@ -418,18 +424,18 @@ __device__ __forceinline__ void input_body(const InDesc* descs, int ndesc, long 
     }
 }
 
-template <class TF, class OutT, bool SCALED, bool XB>
+template <class TF, class OutT, bool SCALED, bool XB, bool KEEP>
 __global__ void __launch_bounds__(kInThreads, 2)
     input_transform_kernel(const __grid_constant__ InDesc d, long long total, int buf_bytes, int nbufs, DevErr* err) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    input_body<TF, OutT, SCALED, XB>(&d, 1, total, buf_bytes, nbufs, smem_raw, err);
+    input_body<TF, OutT, SCALED, XB, KEEP>(&d, 1, total, buf_bytes, nbufs, smem_raw, err);
 }
 
 template <class TF, class OutT, bool SCALED>
 __global__ void __launch_bounds__(kInThreads, 2) input_transform_grouped(const InDesc* __restrict__ descs, int ndesc,
                                                                        long long total, int buf_bytes, DevErr* err) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    input_body<TF, OutT, SCALED, false>(descs, ndesc, total, buf_bytes, 2, smem_raw, err);
+    input_body<TF, OutT, SCALED, false, false>(descs, ndesc, total, buf_bytes, 2, smem_raw, err);
 }
 
 // ---- output transform ----------------------------------------------------------
@@ -532,9 +538,10 @@ __device__ __forceinline__ void output_staged_body(const OutDesc* descs, int nde
             for (int e = lane; e < E; e += 32) mine += bytes;
             if (mine) fence_proxy_async_smem();  // earlier reads of this buffer before the async writes
             mbar_arrive_expect_tx(&full[b], mine);
+            const uint64_t drop = l2_evict_first();   // M is read once
             for (int e = lane; e < E; e += 32)
-                bulk_g2s(bufs + b * kItemBytes + e * (kOsTiles * 16),
-                         Mb + ((static_cast<long long>(e) * KG + g) * P + p0) * 16, bytes, &full[b]);
+                bulk_g2s_hint(bufs + b * kItemBytes + e * (kOsTiles * 16),
+                              Mb + ((static_cast<long long>(e) * KG + g) * P + p0) * 16, bytes, &full[b], drop);
         }
     } else {
         const int t = threadIdx.x >> 1, hh = threadIdx.x & 1;
@@ -604,6 +611,18 @@ struct InBlocking {
     int tb, nbh, cb, stride, buf;
 };
 
+long long l2_bytes() {
+    static long long cached[64] = {};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 0;
+    if (!cached[dev]) {
+        int v = 0;
+        cudaDeviceGetAttribute(&v, cudaDevAttrL2CacheSize, dev);
+        cached[dev] = v > 0 ? v : 1;
+    }
+    return cached[dev];
+}
+
 int sm_count() {
     static int cached[64] = {0};
     int dev = 0;
@@ -658,9 +677,9 @@ InBlocking choose_in_blocking(const Geom& g) {
     return best;
 }
 
-template <class TF, class OutT, bool SCALED, bool XB = false>
+template <class TF, class OutT, bool SCALED, bool XB = false, bool KEEP = false>
 cudaError_t input_launch(const InDesc& d, int smem, DevErr* err, cudaStream_t s) {
-    auto kern = input_transform_kernel<TF, OutT, SCALED, XB>;
+    auto kern = input_transform_kernel<TF, OutT, SCALED, XB, KEEP>;
     // a third staging buffer where two CTAs of three still fit an SM: the
     // next item's copies then start two items ahead of the arithmetic
     const int buf = (smem - kInHeader - 2 * kInSlack) / 2;
@@ -798,6 +817,12 @@ cudaError_t launch_input_transform(Xform xf, OpType op, const Geom& g, const voi
                                    const float* scale, DevErr* err, cudaStream_t stream, bool x_bf16) {
     int smem = 0;
     const InDesc d = make_in_desc(g, x, x_end, V, scale, &smem);
+    // V of this launch within the L2 size: written with the evict_last
+    // priority, the GEMM that follows reads most of it from L2 (cfg2 F(4x3),
+    // 116 MB of V: 146 -> 140 us per call, same box); a larger V (F(2x3) on
+    // cfg2: 205 MB) would only push itself out.  fp16 unscaled paths only.
+    const long long v_bytes = static_cast<long long>(g.alpha) * g.alpha * d.CG * 8 * d.Pp * 2;
+    const bool keep = v_bytes <= l2_bytes();
     const bool bf = op == OpType::BF16, sc = scale != nullptr;
     if (x_bf16) {
         // bf16 tensors: F(2x3) with bf16 operands, F(4x3) with fp16 operands
@@ -809,14 +834,16 @@ cudaError_t launch_input_transform(Xform xf, OpType op, const Geom& g, const voi
     }
     switch (xf) {
         case Xform::F2:  // never scaled
-            return bf ? input_launch<F2, __nv_bfloat16, false>(d, smem, err, stream)
-                      : input_launch<F2, __half, false>(d, smem, err, stream);
+            if (bf) return input_launch<F2, __nv_bfloat16, false>(d, smem, err, stream);
+            return keep ? input_launch<F2, __half, false, false, true>(d, smem, err, stream)
+                        : input_launch<F2, __half, false>(d, smem, err, stream);
         case Xform::F4:
             if (sc)
                 return bf ? input_launch<F4, __nv_bfloat16, true>(d, smem, err, stream)
                           : input_launch<F4, __half, true>(d, smem, err, stream);
-            return bf ? input_launch<F4, __nv_bfloat16, false>(d, smem, err, stream)
-                      : input_launch<F4, __half, false>(d, smem, err, stream);
+            if (bf) return input_launch<F4, __nv_bfloat16, false>(d, smem, err, stream);
+            return keep ? input_launch<F4, __half, false, false, true>(d, smem, err, stream)
+                        : input_launch<F4, __half, false>(d, smem, err, stream);
         case Xform::F4Ref:
             if (sc)
                 return bf ? input_launch<F4Ref, __nv_bfloat16, true>(d, smem, err, stream)
