@@ -249,7 +249,9 @@ __device__ __forceinline__ void gemm_body(const GemmDesc* __restrict__ descs, in
         // epilogue warps 2..9: TMEM lane quarter = warp % 4; warps 2-5 store
         // the first half of the accumulator columns, 6-9 the second (BN >= 64)
         const int quarter = warp & 3;
-        const uint64_t m_pol = l2_evict_first();   // M is larger than L2: do not let it push V out
+        // M that fits in L2 stays for the output transform; larger M must not
+        // push V out
+        const uint64_t m_pol = descs[0].keep_m ? l2_evict_last() : l2_evict_first();
         const int half = (warp - 2) >> 2;
         const int row = quarter * 32 + lane;
         int acc = 0;
@@ -419,6 +421,7 @@ cudaError_t make_gemm_desc(GemmDesc& d, OpType op, int E, long long P, int K, in
     d.kg_count = m_fp32 ? Kp / 4 : Kp / 8;
     d.m_row = m_row ? 1 : 0;
     d.kp = Kp;
+    d.keep_m = 0;   // plan_gemm decides for single launches; grouped ones stream M
     d.m_blocks = static_cast<int>((P + kBM - 1) / kBM);
     d.n_blocks = (K + bn - 1) / bn;
     d.k_blocks = (Cp + kBK - 1) / kBK;
@@ -456,6 +459,9 @@ cudaError_t plan_gemm(GemmPlan& gp, OpType op, int E, long long P, int K, int Kp
                       const void* U, void* Mw, bool m_fp32, int bn, int num_sms, bool m_row) {
     cudaError_t e = make_gemm_desc(gp.desc, op, E, P, K, Kp, Cp, V, U, Mw, m_fp32, bn, m_row);
     if (e != cudaSuccess) return e;
+    // M of this launch within the L2 size: kept there for the output transform
+    // that reads it next (cfg3 F(4x3): 116 MB); larger M is streamed out
+    gp.desc.keep_m = static_cast<long long>(E) * P * Kp * (m_fp32 ? 4 : 2) <= l2_cache_bytes();
     gp.op = op;
     gp.bn = bn;
     gp.m_fp32 = m_fp32;

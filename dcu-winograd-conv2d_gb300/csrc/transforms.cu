@@ -611,18 +611,6 @@ struct InBlocking {
     int tb, nbh, cb, stride, buf;
 };
 
-long long l2_bytes() {
-    static long long cached[64] = {};
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 0;
-    if (!cached[dev]) {
-        int v = 0;
-        cudaDeviceGetAttribute(&v, cudaDevAttrL2CacheSize, dev);
-        cached[dev] = v > 0 ? v : 1;
-    }
-    return cached[dev];
-}
-
 int sm_count() {
     static int cached[64] = {0};
     int dev = 0;
@@ -745,6 +733,18 @@ cudaError_t filter_launch(const void* w, void* U, int K, int C, int Cp, cudaStre
 
 }  // namespace
 
+long long l2_cache_bytes() {
+    static long long cached[64] = {};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 0;
+    if (!cached[dev]) {
+        int v = 0;
+        cudaDeviceGetAttribute(&v, cudaDevAttrL2CacheSize, dev);
+        cached[dev] = v > 0 ? v : 1;
+    }
+    return cached[dev];
+}
+
 cudaError_t launch_filter_transform(Xform xf, OpType op, const void* weight, void* U, int K, int C, int Cp,
                                     cudaStream_t stream, bool w_bf16) {
     const bool bf = op == OpType::BF16;
@@ -822,7 +822,7 @@ cudaError_t launch_input_transform(Xform xf, OpType op, const Geom& g, const voi
     // 116 MB of V: 146 -> 140 us per call, same box); a larger V (F(2x3) on
     // cfg2: 205 MB) would only push itself out.  fp16 unscaled paths only.
     const long long v_bytes = static_cast<long long>(g.alpha) * g.alpha * d.CG * 8 * d.Pp * 2;
-    const bool keep = v_bytes <= l2_bytes();
+    const bool keep = v_bytes <= l2_cache_bytes();
     const bool bf = op == OpType::BF16, sc = scale != nullptr;
     if (x_bf16) {
         // bf16 tensors: F(2x3) with bf16 operands, F(4x3) with fp16 operands

@@ -112,6 +112,7 @@ struct alignas(64) GemmDesc {
     int P, kg_count, m_blocks, n_blocks, k_blocks, E;
     int m_row;           // 1: M[e][P][Kp] (rows of output channels, NHWC output path)
     int kp;
+    int keep_m;          // M fits in L2: store it with the evict_last priority
     long long tile_begin;
     long long tiles;     // E * m_blocks * n_blocks
 };
@@ -216,6 +217,9 @@ cudaError_t launch_row4x3(const RowPlan& rp, const void* x, const void* x_end, v
 // interleaved kernel: images [n_base, n_base + n_images) of the bound input into
 // out (which holds those images)
 cudaError_t launch_row4x3i(const RowPlan& rp, void* out, int n_base, int n_images, DevErr* err, cudaStream_t stream);
+
+// L2 size of the current device in bytes.
+long long l2_cache_bytes();
 
 // Tensor-map encoder from the driver (resolved once through the runtime).
 CUresult encode_tiled(CUtensorMap* map, CUtensorMapDataType dt, cuuint32_t rank, void* addr, const cuuint64_t* dims,
