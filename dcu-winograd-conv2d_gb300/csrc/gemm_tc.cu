@@ -27,6 +27,7 @@
 #include <cudaTypedefs.h>
 
 #include <algorithm>
+#include <cstdlib>
 
 #include "wg_kernels.h"
 #include "wg_launch.h"
@@ -306,6 +307,19 @@ __device__ __forceinline__ void gemm_body(const GemmDesc* __restrict__ descs, in
             }
             tc_fence_before();
             mbar_arrive(&tempty[acc]);
+            if (d.discard_v) {
+                // this tile consumed every granule of its 128 rows of V, and
+                // no other tile reads them: drop the lines without write-back
+                const int et = (warp - 2) * 32 + lane, n_et = 128 * kEpiHalves;
+                const int rows = min(kBM, d.v_pp - it.mb * kBM);   // a multiple of 8: whole lines
+                const int lpg = rows / 8;
+                const unsigned char* vb = static_cast<const unsigned char*>(d.V) +
+                                          ((static_cast<long long>(it.e) * d.v_cg) * d.v_pp + static_cast<long long>(it.mb) * kBM) * 16;
+                for (int i = et; i < d.v_cg * lpg; i += n_et) {
+                    const int g = i / lpg, l = i - g * lpg;
+                    discard_l2_line(vb + static_cast<long long>(g) * d.v_pp * 16 + l * 128);
+                }
+            }
             if (++acc == 2) {
                 acc = 0;
                 acc_phase ^= 1u;
@@ -422,6 +436,10 @@ cudaError_t make_gemm_desc(GemmDesc& d, OpType op, int E, long long P, int K, in
     d.m_row = m_row ? 1 : 0;
     d.kp = Kp;
     d.keep_m = 0;   // plan_gemm decides for single launches; grouped ones stream M
+    d.V = V;
+    d.v_cg = Cp / 8;
+    d.v_pp = static_cast<int>(round_rows(P));
+    d.discard_v = 0;
     d.m_blocks = static_cast<int>((P + kBM - 1) / kBM);
     d.n_blocks = (K + bn - 1) / bn;
     d.k_blocks = (Cp + kBK - 1) / kBK;
@@ -462,6 +480,10 @@ cudaError_t plan_gemm(GemmPlan& gp, OpType op, int E, long long P, int K, int Kp
     // M of this launch within the L2 size: kept there for the output transform
     // that reads it next (cfg3 F(4x3): 116 MB); larger M is streamed out
     gp.desc.keep_m = static_cast<long long>(E) * P * Kp * (m_fp32 ? 4 : 2) <= l2_cache_bytes();
+    // V has one reader per tile when one block covers all output channels;
+    // WG_CONV2D_KEEP_WORKSPACE=1 keeps it (to read the workspace back)
+    const char* keep_ws = std::getenv("WG_CONV2D_KEEP_WORKSPACE");
+    gp.desc.discard_v = gp.desc.n_blocks == 1 && !(keep_ws && std::atoi(keep_ws) != 0);
     gp.op = op;
     gp.bn = bn;
     gp.m_fp32 = m_fp32;

@@ -113,6 +113,11 @@ struct alignas(64) GemmDesc {
     int m_row;           // 1: M[e][P][Kp] (rows of output channels, NHWC output path)
     int kp;
     int keep_m;          // M fits in L2: store it with the evict_last priority
+    // V[E][v_cg][v_pp][8] is read by this GEMM only (one block of output
+    // channels): its lines are discarded from L2 once a tile is done, so the
+    // dirty lines are never written back to HBM
+    const void* V;
+    int v_cg, v_pp, discard_v;
     long long tile_begin;
     long long tiles;     // E * m_blocks * n_blocks
 };

@@ -160,6 +160,12 @@ __device__ __forceinline__ uint64_t l2_evict_unchanged() {
     asm volatile("createpolicy.fractional.L2::evict_unchanged.b64 %0, 1.0;" : "=l"(p));
     return p;
 }
+// Drops one 128-byte line of global memory from L2 without writing it back:
+// its contents become undefined.  For scratch data nothing reads again.
+__device__ __forceinline__ void discard_l2_line(const void* ptr) {
+    asm volatile("discard.global.L2 [%0], 128;" ::"l"(ptr) : "memory");
+}
+
 __device__ __forceinline__ void st_hint_b32(void* ptr, uint32_t v, uint64_t pol) {
     asm volatile("st.global.L2::cache_hint.b32 [%0], %1, %2;" ::"l"(ptr), "r"(v), "l"(pol));
 }

@@ -106,8 +106,11 @@ def _dev_array(wg, ptr, count, dtype):
 
 
 @pytest.mark.parametrize("algo,variant", [(1, "F2"), (0, "F4"), (0, "F4Ref")])
-def test_transform_kernels_elementwise(wg, algo, variant):
-    """U, V and M read back from the workspace, each against its restatement."""
+def test_transform_kernels_elementwise(wg, monkeypatch, algo, variant):
+    """U, V and M read back from the workspace, each against its restatement
+    (the GEMM otherwise drops V from L2 once it is read, leaving its memory
+    undefined)."""
+    monkeypatch.setenv("WG_CONV2D_KEEP_WORKSPACE", "1")
     n, c, h, w, k = 2, 20, 11, 13, 24
     x, wt = O.uniform_inputs(31, n, c, h, w, k)
     opts = opts_for(wg, algo, f4_points=1 if variant == "F4Ref" else 0)
