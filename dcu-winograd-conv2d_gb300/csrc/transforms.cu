@@ -26,6 +26,7 @@
 #include <cuda_fp16.h>
 
 #include <algorithm>
+#include <cstdlib>
 
 #include "wg_kernels.h"
 #include "wg_launch.h"
@@ -583,6 +584,20 @@ __device__ __forceinline__ void output_staged_body(const OutDesc* descs, int nde
                         if (i < vr) store_row<M>(o + static_cast<long long>(i) * OW, &y[i * M], vc, inv);
                 }
             }
+            if (d.discard_m) {
+                // the item's M runs are in shared memory and nothing reads
+                // them again: drop the 128-byte lines that lie wholly inside
+                // them (a line shared with the next granule's rows stays)
+                const long long p0 = (item / KG) * kOsTiles;
+                const long long nbytes = min(static_cast<long long>(kOsTiles), P - p0) * 16;
+                const unsigned char* Mb = static_cast<const unsigned char*>(d.Mw);
+                for (int i = threadIdx.x; i < E * 8; i += 128) {
+                    const int e = i >> 3, l = i & 7;
+                    const long long s0 = ((static_cast<long long>(e) * KG + g) * P + p0) * 16;
+                    const long long first = (s0 + 127) & ~127LL, end = (s0 + nbytes) & ~127LL;
+                    if (first + (l + 1) * 128LL <= end) discard_l2_line(Mb + first + l * 128LL);
+                }
+            }
             __syncwarp();
             if (lane == 0) mbar_arrive(&empty[b]);
         }
@@ -810,6 +825,14 @@ OutDesc make_out_desc(const Geom& g, bool m_fp32, const void* Mw, void* out, con
     d.gx = (g.P + kOsTiles - 1) / kOsTiles;
     d.gy = d.KG;
     d.blk_begin = 0;
+    // M larger than L2 streams through it: its lines are dropped as soon as
+    // they are read (cfg2 F(4x3), 231 MB: output transform 48.4 -> 42.1 us on
+    // one box); M that fits stays in L2 for this kernel, where discarding only
+    // costs time (cfg3, 116 MB: 22.5 -> 23.8 us).  WG_CONV2D_KEEP_WORKSPACE=1
+    // keeps M readable after the call.
+    const char* keep_ws = std::getenv("WG_CONV2D_KEEP_WORKSPACE");
+    const long long m_bytes = static_cast<long long>(g.alpha) * g.alpha * d.KG * g.P * 16;
+    d.discard_m = !(keep_ws && std::atoi(keep_ws) != 0) && m_bytes > l2_cache_bytes();
     return d;
 }
 

@@ -82,6 +82,7 @@ struct OutDesc {
     long long gx;         // work items along blocks of 64 tiles
     int gy;               // work items along granules
     long long blk_begin;
+    int discard_m;        // M is read once here: drop its L2 lines without write-back
 };
 
 // Descriptor of one problem's input transform and the dynamic shared memory
