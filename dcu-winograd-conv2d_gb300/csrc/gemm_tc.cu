@@ -93,10 +93,10 @@ __device__ __forceinline__ void store32<float>(float* Mw, const uint32_t (&r)[32
 // row p (one 16-byte store for fp32, 8 bytes for fp16); Kp is a multiple of 8.
 template <class MT>
 __device__ __forceinline__ void store4_row(MT* Mw, const uint32_t (&v)[4], long long P, long long p, int k0, int kp,
-                                           int e) {
+                                           int e, uint64_t pol) {
     MT* dst = Mw + (static_cast<long long>(e) * P + p) * kp + k0;
     if constexpr (sizeof(MT) == 4) {
-        *reinterpret_cast<uint4*>(dst) = make_uint4(v[0], v[1], v[2], v[3]);
+        st_hint_v4(dst, make_uint4(v[0], v[1], v[2], v[3]), pol);
     } else {
         __half2 a = __floats2half2_rn(__uint_as_float(v[0]), __uint_as_float(v[1]));
         __half2 b = __floats2half2_rn(__uint_as_float(v[2]), __uint_as_float(v[3]));
@@ -297,7 +297,7 @@ __device__ __forceinline__ void gemm_body(const GemmDesc* __restrict__ descs, in
 #pragma unroll
                         for (int j = 0; j < 4; ++j) v[j] = xp[row_w * 32 + ((c0 + j) ^ row_w)];
                         const long long pr = static_cast<long long>(it.mb) * kBM + quarter * 32 + row_w;
-                        if (pr < P && k0 < kp) store4_row<MT>(Mw, v, P, pr, k0, kp, it.e);
+                        if (pr < P && k0 < kp) store4_row<MT>(Mw, v, P, pr, k0, kp, it.e, m_pol);
                     }
                     __syncwarp();
                 } else if (p < P) {

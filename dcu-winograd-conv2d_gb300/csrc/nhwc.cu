@@ -18,6 +18,7 @@
 #include <cuda_fp16.h>
 
 #include <algorithm>
+#include <cstdlib>
 
 #include "wg_kernels.h"
 #include "wg_launch.h"
@@ -79,7 +80,7 @@ template <> __device__ __forceinline__ uint32_t npack<__nv_bfloat16>(float2 v) {
     return *reinterpret_cast<uint32_t*>(&h);
 }
 
-template <class TF, class OutT>
+template <class TF, class OutT, bool KEEP>
 __device__ __forceinline__ void nh_compute(const NhwcInDesc& d, long long local, int n_base, const unsigned char* buf,
                                            int cw) {
     constexpr int M = TF::M, A = TF::ALPHA;
@@ -123,16 +124,21 @@ __device__ __forceinline__ void nh_compute(const NhwcInDesc& d, long long local,
 #pragma unroll
             for (int i = 0; i < A; ++i) pk[i * A + j] = npack<OutT>(v[i]);
         }
+        // V kept in L2 for the GEMM where it fits (KEEP), plain stores otherwise
         OutT* dst = V + ((static_cast<long long>(c0 / 8 + g)) * Pp + p0 + t) * 8 + sub * 2;
+        const uint64_t keep = KEEP ? l2_evict_last() : 0;
 #pragma unroll
         for (int e = 0; e < A * A; ++e) {
-            *reinterpret_cast<uint32_t*>(dst) = pk[e];
+            if constexpr (KEEP)
+                st_hint_b32(dst, pk[e], keep);
+            else
+                *reinterpret_cast<uint32_t*>(dst) = pk[e];
             dst += estride;
         }
     }
 }
 
-template <class TF, class OutT>
+template <class TF, class OutT, bool KEEP>
 __global__ void __launch_bounds__(kNhThreads, 2)
     nhwc_input_transform(const __grid_constant__ NhwcInDesc d, int n_base, long long total, int buf_bytes,
                          DevErr* err) {
@@ -173,7 +179,7 @@ __global__ void __launch_bounds__(kNhThreads, 2)
         for (long long item = blockIdx.x; item < total; item += gridDim.x, ++k) {
             const int b = k & 1;
             if (!mbar_wait(&full[b], (k >> 1) & 1, abort_flag, err, ERR_SITE_FULL)) break;
-            nh_compute<TF, OutT>(d, item, n_base, bufs + b * buf_bytes, warp);
+            nh_compute<TF, OutT, KEEP>(d, item, n_base, bufs + b * buf_bytes, warp);
             __syncwarp();
             if ((threadIdx.x & 31) == 0) mbar_arrive(&empty[b]);
         }
@@ -197,12 +203,34 @@ template <> struct MP<__half> {
 };
 
 template <class TF, class MT>
+__device__ __forceinline__ void nh_out_tile(const NhwcOutDesc& d, long long p);
+
+template <class TF, class MT>
 __global__ void __launch_bounds__(256) nhwc_output_transform(const __grid_constant__ NhwcOutDesc d) {
-    constexpr int M = TF::M, A = TF::ALPHA, E = A * A;
+    constexpr int A = TF::ALPHA, E = A * A;
     pdl_wait();     // M written, earlier readers of the output done
     pdl_trigger();
     const long long p = static_cast<long long>(blockIdx.x) * d.tpc + threadIdx.x / d.tpt;
-    if (p >= d.P || threadIdx.x >= d.tpt * d.tpc) return;
+    if (p < d.P && threadIdx.x < d.tpt * d.tpc) nh_out_tile<TF, MT>(d, p);
+    if (d.discard_m) {
+        // every M row of the CTA's tiles has been read (rows are whole 128-byte
+        // lines, each read by this CTA only): drop them without write-back
+        __syncthreads();
+        const long long p_first = static_cast<long long>(blockIdx.x) * d.tpc;
+        const int tiles = static_cast<int>(min(static_cast<long long>(d.tpc), d.P - p_first));
+        const int lpr = d.Kp * static_cast<int>(sizeof(MT)) / 128;   // lines per row
+        const unsigned char* Mb = static_cast<const unsigned char*>(d.Mw);
+        for (int i = threadIdx.x; i < E * tiles * lpr; i += blockDim.x) {
+            const int l = i % lpr, rest = i / lpr;
+            const int tt = rest % tiles, e = rest / tiles;
+            discard_l2_line(Mb + ((static_cast<long long>(e) * d.P + p_first + tt) * d.Kp) * sizeof(MT) + l * 128);
+        }
+    }
+}
+
+template <class TF, class MT>
+__device__ __forceinline__ void nh_out_tile(const NhwcOutDesc& d, long long p) {
+    constexpr int M = TF::M, A = TF::ALPHA, E = A * A;
     const int tw = static_cast<int>(p % d.tiles_w);
     const long long r = p / d.tiles_w;
     const int th = static_cast<int>(r % d.tiles_h);
@@ -303,13 +331,19 @@ cudaError_t launch_nhwc_input_transform(Xform xf, OpType op, const NhwcInDesc& d
         if (e != cudaSuccess) return e;
         return launch_pdl(kern, dim3(grid), dim3(kNhThreads), smem, s, d, n_base, total, buf, err);
     };
+    // V of this launch within the L2 size: kept there for the GEMM (fp16)
+    const int A = xf == Xform::F2 ? 4 : 6;
+    const bool keep = !bf && static_cast<long long>(A) * A * d.CG * 8 * d.Pp * 2 <= l2_cache_bytes();
     switch (xf) {
         case Xform::F2:
-            return bf ? go(nhwc_input_transform<F2, __nv_bfloat16>) : go(nhwc_input_transform<F2, __half>);
+            if (bf) return go(nhwc_input_transform<F2, __nv_bfloat16, false>);
+            return keep ? go(nhwc_input_transform<F2, __half, true>) : go(nhwc_input_transform<F2, __half, false>);
         case Xform::F4:
-            return bf ? go(nhwc_input_transform<F4, __nv_bfloat16>) : go(nhwc_input_transform<F4, __half>);
+            if (bf) return go(nhwc_input_transform<F4, __nv_bfloat16, false>);
+            return keep ? go(nhwc_input_transform<F4, __half, true>) : go(nhwc_input_transform<F4, __half, false>);
         case Xform::F4Ref:
-            return bf ? go(nhwc_input_transform<F4Ref, __nv_bfloat16>) : go(nhwc_input_transform<F4Ref, __half>);
+            return bf ? go(nhwc_input_transform<F4Ref, __nv_bfloat16, false>)
+                      : go(nhwc_input_transform<F4Ref, __half, false>);
     }
     return cudaErrorInvalidValue;
 }
@@ -325,11 +359,18 @@ NhwcOutDesc make_nhwc_out_desc(const Geom& g, const void* Mw, void* out) {
     return d;
 }
 
-cudaError_t launch_nhwc_output_transform(Xform xf, bool m_fp32, const NhwcOutDesc& d, cudaStream_t s) {
-    const long long blocks = (d.P + d.tpc - 1) / d.tpc;
+cudaError_t launch_nhwc_output_transform(Xform xf, bool m_fp32, const NhwcOutDesc& dd, cudaStream_t s) {
+    const long long blocks = (dd.P + dd.tpc - 1) / dd.tpc;
     if (blocks <= 0) return cudaSuccess;
     if (blocks > 0x7fffffffLL) return cudaErrorInvalidValue;
     const dim3 grid(static_cast<unsigned>(blocks));
+    // M larger than L2 is dropped from it as soon as it is read, where its rows
+    // are whole 128-byte lines; WG_CONV2D_KEEP_WORKSPACE=1 keeps it
+    NhwcOutDesc d = dd;
+    const int esize = m_fp32 ? 4 : 2, A = xf == Xform::F2 ? 4 : 6;
+    const char* keep_ws = std::getenv("WG_CONV2D_KEEP_WORKSPACE");
+    d.discard_m = !(keep_ws && std::atoi(keep_ws) != 0) && (d.Kp * esize) % 128 == 0 &&
+                  static_cast<long long>(A) * A * d.P * d.Kp * esize > l2_cache_bytes();
     switch (xf) {
         case Xform::F2:
             return m_fp32 ? launch_pdl(nhwc_output_transform<F2, float>, grid, dim3(256), 0, s, d)

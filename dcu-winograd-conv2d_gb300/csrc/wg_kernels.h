@@ -170,6 +170,7 @@ struct NhwcOutDesc {
     int K, Kp, OH, OW, tiles_h, tiles_w;
     long long P;
     int tpt, tpc;         // threads per tile, tiles per CTA
+    int discard_m;        // drop M's lines from L2 once read (set by the launcher)
 };
 NhwcOutDesc make_nhwc_out_desc(const Geom& g, const void* Mw, void* out);
 cudaError_t launch_nhwc_output_transform(Xform xf, bool m_fp32, const NhwcOutDesc& d, cudaStream_t stream);
