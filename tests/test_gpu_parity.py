@@ -282,7 +282,7 @@ def test_autotune_choice_is_cached_and_correct(wg):
     wg.lib().conv2d_autotune_clear()
     a1 = wg.autotune(prob)
     a2 = wg.autotune(prob)
-    assert a1 == a2 and a1[0] in (0, 1, 2)
+    assert a1 == a2 and a1[0] in (0, 1, 2, 4)
     op = wg.Conv2d(prob, opts_for(wg, wg.ALGO_AUTO))
     assert op.algo == a1[0]
     op(torch.cuda.current_stream().cuda_stream)
