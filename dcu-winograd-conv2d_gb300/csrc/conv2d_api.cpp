@@ -391,12 +391,40 @@ int Plan::run(cudaStream_t s) {
 // whether copy engines or SM loads and stores move the bytes).  Chunks hold at
 // least 6 MB of copies and there are at most 8 of them: on the 32 x 256 x 56^2
 // layer (103 MB of copies) 8 chunks took 402-411 us per call, 6 took 420,
-// 4 took 439, 12 and 16 took 450.  WG_CONV2D_HOST_CHUNKS sets another maximum
-// (1-16).  Each chunk's copies and kernels are queued together, the input
-// copies three chunks ahead.
+// 4 took 439, 12 and 16 took 450; chunks ramping from 1 image up to 4 and
+// back measured 418-428 us against 415 for 8 x 4.  WG_CONV2D_HOST_CHUNKS sets
+// another maximum (1-16), WG_CONV2D_HOST_SIZES every chunk's image count.
+// Each chunk's copies and kernels are queued together, the input copies
+// three chunks ahead.
 namespace {
 
+// WG_CONV2D_HOST_SIZES="a,b,..." (positive image counts summing to n, at most
+// kMaxHostChunks of them, at most kMaxHostPlans distinct ones) -> their count,
+// else 0.
+int host_sizes_env(int n, int* sizes) {
+    const char* p = std::getenv("WG_CONV2D_HOST_SIZES");
+    if (!p || !*p) return 0;
+    int cnt = 0;
+    long long sum = 0;
+    while (*p) {
+        char* q = nullptr;
+        const long v = std::strtol(p, &q, 10);
+        if (q == p || v <= 0 || v > n || cnt == Plan::kMaxHostChunks || (*q && *q != ',')) return 0;
+        sizes[cnt++] = static_cast<int>(v);
+        sum += v;
+        p = *q ? q + 1 : q;
+    }
+    int distinct = 0;
+    for (int i = 0; i < cnt; ++i) {
+        bool seen = false;
+        for (int j = 0; j < i; ++j) seen = seen || sizes[j] == sizes[i];
+        distinct += seen ? 0 : 1;
+    }
+    return (sum == n && distinct <= Plan::kMaxHostPlans) ? cnt : 0;
+}
+
 int host_schedule(int n, long long img_copy_bytes, int* sizes) {
+    if (const int cnt = host_sizes_env(n, sizes)) return cnt;
     const long long total = static_cast<long long>(n) * img_copy_bytes;
     long long max_chunks = 8;
     if (const char* e = std::getenv("WG_CONV2D_HOST_CHUNKS")) max_chunks = std::max(1, std::min(std::atoi(e), Plan::kMaxHostChunks));

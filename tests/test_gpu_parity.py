@@ -436,6 +436,30 @@ def test_host_chunks_over_a_smaller_image_chunk_workspace(wg, algo):
     assert np.array_equal(hout.numpy().view(np.uint16), dev.view(np.uint16))
 
 
+@pytest.mark.parametrize("algo", [0, 2])
+def test_host_chunk_sizes_from_the_environment(wg, monkeypatch, algo):
+    """WG_CONV2D_HOST_SIZES lists the image count of every host chunk; valid
+    lists (ragged, one chunk, one image per chunk, a trailing comma) and
+    invalid ones (wrong sum, a zero, junk: these fall back to the default
+    schedule) all equal the device-buffer call bit for bit."""
+    n, c, h, k = 11, 64, 100, 64
+    x, wt = O.uniform_inputs(21 + algo, n, c, h, h, k)
+    xt = torch.empty((n, c, h, h), dtype=torch.float16, device="cuda")
+    wtt = torch.from_numpy(wt).cuda()
+    y = torch.empty((n, k, h, h), dtype=torch.float16, device="cuda")
+    prob = wg.make_problem(xt.data_ptr(), wtt.data_ptr(), y.data_ptr(), n, c, h, h, k)
+    op = wg.Conv2d(prob, opts_for(wg, algo))
+    dev, _ = run(wg, x, wt, 1, 1, opts_for(wg, algo))
+    s = torch.cuda.current_stream().cuda_stream
+    hin = torch.from_numpy(x).pin_memory()
+    for sizes in ["1,3,5,2", "11", ",".join(["1"] * 11), "1,2,3", "4,0,7", "4,x,7", "5,6,", "1,2,3,4,1"]:
+        monkeypatch.setenv("WG_CONV2D_HOST_SIZES", sizes)
+        hout = torch.zeros((n, k, h, h), dtype=torch.float16).pin_memory()
+        op.host(hin.data_ptr(), hout.data_ptr(), s)
+        assert np.array_equal(hout.numpy().view(np.uint16), dev.view(np.uint16)), sizes
+    assert op.check_device()[0] == wg.OK
+
+
 @pytest.mark.parametrize("algo", [0, 4])
 def test_host_pipeline_graph_replay(wg, monkeypatch, algo):
     """WG_CONV2D_HOST_GRAPH=1: the first host call captures the pipeline into
