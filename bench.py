@@ -185,6 +185,8 @@ def load_phase(step, device, seconds=0.6):
     """Untimed steps of the benchmark's own work for `seconds`, so that the
     clock samples (200 ms apart) see the GPU under the load the timed steps
     then put on it; the timed steps follow at once."""
+    import torch
+
     t0 = time.perf_counter()
     i = 0
     while time.perf_counter() - t0 < seconds:
