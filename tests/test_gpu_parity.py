@@ -177,6 +177,33 @@ def test_reference_harness_replay_cfg1(wg):
     assert O.rel_errors(y, ref)[0] <= TOL[4]
 
 
+# The reference benchmark's contest shapes (N, C, H = W, K), its pre.sh and
+# final.sh runs; 3x3, stride 1, pad 1.
+CONTEST_SHAPES = [
+    (64, 256, 14, 256), (256, 192, 14, 192), (16, 256, 26, 512), (32, 256, 14, 256),
+    (2, 1280, 16, 1280), (2, 960, 64, 32), (16, 128, 64, 27), (16, 256, 32, 256),
+    (16, 64, 128, 64), (2, 1920, 32, 640), (2, 640, 64, 640), (2, 320, 64, 4),
+]
+
+
+@pytest.mark.parametrize("n,c,hw,k", CONTEST_SHAPES)
+def test_contest_shapes_as_the_reference_checks_them(wg, n, c, hw, k):
+    """Each contest shape through the drop-in API with the reference's
+    selection and its input fill (glibc rand, src/main.cpp:36-44), checked
+    with the reference benchmark's criterion and against FP64 on image 0 and
+    up to 8 output channels spread over K (the share of the output the CPU
+    oracle computes in about a second)."""
+    x, wt = O.reference_style_inputs(n, c, hw, hw, k)
+    y, op = run(wg, x, wt, 1, 1, None)
+    assert op.algo == O.select_reference(n, c, hw, hw, k)
+    ks = np.unique(np.linspace(0, k - 1, min(k, 8)).round().astype(int))
+    ref16, r64 = O.conv2d_direct(x[:1], wt[ks], nthreads=8)
+    got = y[:1, ks]
+    assert O.reference_criterion_failures(got, ref16) == 0
+    mx, mean, _ = O.rel_errors(got, r64)
+    assert mx <= tol_for(algo_m(op.algo), c), (n, c, hw, k, op.algo, mx, mean)
+
+
 def test_legacy_void_entry_point(wg):
     import ctypes
     x, wt = O.uniform_inputs(8, 1, 16, 12, 12, 16)
