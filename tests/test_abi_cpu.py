@@ -53,12 +53,14 @@ def test_param_size(wg):
 
 @pytest.mark.parametrize("field,value,status", [
     ("r", 5, 2), ("s", 1, 2), ("u", 2, 2), ("v", 2, 2), ("n", 0, 1), ("k", 0, 1), ("h", 1, 1),
+    ("c", 0, 1), ("h", 0, 1), ("w", 0, 1), ("w", 1, 1), ("p", 65, 2), ("q", 65, 2),
+    ("c", 65536, 2), ("k", 65536, 2), ("h", 65536, 2), ("w", 65536, 2), ("n", 1 << 28, 2),
 ])
 def test_unsupported_descriptors_rejected(wg, field, value, status):
     prob = wg.make_problem(16, 16, 16, 2, 8, 8, 8, 8)
     setattr(prob, field, value)
-    if field == "h":
-        prob.p = 0  # 1x? image without padding has no 3x3 output
+    if (field, value) in (("h", 1), ("w", 1)):
+        prob.p = prob.q = 0  # a 1-pixel image without padding has no 3x3 output
     with pytest.raises(wg.Conv2dError) as ei:
         wg.Conv2d(prob)
     assert ei.value.status == status
