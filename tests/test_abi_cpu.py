@@ -24,6 +24,21 @@ def declared_functions():
     return sorted(set(names))
 
 
+def test_missing_library_fails_loudly(tmp_path):
+    """Without the built library the operator refuses to run: there is no
+    fallback path to compute on."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location(
+        "wgconv_unbuilt", os.path.join(ROOT, "dcu-winograd-conv2d_gb300", "__init__.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    mod.LIB_PATH = str(tmp_path / "libwgconv.so")
+    with pytest.raises(RuntimeError, match="not built"):
+        mod.lib()
+    with pytest.raises(RuntimeError, match="not built"):
+        mod.Conv2d(mod.make_problem(16, 16, 16, 1, 8, 8, 8, 8))
+
+
 def test_header_declares_what_the_binding_expects(wg):
     assert set(declared_functions()) == set(wg.EXPORTS)
 
