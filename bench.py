@@ -356,6 +356,51 @@ def roofline_for(name, wg, geo, ms, pk, pk_kind):
     return out
 
 
+def f2x3_paths(wg, torch, xs, ys, wt, geo, sptr, device, reps, pk, pk_kind):
+    """The F(2x3) paths (non-fused and fused) on the same buffer sets as the
+    headline run: effective TFLOP/s per call (back-to-back calls) and, per
+    kernel, its roofline: HBM GB/s for the transforms, tensor-pipe share for
+    the 16 batched C x K GEMMs.  A failure is reported, not raised."""
+    n, c, h, w, k = geo
+    flops = direct_flops(n, c, h, w, k)
+    out = {}
+    for label, algo in (("non_fused", wg.ALGO_2X3), ("fused", wg.ALGO_2X3_FUSED)):
+        ops = []
+        try:
+            for x, y in zip(xs, ys):
+                prob = wg.make_problem(x.data_ptr(), wt.data_ptr(), y.data_ptr(), n, c, h, w, k)
+                ops.append(wg.Conv2d(prob, wg.default_options(algo=algo)))
+            for i in range(3):
+                ops[i % len(ops)](sptr)
+            torch.cuda.synchronize(device)
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            stream = torch.cuda.current_stream(device)
+            a.record(stream)
+            for i in range(reps):
+                ops[i % len(ops)](sptr)
+            b.record(stream)
+            torch.cuda.synchronize(device)
+            ms = a.elapsed_time(b) / reps
+            kt = {}
+            for i in range(reps):
+                for nm, t in zip(ops[0].kernel_names(), ops[i % len(ops)].timed(sptr)):
+                    kt.setdefault(nm, []).append(t)
+            kernels = {}
+            for nm, v in kt.items():
+                r = roofline_for(nm, wg, (n, c, h, w, k, 2), sum(v) / len(v), pk, pk_kind)
+                kernels[nm] = {key: r[key] for key in ("launch_us", "bound", "achieved", "unit", "frac",
+                                                      "algorithmic_per_launch", "tensor_frac") if key in r}
+            ok = all(op.check_device()[0] == wg.OK for op in ops)
+            out[label] = {"value": flops / (ms * 1e-3) / 1e12, "unit": "TFLOP/s", "ms_per_call": ms,
+                          "calls": reps, "kernels": kernels, "device_ok": ok}
+        except Exception as e:  # reported beside the headline, which stands on its own
+            out[label] = {"error": f"{type(e).__name__}: {e}"[:300]}
+        finally:
+            for op in ops:
+                op.destroy()
+    return out
+
+
 def committed_traffic(kernel, workload):
     """DRAM bytes per launch recorded from an ncu capture in profiles/ (a line
     `traffic <kernel> <workload> <bytes>` in profiles/traffic.txt), else None."""
@@ -463,6 +508,12 @@ def our_arm(args):
     roof["share_of_step"] = tot[dominant] / max(1e-9, sum(tot.values()))
     kernel_ms = {nm: sum(v) / len(v) * (len(v) / reps) for nm, v in kt.items()}
 
+    # the workload names F(2x3), fused and non-fused: both measured beside the
+    # autotuned headline, on the same buffers
+    f2x3 = None
+    if args.workload == "cfg2" and not args.nhwc and world == 1:
+        f2x3 = f2x3_paths(wg, torch, xs, ys, wt, (n, c, h, w, k), sptr, device, reps, pk, pk_kind)
+
     # end to end through the host-buffer entry point
     e2e = None
     if not args.no_e2e:
@@ -525,6 +576,7 @@ def our_arm(args):
         "e2e": e2e,
         "cpu_baseline": cpu,
         "cudnn": cudnn,
+        "f2x3": f2x3,
         "clocks": clocks,
         "gpu_launches": args.steps * ops[0].launches_per_call,
     }
