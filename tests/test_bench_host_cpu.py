@@ -83,3 +83,37 @@ def test_load_phase_runs_steps_for_the_given_time(monkeypatch):
     b.load_phase(lambda i: steps.append(i), "cuda:0", seconds=0.05)
     assert steps == list(range(len(steps))) and len(steps) >= 16 and len(steps) % 16 == 0
     assert syncs and all(d == "cuda:0" for d in syncs)
+
+
+def test_f2x3_report_records_a_failing_path_instead_of_raising():
+    """A failure of either F(2x3) path is reported in the bench line; the
+    headline it sits beside is not lost."""
+    b = load_bench()
+
+    class _Buf:
+        def data_ptr(self):
+            return 16
+
+    class _Err(Exception):
+        pass
+
+    class _Wg:
+        ALGO_2X3, ALGO_2X3_FUSED = 1, 2
+
+        @staticmethod
+        def make_problem(*a):
+            return a
+
+        @staticmethod
+        def default_options(algo):
+            return algo
+
+        @staticmethod
+        def Conv2d(prob, opts):
+            raise _Err(f"cannot plan algorithm {opts}")
+
+    out = b.f2x3_paths(_Wg, None, [_Buf()], [_Buf()], _Buf(), (1, 8, 8, 8, 8), 0, "cuda:0", 3,
+                       {"hbm_gbs": 1.0, "bf16_tflops": 1.0}, "measured")
+    assert set(out) == {"non_fused", "fused"}
+    assert out["non_fused"]["error"] == "_Err: cannot plan algorithm 1"
+    assert out["fused"]["error"] == "_Err: cannot plan algorithm 2"
