@@ -328,6 +328,34 @@ def winograd_conv(x, wt, m, p=1, q=1, variant=None):
     return output_transform(Mw, m, n, k, oh, ow, variant)
 
 
+def row_winograd_conv(x, wt, p=1, q=1, variant="F4"):
+    """Row-Winograd F(4x3) in float64: the 1-D transform F(4,3) along the
+    width and the three filter rows summed directly along the height, the
+    arithmetic of the operator's fused row kernel (it has no counterpart in
+    the reference).  For output row i and 4-wide tile t:
+        y[i][4t:4t+4] = A^T sum_r sum_c (G g[k][c][r]) . (B^T x[c][i+r-p][4t-q:4t-q+6]).
+    Equals the direct convolution up to float64 rounding."""
+    m, B, Gm, A = XFORMS[variant]
+    x = np.asarray(x, dtype=np.float64)
+    g = np.asarray(wt, dtype=np.float64)
+    n, c, h, w = x.shape
+    k = g.shape[0]
+    oh, ow = out_hw(h, w, 3, 3, 1, 1, p, q)
+    a = m + 2
+    tw = -(-ow // m)
+    wp = tw * m + 2
+    xp = np.zeros((n, c, oh + 2, wp))
+    hh = min(h, oh + 2 - p)
+    ww = min(w, wp - q)
+    xp[:, :, p:p + hh, q:q + ww] = x[:, :, :hh, :ww]
+    d = np.stack([xp[:, :, :, t * m:t * m + a] for t in range(tw)], axis=3)   # [N][C][OH+2][TW][alpha]
+    v = np.einsum("ej,nchtj->nchte", B, d)
+    u = np.einsum("es,kcrs->kcre", Gm, g)                                    # [K][C][3][alpha]
+    mm = sum(np.einsum("kce,ncite->nkite", u[:, :, r, :], v[:, :, r:r + oh]) for r in range(3))
+    y = np.einsum("oe,nkite->nkito", A, mm).reshape(n, k, oh, tw * m)
+    return y[:, :, :, :ow]
+
+
 def direct_flops(n, c, h, w, k, p=1, q=1):
     oh, ow = out_hw(h, w, 3, 3, 1, 1, p, q)
     return 2.0 * n * k * oh * ow * c * 9

@@ -99,3 +99,16 @@ def test_reference_build_agrees_when_present():
         a, _ = O.conv2d_direct(x, wt, p=p, q=p)
         b = O.ref_conv2dcpu(x, wt, p=p, q=p)
         assert np.array_equal(a.view(np.uint16), b.view(np.uint16))
+
+
+@pytest.mark.parametrize("variant", ["F4", "F4Ref"])
+@pytest.mark.parametrize("shape,pad", [((2, 5, 9, 11, 6), (1, 1)), ((1, 3, 7, 7, 4), (0, 0)),
+                                       ((2, 4, 6, 13, 3), (2, 2)), ((1, 6, 10, 5, 5), (1, 0))])
+def test_row_winograd_restatement_equals_direct_fp64(variant, shape, pad):
+    """The row-Winograd F(4x3) arithmetic (1-D F(4,3) along the width, direct
+    sum over the filter rows) is an exact convolution in float64."""
+    x, wt = O.uniform_inputs(8, *shape)
+    y = O.row_winograd_conv(x.astype(np.float64), wt.astype(np.float64), *pad, variant=variant)
+    _, r64 = O.conv2d_direct(x, wt, p=pad[0], q=pad[1])
+    assert y.shape == r64.shape
+    assert np.abs(y - r64).max() < 1e-10
