@@ -50,7 +50,8 @@ EXPORTS = [
     "conv2d_refresh_filter", "conv2d_destroy", "conv2d_get_algo", "conv2d_workspace_bytes",
     "conv2d_launches_per_call", "conv2d_check_device", "conv2d_last_error", "conv2d_last_error_message",
     "conv2d_status_string", "conv2d_select_reference", "conv2d_copy_to_host", "conv2d_fp16_timed",
-    "conv2d_autotune", "conv2d_autotune_clear", "conv2d_fp16_noalloc",
+    "conv2d_autotune", "conv2d_autotune_clear", "conv2d_fp16_noalloc", "conv2d_noalloc_check_device",
+    "conv2d_noalloc_selftest_expire",
     "conv2d_batch_create", "conv2d_batch_run", "conv2d_batch_run_percall", "conv2d_batch_info",
     "conv2d_batch_launches", "conv2d_batch_check_device", "conv2d_batch_destroy",
     "conv2d_server_config_default", "conv2d_server_create", "conv2d_server_add_layer", "conv2d_server_submit",
@@ -111,6 +112,8 @@ def lib():
         L.conv2d_autotune.argtypes = [ctypes.POINTER(Problem), ctypes.POINTER(Options), ip, ip]
         L.conv2d_autotune_clear.restype = None
         L.conv2d_fp16_noalloc.argtypes = [ctypes.POINTER(Problem), vp]
+        L.conv2d_noalloc_check_device.argtypes = [ip]
+        L.conv2d_noalloc_selftest_expire.argtypes = [vp]
         L.conv2d_batch_create.argtypes = [ctypes.POINTER(Problem), ctypes.c_int, ctypes.POINTER(Options),
                                           ctypes.POINTER(vp)]
         L.conv2d_batch_run.argtypes = [vp, vp]
@@ -262,6 +265,14 @@ def conv2d_noalloc(problem: Problem, stream: int | None = None):
     """F(2x3) convolution through the entry point that allocates no device
     memory (workspace in the library's fixed scratch array)."""
     _check(lib().conv2d_fp16_noalloc(ctypes.byref(problem), ctypes.c_void_p(stream or 0)))
+
+
+def noalloc_check_device():
+    """(status, site) of the no-allocation path's error word on the current
+    device (waits for the device; clears the word)."""
+    site = ctypes.c_int(0)
+    st = lib().conv2d_noalloc_check_device(ctypes.byref(site))
+    return st, site.value
 
 
 class ServerConfig(ctypes.Structure):

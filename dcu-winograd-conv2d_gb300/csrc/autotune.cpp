@@ -1,7 +1,7 @@
 // Per-shape algorithm and tile choice (CONV2D_ALGO_AUTO).
 //
 // The reference picks F(2x3) fused / F(2x3) / F(4x3) with fixed size rules
-// (src/conv2d.cpp:125-156).  Here every candidate (algorithm x GEMM channel
+// (src/conv2d.cpp:83-114).  Here every candidate (algorithm x GEMM channel
 // tile, plus the row-Winograd F(4x3) kernel this operator adds) is planned on scratch output memory and timed on the device the
 // first time a shape is seen; the winner is cached per shape and, when
 // WG_CONV2D_TUNE_FILE names a file, persisted there so later processes make

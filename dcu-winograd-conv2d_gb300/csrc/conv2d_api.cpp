@@ -3,12 +3,12 @@
 // Mirrors the reference's operator API (include/conv2d.h:8-42,
 // src/conv2d.cpp:1-133): getParamsize returns the size of the opaque param
 // blob, getkernelInfo fills it (selection + device workspace, as
-// src/conv2d.cpp:66-157 does), conv2d_fp16 runs the selected algorithm
-// (src/conv2d.cpp:160-175).  Differences, each deliberate:
+// src/conv2d.cpp:24-116 does), conv2d_fp16 runs the selected algorithm
+// (src/conv2d.cpp:118-133).  Differences, each deliberate:
 //   * sizes are computed in 64-bit arithmetic (the reference's unsigned 32-bit
 //     products overflow for large batches);
 //   * no file-static state is mutated (the reference rewrites its tile
-//     constants on the F(2x3)-non-fused branch, src/conv2d.cpp:131-134);
+//     constants on the F(2x3)-non-fused branch, src/conv2d.cpp:89-92);
 //   * unsupported descriptors return a status code;
 //   * the filter transform runs once per weight set (first call) instead of
 //     on every call, and the workspace can be released (conv2d_destroy).
@@ -66,7 +66,7 @@ int env_algo(int dflt) {
 int select_reference64(unsigned long long n, unsigned long long c, unsigned long long h, unsigned long long w,
                        unsigned long long k, unsigned long long r, unsigned long long s, unsigned long long oh,
                        unsigned long long ow) {
-    // src/conv2d.cpp:118-156 with the tile constants of a first call:
+    // src/conv2d.cpp:76-114 with the tile constants of a first call:
     // fused F(2x3) when the image is at least 10x the filter, F(2x3)
     // non-fused when the F(4x3) filter workspace exceeds 4x the input one,
     // else F(4x3).
@@ -365,8 +365,7 @@ int Plan::run_range(int n0, int nc, const GemmPlan* gp, cudaStream_t s) {
 }
 
 int Plan::run(cudaStream_t s) {
-    int cur = -1;
-    if (cudaGetDevice(&cur) == cudaSuccess && cur != device) cudaSetDevice(device);
+    DeviceGuard dg(device);
     if (!filter_ready || opt.filter_policy == 1) {
         int st = filter(s);
         if (st) return st;
@@ -461,8 +460,7 @@ const GemmPlan* Plan::host_gemm_for(int nc) {
 // front-loads its set-up (on the 32 x 256 x 56^2 layer: 413-418 us per call
 // queued directly, 434-437 us replayed).
 int Plan::run_host(const void* host_in, void* host_out, cudaStream_t s) {
-    int cur = -1;
-    if (cudaGetDevice(&cur) == cudaSuccess && cur != device) cudaSetDevice(device);
+    DeviceGuard dg(device);
     if (!filter_ready || opt.filter_policy == 1) {
         int st = filter(s);
         if (st) return st;
@@ -670,14 +668,18 @@ int conv2d_fp16_host(const void* param_ptr, const void* host_in, void* host_out,
 int conv2d_refresh_filter(const void* param_ptr, void* stream) {
     Plan* pl = plan_of(param_ptr);
     if (!pl) return fail(CONV2D_ERR_INVALID, "param blob not set up by getkernelInfo");
+    DeviceGuard dg(pl->device);
     return pl->filter(static_cast<cudaStream_t>(stream));
 }
 
 int conv2d_destroy(void* param_ptr) {
     Plan* pl = plan_of(param_ptr);
     if (!pl) return fail(CONV2D_ERR_INVALID, "param blob not set up by getkernelInfo");
-    cudaDeviceSynchronize();
-    delete pl;
+    {
+        DeviceGuard dg(pl->device);
+        cudaDeviceSynchronize();
+        delete pl;
+    }
     std::memset(param_ptr, 0, sizeof(ParamBlob));
     return CONV2D_OK;
 }
@@ -700,6 +702,7 @@ int conv2d_launches_per_call(const void* param_ptr) {
 int conv2d_check_device(const void* param_ptr, int* site) {
     Plan* pl = plan_of(param_ptr);
     if (!pl) return fail(CONV2D_ERR_INVALID, "param blob not set up by getkernelInfo");
+    DeviceGuard dg(pl->device);
     cudaError_t ce = cudaDeviceSynchronize();
     if (ce != cudaSuccess) return cuda_fail(ce, "device synchronize");
     DevErr h{};
@@ -741,6 +744,7 @@ int conv2d_fp16_timed(const void* param_ptr, void* stream, float* kernel_ms, int
     Plan* pl = plan_of(param_ptr);
     if (!pl) return fail(CONV2D_ERR_INVALID, "param blob not set up by getkernelInfo");
     if (!kernel_ms || max_kernels <= 0) return fail(CONV2D_ERR_INVALID, "null output array");
+    DeviceGuard dg(pl->device);
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     if (!pl->filter_ready) {
         int st = pl->filter(s);

@@ -15,6 +15,11 @@
 // make that first call before any stream capture.  Every call on a device
 // uses the same array: calls whose work overlaps on the GPU (two streams, or
 // two host threads) race on it and must be ordered by the caller.
+//
+// Errors: the kernels' bounded waits report into an error word at the start
+// of the array, which every call clears first; conv2d_noalloc_check_device
+// waits for the device and reports (and clears) it, as conv2d_check_device
+// does for a param blob.
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -24,6 +29,7 @@
 #include "../../include/conv2d.h"
 #include "wg_kernels.h"
 #include "wg_plan.h"
+#include "wg_ptx.cuh"
 
 namespace wg {
 
@@ -55,6 +61,16 @@ cudaError_t scratch_for(int device, void** out) {
 
 int noalloc_fail(int status, const char* msg) { return set_last_error(status, msg); }
 
+// Test hook of the error path: one thread waits on a barrier that nothing
+// completes; the bounded wait gives up after its time limit and records the
+// timeout in `err`, as a kernel of the no-allocation path would.
+__global__ void noalloc_expire_kernel(DevErr* err) {
+    __shared__ uint64_t bar;
+    mbar_init(&bar, 1);
+    fence_barrier_init();
+    mbar_wait(&bar, 0, nullptr, err, ERR_SITE_FULL);
+}
+
 }  // namespace
 
 }  // namespace wg
@@ -77,6 +93,14 @@ extern "C" int conv2d_fp16_noalloc(const problem_t* problem, void* stream) {
     if (bErr + bU + bV + bM > static_cast<long long>(kNoAllocScratchBytes))
         return noalloc_fail(CONV2D_ERR_UNSUPPORTED,
                             "problem needs more workspace than the 32 MiB no-allocation scratch holds");
+    {
+        // the input transform stages whole input rows in shared memory: rows
+        // too wide for it are refused before anything is queued
+        int in_smem = 0;
+        make_in_desc(g, problem->in, problem->in, nullptr, nullptr, &in_smem);
+        if (in_smem > 232448)
+            return noalloc_fail(CONV2D_ERR_UNSUPPORTED, "input rows too wide for the staged input transform");
+    }
     int device = 0;
     if (cudaGetDevice(&device) != cudaSuccess) return noalloc_fail(CONV2D_ERR_CUDA, "no CUDA device");
     void* base = nullptr;
@@ -105,4 +129,39 @@ extern "C" int conv2d_fp16_noalloc(const problem_t* problem, void* stream) {
         launch_output_transform(Xform::F2, false, g, Mw, problem->out, nullptr, err, s) != cudaSuccess)
         return noalloc_fail(CONV2D_ERR_CUDA, "kernel launch failed");
     return CONV2D_OK;
+}
+
+extern "C" int conv2d_noalloc_check_device(int* site) {
+    int device = 0;
+    if (cudaGetDevice(&device) != cudaSuccess) return noalloc_fail(CONV2D_ERR_CUDA, "no CUDA device");
+    if (site) *site = 0;
+    if (device < 0 || device >= kMaxDevices) return noalloc_fail(CONV2D_ERR_CUDA, "device index out of range");
+    void* base = nullptr;
+    {
+        std::lock_guard<std::mutex> lk(g_mu);
+        base = g_dev_ptr[device];
+    }
+    if (!base) return CONV2D_OK;   // no call has run on this device
+    if (cudaDeviceSynchronize() != cudaSuccess) return noalloc_fail(CONV2D_ERR_CUDA, "device synchronize failed");
+    DevErr h{};
+    if (cudaMemcpy(&h, base, sizeof(h), cudaMemcpyDeviceToHost) != cudaSuccess)
+        return noalloc_fail(CONV2D_ERR_CUDA, "error word copy failed");
+    if (site) *site = static_cast<int>(h.code);
+    if (h.code) {
+        if (cudaMemset(base, 0, sizeof(DevErr)) != cudaSuccess)
+            return noalloc_fail(CONV2D_ERR_CUDA, "error word reset failed");
+        return noalloc_fail(CONV2D_ERR_TIMEOUT, "a kernel of the no-allocation path gave up a bounded wait");
+    }
+    return CONV2D_OK;
+}
+
+extern "C" int conv2d_noalloc_selftest_expire(void* stream) {
+    int device = 0;
+    if (cudaGetDevice(&device) != cudaSuccess) return noalloc_fail(CONV2D_ERR_CUDA, "no CUDA device");
+    void* base = nullptr;
+    if (scratch_for(device, &base) != cudaSuccess)
+        return noalloc_fail(CONV2D_ERR_CUDA, "cudaGetSymbolAddress of the scratch array failed");
+    noalloc_expire_kernel<<<1, 1, 0, static_cast<cudaStream_t>(stream)>>>(static_cast<DevErr*>(base));
+    const cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? CONV2D_OK : noalloc_fail(CONV2D_ERR_CUDA, cudaGetErrorString(e));
 }

@@ -73,8 +73,7 @@ extern "C" {
 int conv2d_plan_save(const void* param, const char* path) {
     Plan* pl = plan_of(param);
     if (!pl || !path) return set_last_error(CONV2D_ERR_INVALID, "param blob not set up, or null path");
-    int cur = -1;
-    if (cudaGetDevice(&cur) == cudaSuccess && cur != pl->device) cudaSetDevice(pl->device);
+    DeviceGuard dg(pl->device);
     if (!pl->filter_ready || pl->opt.filter_policy == 1) {
         const int st = pl->filter(nullptr);
         if (st) return st;
@@ -117,8 +116,7 @@ int conv2d_plan_load(const void* param, const char* path) {
     std::fclose(f);
     if (!ok) return set_last_error(CONV2D_ERR_INVALID, "plan file truncated");
     if (fnv1a(u.data(), u.size()) != h.checksum) return set_last_error(CONV2D_ERR_INVALID, "plan file checksum mismatch");
-    int cur = -1;
-    if (cudaGetDevice(&cur) == cudaSuccess && cur != pl->device) cudaSetDevice(pl->device);
+    DeviceGuard dg(pl->device);
     // U may still be read by work queued earlier on any stream
     if (cudaDeviceSynchronize() != cudaSuccess || cudaMemcpy(pl->U, u.data(), u.size(), cudaMemcpyHostToDevice) != cudaSuccess)
         return set_last_error(CONV2D_ERR_CUDA, "copy of the transformed filter failed");

@@ -94,6 +94,25 @@ struct Plan {
     void release();
 };
 
+// Makes `device` current for the guard's lifetime and then restores the
+// device that was current before: an entry point working on a plan of another
+// device must not change the calling thread's current device.
+class DeviceGuard {
+   public:
+    explicit DeviceGuard(int device) {
+        int cur = -1;
+        if (cudaGetDevice(&cur) == cudaSuccess && cur != device && cudaSetDevice(device) == cudaSuccess) prev_ = cur;
+    }
+    ~DeviceGuard() {
+        if (prev_ >= 0) cudaSetDevice(prev_);
+    }
+    DeviceGuard(const DeviceGuard&) = delete;
+    DeviceGuard& operator=(const DeviceGuard&) = delete;
+
+   private:
+    int prev_ = -1;
+};
+
 int validate_problem(const problem_t* pr);
 int options_default(conv2d_options_t* o);
 int default_bn(int K);

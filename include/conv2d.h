@@ -20,6 +20,14 @@
  * transform (about 1,200 columns for F(4x3)).  Unsupported descriptors are
  * rejected with a status code (the reference computes garbage for them).
  *
+ * WEIGHTS ARE READ ONCE.  Unlike the reference, which re-reads `weight` on
+ * every call, the filter is transformed into the Winograd domain on the first
+ * conv2d_fp16 call after getkernelInfo and the transformed copy is reused by
+ * every later call.  A caller that changes the weights in place must call
+ * conv2d_refresh_filter (or set filter_policy = 1 / WG_CONV2D_FILTER_EVERY_CALL=1
+ * to transform on every call, as the reference does); otherwise later calls
+ * use the old weights.
+ *
  * The reference exports getParamsize/getkernelInfo with C++ linkage; this
  * library exports them both with C linkage (declared here) and with the
  * reference's C++-mangled names, so code compiled against either header links.
@@ -81,7 +89,7 @@ enum {
 /* Algorithms; values 0..2 are the reference's enum winograd_select
  * (include/common.h:140-144). */
 enum {
-    CONV2D_ALGO_REFERENCE = -1,  /* the reference's selection rule (src/conv2d.cpp:125-156) */
+    CONV2D_ALGO_REFERENCE = -1,  /* the reference's selection rule (src/conv2d.cpp:83-114) */
     CONV2D_ALGO_4X3_NON_FUSED = 0,
     CONV2D_ALGO_2X3_NON_FUSED = 1,
     CONV2D_ALGO_2X3_FUSED = 2,
@@ -130,9 +138,10 @@ int conv2d_fp16_ex(const void* param_ptr, void* stream);
 
 /* End-to-end call with HOST buffers: copies host_in (n*c*h*w fp16) to the
  * problem's device input, runs, copies the output to host_out and waits for
- * the stream.  The batch is cut into up to 4 image chunks whose input copies,
- * compute and output copies overlap (two internal copy streams); with pinned
- * host memory the copies run at full link speed. */
+ * the stream.  The batch is cut into up to 8 image chunks (at least 6 MB of
+ * copies each; WG_CONV2D_HOST_CHUNKS / WG_CONV2D_HOST_SIZES override) whose
+ * input copies, compute and output copies overlap (two internal copy
+ * streams); with pinned host memory the copies run at full link speed. */
 int conv2d_fp16_host(const void* param_ptr, const void* host_in, void* host_out, void* stream);
 
 /* Re-run the filter transform (after the caller changed the weights in place). */
@@ -274,8 +283,26 @@ int conv2d_fp16_timed(const void* param_ptr, void* stream, float* kernel_ms, int
  * tiles rounded up to 8 for P8) exceeds it return CONV2D_ERR_UNSUPPORTED.
  * The first call on a device looks the array up (make it before any stream
  * capture); all calls on a device share the array, so calls that overlap on
- * the GPU race and the caller must order them. */
+ * the GPU race and the caller must order them.  Input rows too wide for the
+ * staged input transform also return CONV2D_ERR_UNSUPPORTED, before anything
+ * is queued.  A kernel that gives up a bounded wait leaves a garbage output
+ * and records the failure in an error word inside the array (each call
+ * clears it first): read it with conv2d_noalloc_check_device. */
 int conv2d_fp16_noalloc(const problem_t* problem, void* stream);
+
+/* No counterpart in the reference.  Waits for the current device, then
+ * reports (and clears) the error word of conv2d_fp16_noalloc on that device:
+ * CONV2D_OK, or CONV2D_ERR_TIMEOUT when one of its kernels gave up a bounded
+ * wait since the last call; `site` (may be NULL) receives the first failing
+ * wait site.  Allocates nothing. */
+int conv2d_noalloc_check_device(int* site);
+
+/* No counterpart in the reference; a test hook of the error path above.
+ * Queues on `stream` one thread that waits on a barrier nothing completes:
+ * after the wait limit (0.5 s) it gives up and records a timeout in the
+ * no-allocation error word, as a kernel of conv2d_fp16_noalloc would.  The
+ * device stays usable. */
+int conv2d_noalloc_selftest_expire(void* stream);
 
 /* Copies `bytes` from device memory to host memory and waits (used by tests
  * to read the Winograd-domain workspaces U_d/V_d/M_d of the param blob). */

@@ -15,7 +15,7 @@
  *   - the benchmark's input generator (src/main.cpp:36-44): glibc rand()
  *     with its default seed, (rand()%255)/255.0 rounded to fp16, the input
  *     first, then the weights.
- *   - the algorithm selection of getkernelInfo (src/conv2d.cpp:66-157), in
+ *   - the algorithm selection of getkernelInfo (src/conv2d.cpp:76-114), in
  *     the reference's unsigned 32-bit arithmetic and with the tile
  *     constants it starts with (src/conv2d.cpp:3-8).
  *
@@ -266,7 +266,7 @@ int orc_conv2d_direct(const uint16_t *in, const uint16_t *wt, uint16_t *out16, d
     return 0;
 }
 
-/* ---- algorithm selection (src/conv2d.cpp:66-157) ----------------------- */
+/* ---- algorithm selection (src/conv2d.cpp:76-114) ----------------------- */
 /* 0 = F(4x3) non-fused, 1 = F(2x3) non-fused, 2 = F(2x3) fused: the order
  * of enum winograd_select (include/common.h:140-144).  Arithmetic is the
  * reference's unsigned 32-bit arithmetic with the tile constants of a

@@ -8,7 +8,7 @@ Contents
     (reference ``include/verfiy.h:5-44``) restated in C, returning both the
     fp16-rounded result and the FP64 sum; the benchmark's glibc-``rand()``
     input fill (``src/main.cpp:36-44``); the algorithm selection of
-    ``getkernelInfo`` (``src/conv2d.cpp:66-157``).
+    ``getkernelInfo`` (``src/conv2d.cpp:24-116``).
   * ctypes binding of the reference's own ``conv2dcpu`` compiled from the
     reference sources (``oracle/_ref``), when that build exists.
   * numpy float64 restatements of the Winograd transforms, with the matrices

@@ -14,7 +14,9 @@ import oracle as O
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 HEADER = os.path.join(ROOT, "include", "conv2d.h")
-REF_HEADER_DIR = "/root/reference/include"
+# the reference tree is read only where it is present (its header, to compile
+# a caller written for it); WG_REFERENCE_TREE points elsewhere
+REF_HEADER_DIR = os.path.join(os.environ.get("WG_REFERENCE_TREE", "/root/reference"), "include")
 
 
 def declared_functions():
@@ -89,6 +91,17 @@ def test_null_pointers_rejected(wg):
     # a blob that getkernelInfo never filled
     blob = (ctypes.c_ubyte * 256)()
     assert wg.lib().conv2d_fp16_ex(ctypes.cast(blob, ctypes.c_void_p), None) == wg.ERR_INVALID
+
+
+def test_noalloc_refuses_before_any_cuda_call(wg):
+    """The no-allocation entry point checks its scratch size and the staged
+    input rows on the host, before it touches the device."""
+    too_big = wg.make_problem(256, 256, 256, 64, 256, 56, 56, 256)
+    assert wg.lib().conv2d_fp16_noalloc(ctypes.byref(too_big), None) == wg.ERR_UNSUPPORTED
+    assert b"32 MiB" in wg.lib().conv2d_last_error_message()
+    too_wide = wg.make_problem(256, 256, 256, 1, 8, 3, 4000, 8)
+    assert wg.lib().conv2d_fp16_noalloc(ctypes.byref(too_wide), None) == wg.ERR_UNSUPPORTED
+    assert b"too wide" in wg.lib().conv2d_last_error_message()
 
 
 SHAPES = [
