@@ -3,15 +3,19 @@
 
 Default workload: N=32, C=256, H=W=56, K=256, 3x3, pad 1, stride 1, fp16
 NCHW input ~U[-1,1] and fp16 filter ~N(0, std 1/sqrt(9C)) from a fixed seed,
-run through the operator's C ABI with the reference's algorithm selection
-(F(2x3) fused for this shape) unless --algo says otherwise.
+run through the operator's C ABI with the per-shape autotuner's algorithm
+(--algo ref gives the reference's selection rule, F(2x3) fused here).
 
 One step = one conv2d call over one batch.  `value` is effective TFLOP/s
 (direct-convolution FLOPs 2*N*K*OH*OW*C*9 / time) with inputs resident in
 HBM; `e2e` is the same metric through the host-buffer C entry point
 (conv2d_fp16_host: pinned input copied in, output copied out, every step).
 Buffer sets rotate so the bytes touched between two uses of one set exceed
-the 129 MB L2.
+the 129 MB L2.  The line also carries the metric's comparison: the
+24-problem batch grouped vs per-call (`batched`), a bounded request trace
+through the continuous-batching server vs the plain per-call path
+(`served`), both summarised in `served_vs_percall`, and the relative error
+of the timed output against FP64 (`rel_err`).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
                     [--workload cfg2|cfg1|cfg3|...] [--algo ref|fused|2x3|4x3|row|auto]
@@ -36,7 +40,8 @@ L2_BYTES = 129 * 1024 * 1024
 # (n, c, h, w, k, input distribution, filter distribution, description)
 WORKLOADS = {
     "cfg2": (32, 256, 56, 56, 256, "uniform", "normal",
-             "single-shape F(2x3) workload: N=32 C=256 H=W=56 K=256, 3x3 pad 1 stride 1, fp16 NCHW"),
+             "single-shape workload N=32 C=256 H=W=56 K=256, 3x3 pad 1 stride 1, fp16 NCHW (configured as "
+             "F(2x3) fused and non-fused: both reported under f2x3; the headline runs the autotuner's choice)"),
     "cfg1": (1, 64, 56, 56, 64, "uniform", "uniform",
              "small workload: N=1 C=64 H=W=56 K=64, 3x3 pad 1 stride 1, fp16 NCHW"),
     "cfg3": (32, 512, 28, 28, 512, "normal", "normal",
@@ -303,20 +308,23 @@ def make_inputs(torch, workload, device, seed):
     return x, wt
 
 
-def roofline_for(name, wg, geo, ms, pk, pk_kind):
-    """Roofline of one kernel from its algorithmic work per launch.
+def algorithmic_work(name, geo):
+    """Per-launch work of one kernel (P tiles, E = (m+2)^2 Winograd elements,
+    fp16 tensors and operands).
 
-    GEMM-shaped kernels have both a FLOP count and a byte count; the bound is
-    the roof their arithmetic intensity puts them under (machine balance =
-    peak FLOP/s / peak bytes/s).  Algorithmic bytes (fp16 operands, M in fp32
-    for F(4x3), fp16 otherwise):
-      input_transform   x read (2*N*C*H*W) + V write (2*E*P*C)
-      gemm_tcgen05      V read (2*E*P*C) + U read (2*E*C*K) + M write (E*P*K*4 or *2)
-      output_transform  M read + y write (2*N*K*OH*OW)
-      fused2x3          x read + U read + y write
-      row4x3            x read + U1 read (2*18*C*K) + y write; tensor work
-                        2*18*RT*C*K over RT = N*OH*ceil(OW/4) row tiles
-    """
+    Algorithmic bytes are the per-unit figures of the hot path's measurement
+    table: what a kernel must move whatever its design.  The GEMM's are V and
+    U; its fp32 M is not counted, since an epilogue that applied A^T m A would
+    keep M on chip, and the output transform's are the output y alone.  M is
+    reported separately as `design_bytes` (the bytes this three-kernel design
+    moves), so the difference shows what the unfused M costs.
+      input_transform   x (2*N*C*H*W) + V (2*E*P*C)
+      gemm_tcgen05      V + U (2*E*C*K);            FLOPs 2*E*P*C*K
+      output_transform  y (2*N*K*OH*OW)
+      fused2x3          x + U + y;                   FLOPs 2*16*P*C*K
+      row4x3            x + U1 (2*18*C*K) + y;       FLOPs 2*18*RT*C*K over
+                        RT = N*OH*ceil(OW/4) row tiles
+    Returns (algorithmic bytes, design bytes, FLOPs, formula)."""
     n, c, h, w, k, m = geo
     oh, ow = h, w  # pad 1
     tiles = n * math.ceil(oh / m) * math.ceil(ow / m)
@@ -324,18 +332,28 @@ def roofline_for(name, wg, geo, ms, pk, pk_kind):
     mb = 4.0 if m == 4 else 2.0
     x_b, y_b = 2.0 * n * c * h * w, 2.0 * n * k * oh * ow
     v_b, u_b, m_b = 2.0 * E * tiles * c, 2.0 * E * c * k, mb * E * tiles * k
-    flops = 0.0
     if name == "gemm_tcgen05":
-        flops, byts, formula = 2.0 * E * tiles * c * k, v_b + u_b + m_b, "V + U + M"
-    elif name == "fused2x3":
-        flops, byts, formula = 2.0 * E * tiles * c * k, x_b + u_b + y_b, "x + U + y"
-    elif name == "row4x3":
+        return v_b + u_b, v_b + u_b + m_b, 2.0 * E * tiles * c * k, f"V + U (design adds M {m_b / 1e6:.1f} MB)"
+    if name == "fused2x3":
+        return x_b + u_b + y_b, x_b + u_b + y_b, 2.0 * E * tiles * c * k, "x + U + y"
+    if name == "row4x3":
         rt = n * oh * math.ceil(ow / 4)
-        flops, byts, formula = 2.0 * 18 * rt * c * k, x_b + 2.0 * 18 * c * k + y_b, "x + U1 + y"
-    elif name == "input_transform":
-        byts, formula = x_b + v_b, "x + V"
-    else:
-        byts, formula = m_b + y_b, "M + y"
+        u1 = 2.0 * 18 * c * k
+        return x_b + u1 + y_b, x_b + u1 + y_b, 2.0 * 18 * rt * c * k, "x + U1 + y"
+    if name == "input_transform":
+        return x_b + v_b, x_b + v_b, 0.0, "x + V"
+    if name == "tile_scale":
+        return x_b, x_b, 0.0, "x"
+    return y_b, m_b + y_b, 0.0, f"y (design adds M {m_b / 1e6:.1f} MB)"
+
+
+def roofline_for(name, wg, geo, ms, pk, pk_kind):
+    """Roofline of one kernel from its algorithmic work per launch and its
+    CUDA-event duration `ms`.  A kernel with FLOPs is bound by the roof its
+    arithmetic intensity puts it under (machine balance = peak FLOP/s / peak
+    bytes/s); `frac` is the bound's time over the measured time, i.e. the
+    larger of the two fractions."""
+    byts, design, flops, formula = algorithmic_work(name, geo)
     peak_bw, peak_fl = pk["hbm_gbs"], pk["bf16_tflops"]
     out = {"kernel": name}
     if flops and flops / byts > peak_fl * 1e12 / (peak_bw * 1e9):
@@ -346,14 +364,67 @@ def roofline_for(name, wg, geo, ms, pk, pk_kind):
         ach = byts / (ms * 1e-3) / 1e9
         out.update({"bound": "hbm", "achieved": ach, "peak": peak_bw, "unit": "GB/s", "frac": ach / peak_bw,
                     "peak_source": f"{pk_kind} HBM copy"})
+    E = (geo[5] + 2) ** 2
     out["algorithmic_per_launch"] = f"{byts / 1e6:.1f} MB ({formula})" + (
         (f", {flops / 1e9:.2f} GFLOP (2*18*RT*C*K)" if name == "row4x3" else f", {flops / 1e9:.2f} GFLOP (2*{E}*P*C*K)")
         if flops else "")
     out["algorithmic_bytes"] = byts
+    out["design_bytes"] = design
+    out["design_bytes_frac"] = design / (ms * 1e-3) / 1e9 / peak_bw
     if flops:
         out["tensor_frac"] = flops / (ms * 1e-3) / 1e12 / peak_fl
+        out["hbm_frac"] = byts / (ms * 1e-3) / 1e9 / peak_bw
     out["launch_us"] = ms * 1e3
     return out
+
+
+def step_roofline(geo, algo, wg, ms_step, pk, pk_kind):
+    """Whole-step roofline of one call: the bytes no design can avoid (x, the
+    transformed filter U, y) and the algorithm's tensor work (its Winograd
+    GEMM FLOPs), against the measured time per step."""
+    n, c, h, w, k, m = geo
+    tiles = n * math.ceil(h / m) * math.ceil(w / m)
+    E = (m + 2) ** 2
+    x_b, y_b = 2.0 * n * c * h * w, 2.0 * n * k * h * w
+    if algo == wg.ALGO_4X3_ROW:
+        u_b, flops = 2.0 * 18 * c * k, 2.0 * 18 * n * h * math.ceil(w / 4) * c * k
+    else:
+        u_b, flops = 2.0 * E * c * k, 2.0 * E * tiles * c * k
+    t_bytes = (x_b + u_b + y_b) / (pk["hbm_gbs"] * 1e9)
+    t_flops = flops / (pk["bf16_tflops"] * 1e12)
+    return {"bytes": x_b + u_b + y_b, "formula": "x + U + y", "flops": flops,
+            "bound": "hbm" if t_bytes >= t_flops else "tensor",
+            "floor_us": max(t_bytes, t_flops) * 1e6, "ms_per_step": ms_step,
+            "frac": max(t_bytes, t_flops) / (ms_step * 1e-3), "peak_source": pk_kind}
+
+
+def rel_err_slice(x, wt, y, nhwc, tol, channels=8):
+    """Max / mean relative error of the operator's output against an FP64
+    direct convolution (pad 1) of image 0 at `channels` output channels
+    spread over K: |y - ref| / max(|ref|, rms(ref)), the parity tests'
+    measure, with the tolerance it is held to."""
+    import numpy as np
+    x0 = x[0].float().cpu().numpy().astype(np.float64)
+    if nhwc:
+        x0 = x0.transpose(2, 0, 1)
+    C, H, W = x0.shape
+    K = wt.shape[0]
+    ks = sorted({int(round(i * (K - 1) / max(1, channels - 1))) for i in range(channels)})
+    w64 = wt.float().cpu().numpy().astype(np.float64)[ks]
+    xp = np.zeros((C, H + 2, W + 2))
+    xp[:, 1:H + 1, 1:W + 1] = x0
+    ref = np.zeros((len(ks), H, W))
+    for r in range(3):
+        for s_ in range(3):
+            ref += np.tensordot(w64[:, :, r, s_], xp[:, r:r + H, s_:s_ + W], axes=([1], [0]))
+    y0 = y[0].float().cpu().numpy().astype(np.float64)
+    y0 = y0[:, :, ks].transpose(2, 0, 1) if nhwc else y0[ks]
+    rms = math.sqrt(float(np.mean(ref * ref)))
+    rel = np.abs(y0 - ref) / np.maximum(np.abs(ref), rms)
+    mx = float(rel.max())
+    return {"max": mx, "mean": float(rel.mean()), "tol": tol, "within_tol": bool(mx <= tol),
+            "against": f"FP64 direct convolution of image 0, output channels {ks}",
+            "measure": "|y - ref| / max(|ref|, rms(ref))"}
 
 
 def f2x3_paths(wg, torch, xs, ys, wt, geo, sptr, device, reps, pk, pk_kind):
@@ -389,7 +460,8 @@ def f2x3_paths(wg, torch, xs, ys, wt, geo, sptr, device, reps, pk, pk_kind):
             for nm, v in kt.items():
                 r = roofline_for(nm, wg, (n, c, h, w, k, 2), sum(v) / len(v), pk, pk_kind)
                 kernels[nm] = {key: r[key] for key in ("launch_us", "bound", "achieved", "unit", "frac",
-                                                      "algorithmic_per_launch", "tensor_frac") if key in r}
+                                                      "algorithmic_per_launch", "tensor_frac", "hbm_frac",
+                                                      "design_bytes_frac") if key in r}
             ok = all(op.check_device()[0] == wg.OK for op in ops)
             out[label] = {"value": flops / (ms * 1e-3) / 1e12, "unit": "TFLOP/s", "ms_per_call": ms,
                           "calls": reps, "kernels": kernels, "device_ok": ok}
@@ -439,6 +511,8 @@ def our_arm(args):
         opts.l2_chunk_bytes = args.l2_chunk
     if args.nhwc:
         opts.layout_nhwc = 1
+    if args.m_fp32:
+        opts.m_fp32 = 1
     in_bytes = 2 * n * c * h * w
     out_bytes = 2 * n * k * h * w
     nsets = max(2, math.ceil(3 * L2_BYTES / (in_bytes + out_bytes)))
@@ -505,8 +579,18 @@ def our_arm(args):
     roof = roofline_for(dominant, wg, (n, c, h, w, k, m), dom_ms, pk, pk_kind)
     traffic = committed_traffic(dominant, args.workload)
     roof["traffic"] = traffic
+    roof["traffic_over_algorithmic"] = traffic / roof["algorithmic_bytes"] if traffic else None
     roof["share_of_step"] = tot[dominant] / max(1e-9, sum(tot.values()))
+    roof["step"] = step_roofline((n, c, h, w, k, m), algo, wg, ms_per_step, pk, pk_kind)
     kernel_ms = {nm: sum(v) / len(v) * (len(v) / reps) for nm, v in kt.items()}
+    kernel_roofline = {nm: {key: r[key] for key in ("bound", "frac", "hbm_frac", "tensor_frac", "design_bytes_frac",
+                                                  "algorithmic_per_launch") if key in r}
+                       for nm, r in ((nm, roofline_for(nm, wg, (n, c, h, w, k, m), sum(kt[nm]) / len(kt[nm]), pk,
+                                                       pk_kind)) for nm in kt)}
+
+    # accuracy of what was timed: the last timed step's output against FP64
+    last = (args.steps - 1) % nsets
+    rel_err = rel_err_slice(xs[last], wt, ys[last], args.nhwc, 2e-2 if m == 4 else 1e-2)
 
     # the workload names F(2x3), fused and non-fused: both measured beside the
     # autotuned headline, on the same buffers
@@ -551,7 +635,7 @@ def our_arm(args):
                "sample": f"1 of {n} images ({fl / 1e9:.2f} GFLOP), all {k} output channels, {dt:.2f} s"}
 
     cudnn = None
-    if args.cudnn:
+    if not args.no_cudnn:
         if args.nhwc:  # cuDNN's channels-last kernels on the same values
             cx, cw = x0.contiguous(memory_format=torch.channels_last), wt.contiguous(memory_format=torch.channels_last)
         else:
@@ -559,6 +643,36 @@ def our_arm(args):
         cms = time_cudnn(torch, cx, cw, args.steps, args.warmup)
         cudnn = {"value": flops / (cms * 1e-3) / 1e12, "unit": "TFLOP/s", "ms_per_step": cms,
                  "path": f"torch.nn.functional.conv2d fp16 {'NHWC' if args.nhwc else 'NCHW'}, cudnn.benchmark"}
+    # the metric's comparison: batched and served runs against plain per-call
+    # launches of the same kernels, at the error the single-shape run holds
+    batched = served = None
+    launches_per_call = ops[0].launches_per_call
+    if args.workload == "cfg2" and not args.nhwc and world == 1 and not args.no_serving:
+        for op in ops:
+            op.destroy()
+        ops = []
+        try:
+            batched, _, _ = batched_run(wg, torch, device, max(5, min(args.steps, 20)), args.warmup)
+        except Exception as e:  # reported beside the headline, which stands on its own
+            batched = {"error": f"{type(e).__name__}: {e}"[:300]}
+        try:
+            served, _ = serving_run(wg, torch, device, args.line_requests, [0.9])
+        except Exception as e:
+            served = {"error": f"{type(e).__name__}: {e}"[:300]}
+    served_vs_percall = None
+    if batched or served:
+        served_vs_percall = {
+            "batched_24_problems": (batched or {}).get("grouped_over_percall"),
+            "served_saturated": ((served or {}).get("saturated") or {}).get("served_over_plain"),
+            "served_p50_p99_us_at_0.9_plain_capacity":
+                [(served or {}).get("sweep", [{}])[0].get("served", {}).get(k) for k in ("p50_us", "p99_us")]
+                if served and "sweep" in served else None,
+            "plain_p50_p99_us_at_0.9_plain_capacity":
+                [(served or {}).get("sweep", [{}])[0].get("plain", {}).get(k) for k in ("p50_us", "p99_us")]
+                if served and "sweep" in served else None,
+            "rel_err_max": rel_err["max"], "rel_err_tol": rel_err["tol"],
+            "target": ">= 1.5x plain per-call throughput at the stated error bound",
+        }
     lat = sorted(per_step)
     line = {
         "metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": world, "steps": args.steps,
@@ -569,16 +683,22 @@ def our_arm(args):
                    "input": f"{xdist}, filter {wdist}",
                    "l2": f"{nsets} rotating input/output sets ({nsets * (in_bytes + out_bytes) / 2**20:.0f} MiB) > L2",
                    "layout": "NHWC" if args.nhwc else "NCHW",
+                   "m_storage": "fp32" if (args.m_fp32 or args.nhwc) else "24-bit (F(4x3)) / fp16 (F(2x3))",
                    "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
         "latency_us": {"p50": lat[len(lat) // 2] * 1e3, "p99": lat[min(len(lat) - 1, int(0.99 * len(lat)))] * 1e3},
         "kernel_ms": kernel_ms,
+        "kernel_roofline": kernel_roofline,
         "roofline": roof,
+        "rel_err": rel_err,
         "e2e": e2e,
         "cpu_baseline": cpu,
         "cudnn": cudnn,
         "f2x3": f2x3,
+        "served_vs_percall": served_vs_percall,
+        "batched": batched,
+        "served": served,
         "clocks": clocks,
-        "gpu_launches": args.steps * ops[0].launches_per_call,
+        "gpu_launches": args.steps * launches_per_call,
     }
     if rank == 0:
         print(json.dumps(line), flush=True)
@@ -589,19 +709,14 @@ def our_arm(args):
     return 0
 
 
-def batch_arm(args):
-    """Batched workload: every problem of the draw in one grouped run (grouped
+def batched_run(wg, torch, device, steps, warmup, algo=3, seed=99, with_e2e=False):
+    """The 24-problem batch: every problem in one grouped run (grouped
     launches replayed from a CUDA graph) against the same problems launched
-    one conv2d call at a time."""
-    import torch
-    rank, world, local = env_dist()
-    torch.cuda.set_device(local)
-    device = torch.device("cuda", local)
-    wg = load_pkg()
-    wg.lib()
+    one conv2d call after another on the same stream (the per-call path).
+    Returns a summary dict (and the clock record of the grouped steps)."""
     shapes = batch_shapes()
     g = torch.Generator(device=device)
-    g.manual_seed(99 + rank)
+    g.manual_seed(seed)
     probs, keep = [], []
     flops = 0.0
     in_bytes = out_bytes = 0
@@ -615,11 +730,11 @@ def batch_arm(args):
         in_bytes += x.numel() * 2
         out_bytes += y.numel() * 2
     t0 = time.perf_counter()
-    batch = wg.Batch(probs, wg.default_options(algo=ALGO_ARG[args.algo if args.algo != "ref" else "auto"]))
+    batch = wg.Batch(probs, wg.default_options(algo=algo))
     setup_s = time.perf_counter() - t0
     stream = torch.cuda.current_stream(device)
     sptr = stream.cuda_stream
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         batch.run(sptr)
         batch.run_percall(sptr)
     torch.cuda.synchronize(device)
@@ -628,12 +743,12 @@ def batch_arm(args):
         raise RuntimeError(f"device wait gave up at site {site}")
 
     def timed(fn):
-        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
         torch.cuda.synchronize(device)
         a = torch.cuda.Event(enable_timing=True)
         b = torch.cuda.Event(enable_timing=True)
         a.record(stream)
-        for i in range(args.steps):
+        for i in range(steps):
             evs[i][0].record(stream)
             fn(sptr)
             evs[i][1].record(stream)
@@ -641,23 +756,23 @@ def batch_arm(args):
         torch.cuda.synchronize(device)
         return a.elapsed_time(b), sorted(x.elapsed_time(y) for x, y in evs)
 
-    sampler = ClockSampler(local)
+    sampler = ClockSampler(device.index or 0)
     sampler.start()
     load_phase(lambda i: batch.run(sptr), device)
     grouped_ms, lat = timed(batch.run)
     clocks = with_window(sampler.stop())
     percall_ms, lat_pc = timed(batch.run_percall)
-    value = world * flops * args.steps / (grouped_ms * 1e-3) / 1e12
-    percall = world * flops * args.steps / (percall_ms * 1e-3) / 1e12
-
-    # end to end: inputs copied in from pinned host memory, outputs copied out
+    st, site = batch.check_device()
+    if st != wg.OK:
+        raise RuntimeError(f"device wait gave up at site {site}")
     e2e = None
-    if not args.no_e2e:
+    if with_e2e:
+        # inputs copied in from pinned host memory, outputs copied out
         hin = [torch.empty(x.shape, dtype=torch.float16).pin_memory() for x, _, _ in keep]
         hout = [torch.empty(y.shape, dtype=torch.float16).pin_memory() for _, _, y in keep]
         for h, (x, _, _) in zip(hin, keep):
             h.copy_(x.cpu())
-        e_steps = max(3, min(args.steps, 10))
+        e_steps = max(3, min(steps, 10))
         torch.cuda.synchronize(device)
         t0 = time.perf_counter()
         for _ in range(e_steps):
@@ -668,29 +783,53 @@ def batch_arm(args):
                 h.copy_(y, non_blocking=True)
             torch.cuda.synchronize(device)
         el = time.perf_counter() - t0
-        e2e = {"value": world * flops * e_steps / el / 1e12, "unit": "TFLOP/s", "h2d_bytes_per_step": in_bytes,
+        e2e = {"value": flops * e_steps / el / 1e12, "unit": "TFLOP/s", "h2d_bytes_per_step": in_bytes,
                "d2h_bytes_per_step": out_bytes, "ms_per_step": el / e_steps * 1e3,
                "path": "pinned host copies of all 24 inputs/outputs around one grouped batch run"}
-    algos = [batch.info(i) for i in range(len(shapes))]
+    out = {
+        "workload": BATCH_WORKLOADS["cfg4"], "problems": [list(sh) for sh in shapes],
+        "algo_bn": [batch.info(i) for i in range(len(shapes))], "total_gflop": flops / 1e9, "setup_s": setup_s,
+        "grouped": {"tflops": flops * steps / (grouped_ms * 1e-3) / 1e12, "ms_per_step": grouped_ms / steps,
+                    "launches": batch.launches(True), "p50_us": lat[len(lat) // 2] * 1e3,
+                    "p99_us": lat[min(len(lat) - 1, int(0.99 * len(lat)))] * 1e3},
+        "percall": {"tflops": flops * steps / (percall_ms * 1e-3) / 1e12, "ms_per_step": percall_ms / steps,
+                    "launches": batch.launches(False), "p50_us": lat_pc[len(lat_pc) // 2] * 1e3,
+                    "p99_us": lat_pc[min(len(lat_pc) - 1, int(0.99 * len(lat_pc)))] * 1e3,
+                    "path": "each problem's own conv2d_fp16_ex launches, one problem after another on one stream"},
+        "grouped_over_percall": percall_ms / grouped_ms,
+        "steps": steps, "l2": f"working set {(in_bytes + out_bytes) / 2**30:.1f} GiB of inputs/outputs > L2",
+        "e2e": e2e,
+    }
+    batch.destroy()
+    del keep
+    return out, clocks, flops
+
+
+def batch_arm(args):
+    """Batched workload as its own line (value = the grouped run)."""
+    import torch
+    rank, world, local = env_dist()
+    torch.cuda.set_device(local)
+    device = torch.device("cuda", local)
+    wg = load_pkg()
+    wg.lib()
+    algo = ALGO_ARG[args.algo if args.algo != "ref" else "auto"]
+    res, clocks, flops = batched_run(wg, torch, device, args.steps, args.warmup, algo, 99 + rank, not args.no_e2e)
+    g = res["grouped"]
     line = {
-        "metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": grouped_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "metric": METRIC, "value": world * g["tflops"], "unit": "TFLOP/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": g["ms_per_step"], "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f16", "data": "synthetic (seeded torch RNG)",
-        "config": {"workload": BATCH_WORKLOADS[args.workload], "problems": [list(s) for s in shapes],
-                   "algo_bn": algos, "total_gflop": flops / 1e9, "accumulate": "fp32",
-                   "l2": f"working set {(in_bytes + out_bytes) / 2**30:.1f} GiB of inputs/outputs > L2",
-                   "setup_s": setup_s},
-        "percall": {"value": percall, "ms_per_step": percall_ms / args.steps,
-                    "launches": batch.launches(False)},
-        "grouped_over_percall": value / percall,
-        "latency_us": {"p50": lat[len(lat) // 2] * 1e3, "p99": lat[min(len(lat) - 1, int(0.99 * len(lat)))] * 1e3,
-                       "percall_p50": lat_pc[len(lat_pc) // 2] * 1e3},
-        "e2e": e2e, "clocks": clocks, "roofline": None, "cpu_baseline": None,
-        "gpu_launches": args.steps * batch.launches(True),
+        "config": {"workload": res["workload"], "problems": res["problems"], "algo_bn": res["algo_bn"],
+                   "total_gflop": res["total_gflop"], "accumulate": "fp32", "l2": res["l2"],
+                   "setup_s": res["setup_s"]},
+        "percall": res["percall"], "grouped_over_percall": res["grouped_over_percall"],
+        "latency_us": {"p50": g["p50_us"], "p99": g["p99_us"], "percall_p50": res["percall"]["p50_us"]},
+        "e2e": res["e2e"], "clocks": clocks, "roofline": None, "cpu_baseline": None,
+        "gpu_launches": args.steps * g["launches"],
     }
     if rank == 0:
         print(json.dumps(line), flush=True)
-    batch.destroy()
     return 0
 
 
@@ -730,24 +869,28 @@ def precision_arm(args):
     return 0
 
 
-def serve_arm(args):
-    """Serving loop: the same Poisson request trace through the continuous-
-    batching server (3 slots, up to 64 requests per batch) and through the
-    plain per-request path (1 slot, 1 request per launch sequence)."""
+def serve_layers(seed=20261203):
+    """The 16 resident layers of the serving workload: (c, k, h) each."""
     import numpy as np
-    import torch
-    rank, world, local = env_dist()
-    torch.cuda.set_device(local)
-    device = torch.device("cuda", local)
-    wg = load_pkg()
-    wg.lib()
-    rng = np.random.default_rng(20261203)
+    rng = np.random.default_rng(seed)
     layers = []
     for _ in range(16):
         c = int(rng.choice([64, 128, 256, 512]))
         k = int(rng.choice([64, 128, 256, 512]))
         h = int(rng.choice([7, 14, 28, 56, 112]))
         layers.append((c, k, h))
+    return layers, rng
+
+
+def serving_run(wg, torch, device, count, rates, with_clocks=False):
+    """One request trace through the continuous-batching server (3 slots, up
+    to 64 requests per batch) and through the plain per-call path (each
+    request's own kernels queued on one stream at its arrival, no batching,
+    no wait for earlier requests), same kernels and same arithmetic in both.
+    Saturated (every request arriving at once) and at Poisson arrival rates
+    given as multiples of the plain path's saturated capacity."""
+    import numpy as np
+    layers, rng = serve_layers()
     g = torch.Generator(device=device)
     g.manual_seed(7)
     bufs = []
@@ -756,7 +899,6 @@ def serve_arm(args):
         x = (torch.rand((64, c, h, h), generator=g, device=device) * 2 - 1).half()
         y = torch.empty((64, k, h, h), dtype=torch.float16, device=device)
         bufs.append((w, x, y))
-    count = args.requests
     req_layer = rng.integers(0, 16, count).tolist()
     req_n = rng.integers(1, 65, count).tolist()
     flops = sum(direct_flops(req_n[i], layers[req_layer[i]][0], layers[req_layer[i]][2], layers[req_layer[i]][2],
@@ -765,7 +907,8 @@ def serve_arm(args):
     outs = [bufs[li][2].data_ptr() for li in req_layer]
 
     def make(served):
-        srv = wg.Server(slots=3 if served else 1, max_batch=64 if served else 1, hbm_budget_bytes=40 << 30)
+        srv = (wg.Server(slots=3, max_batch=64, hbm_budget_bytes=40 << 30) if served
+               else wg.Server(per_request=1, hbm_budget_bytes=40 << 30))
         for (c, k, h), (w, _, _) in zip(layers, bufs):
             srv.add_layer(c, k, h, h, w.data_ptr())
         return srv
@@ -780,36 +923,55 @@ def serve_arm(args):
 
     plain = make(False)
     served = make(True)
-    # warm both (kernels, tensor maps) on a short trace, then measure the
-    # plain capacity: all requests arriving at once
+    # warm both (kernels, tensor maps), then measure the plain capacity:
+    # every request arriving at once
     run(plain, 1e9)
     run(served, 1e9)
     sat_plain = run(plain, 1e9)
     capacity = count / sat_plain["wall_s"]
+    sampler = ClockSampler(device.index or 0) if with_clocks else None
+    if sampler:
+        sampler.start()
     sweep = []
-    sampler = ClockSampler(local)
-    sampler.start()
-    for frac in args.rates:
+    for frac in rates:
         rate = frac * capacity
-        s_row = run(served, rate)
-        p_row = run(plain, rate)
-        sweep.append({"load_vs_plain_capacity": frac, "served": s_row, "plain": p_row})
-    clocks = sampler.stop()
+        sweep.append({"load_vs_plain_capacity": frac, "served": run(served, rate), "plain": run(plain, rate)})
     sat_served = run(served, 1e9)
+    clocks = sampler.stop() if sampler else None
     st = served.stats()
     plain.destroy()
     served.destroy()
-    line = {
-        "metric": METRIC, "value": sat_served["tflops"], "unit": "TFLOP/s", "n_gpus": world,
-        "steps": count, "warmup": count, "ms_per_step": sat_served["wall_s"] * 1e3 / count,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f16",
-        "data": "synthetic (seeded)",
-        "config": {"workload": SERVE_WORKLOADS["cfg5"], "layers": [list(l) for l in layers], "requests": count,
-                   "total_gflop": flops / 1e9, "plain_capacity_req_per_s": capacity},
+    out = {
+        "workload": SERVE_WORKLOADS["cfg5"], "layers": [list(l) for l in layers], "requests": count,
+        "total_gflop": flops / 1e9, "plain_capacity_req_per_s": capacity,
+        "plain_path": "per-request kernels queued on one stream at arrival (server per_request mode)",
         "saturated": {"served": sat_served, "plain": sat_plain,
                       "served_over_plain": sat_served["tflops"] / sat_plain["tflops"]},
-        "sweep": sweep, "server_stats": st, "clocks": clocks, "roofline": None, "cpu_baseline": None,
-        "e2e": None, "gpu_launches": None,
+        "sweep": sweep, "server_stats": st,
+    }
+    del bufs
+    return out, clocks
+
+
+def serve_arm(args):
+    """Serving workload as its own line (value = the saturated served run)."""
+    import torch
+    rank, world, local = env_dist()
+    torch.cuda.set_device(local)
+    device = torch.device("cuda", local)
+    wg = load_pkg()
+    wg.lib()
+    res, clocks = serving_run(wg, torch, device, args.requests, args.rates, with_clocks=True)
+    sat = res["saturated"]["served"]
+    line = {
+        "metric": METRIC, "value": world * sat["tflops"], "unit": "TFLOP/s", "n_gpus": world,
+        "steps": args.requests, "warmup": args.requests, "ms_per_step": sat["wall_s"] * 1e3 / args.requests,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f16",
+        "data": "synthetic (seeded)",
+        "config": {"workload": res["workload"], "layers": res["layers"], "requests": args.requests,
+                   "total_gflop": res["total_gflop"], "plain_capacity_req_per_s": res["plain_capacity_req_per_s"]},
+        "saturated": res["saturated"], "sweep": res["sweep"], "server_stats": res["server_stats"],
+        "clocks": clocks, "roofline": None, "cpu_baseline": None, "e2e": None, "gpu_launches": None,
     }
     if rank == 0:
         print(json.dumps(line), flush=True)
@@ -893,8 +1055,12 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--precision", action="store_true", help="F(4x3) precision study instead of timing")
     ap.add_argument("--suite", action="store_true", help="contest shapes through the drop-in API, with cuDNN")
-    ap.add_argument("--cudnn", action="store_true", help="also time cuDNN (torch conv2d) on the workload")
+    ap.add_argument("--no-cudnn", action="store_true", help="skip the cuDNN (torch conv2d) comparison")
+    ap.add_argument("--no-serving", action="store_true",
+                    help="skip the batched (24 uneven problems) and served (request trace) comparisons of the default line")
+    ap.add_argument("--line-requests", type=int, default=2000, help="requests of the default line's serving trace")
     ap.add_argument("--nhwc", action="store_true", help="channels-last input and output tensors")
+    ap.add_argument("--m-fp32", action="store_true", help="F(4x3): store the GEMM result M in fp32 instead of 24 bits")
     ap.add_argument("--images", type=int, default=4, help="images of the precision study")
     args = ap.parse_args()
     if args.warmup < 3:

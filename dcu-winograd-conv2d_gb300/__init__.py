@@ -40,7 +40,7 @@ class Options(ctypes.Structure):
     _fields_ = [("algo", ctypes.c_int), ("operand_bf16", ctypes.c_int), ("tile_scaling", ctypes.c_int),
                 ("f4_points", ctypes.c_int), ("filter_policy", ctypes.c_int), ("gemm_bn", ctypes.c_int),
                 ("l2_chunk_bytes", ctypes.c_longlong), ("io_bf16", ctypes.c_int), ("layout_nhwc", ctypes.c_int),
-                ("reserved", ctypes.c_int * 2)]
+                ("m_fp32", ctypes.c_int), ("reserved", ctypes.c_int * 1)]
 
 
 # every symbol include/conv2d.h declares
@@ -278,14 +278,14 @@ def noalloc_check_device():
 class ServerConfig(ctypes.Structure):
     """conv2d_server_config_t."""
     _fields_ = [("hbm_budget_bytes", ctypes.c_longlong), ("max_batch", ctypes.c_int), ("slots", ctypes.c_int),
-                ("algo", ctypes.c_int), ("reserved", ctypes.c_int * 4)]
+                ("algo", ctypes.c_int), ("per_request", ctypes.c_int), ("reserved", ctypes.c_int * 3)]
 
 
 class ServerStats(ctypes.Structure):
     """conv2d_server_stats_t."""
     _fields_ = [("completed", ctypes.c_longlong), ("batches", ctypes.c_int), ("mean_batch", ctypes.c_double),
                 ("max_inflight_batches", ctypes.c_int), ("arena_used_bytes", ctypes.c_longlong),
-                ("flops", ctypes.c_double)]
+                ("flops", ctypes.c_double), ("busy_us", ctypes.c_double), ("overlap_us", ctypes.c_double)]
 
 
 class Server:

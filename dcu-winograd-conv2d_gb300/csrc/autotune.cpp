@@ -37,7 +37,8 @@ std::map<Key, Choice> g_cache;
 bool g_loaded = false;
 
 Key key_of(const problem_t& pr, const conv2d_options_t& opt) {
-    return Key(pr.n, pr.c, pr.h, pr.w, pr.k, pr.p, pr.q, opt.operand_bf16 + 2 * opt.io_bf16 + 4 * opt.layout_nhwc,
+    return Key(pr.n, pr.c, pr.h, pr.w, pr.k, pr.p, pr.q,
+               opt.operand_bf16 + 2 * opt.io_bf16 + 4 * opt.layout_nhwc + 8 * opt.m_fp32,
                opt.f4_points, opt.tile_scaling);
 }
 

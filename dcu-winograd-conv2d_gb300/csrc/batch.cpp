@@ -41,7 +41,7 @@ struct Batch {
     };
     struct GemmGroup {
         int bn;
-        bool m_fp32;
+        MType mt;
         OpType op;
         const GemmDesc* descs;
         int n;
@@ -50,7 +50,7 @@ struct Batch {
     };
     struct OutGroup {
         Xform xf;
-        bool m_fp32;
+        MType mt;
         const OutDesc* descs;
         int n;
         long long blocks;
@@ -78,10 +78,10 @@ struct Batch {
             if ((e = launch_input_transform_grouped(g.xf, g.op, g.descs, g.n, g.blocks, g.smem, g.scaled, err, s)) != cudaSuccess)
                 return e;
         for (const GemmGroup& g : gemm_groups)
-            if ((e = launch_gemm_grouped(g.descs, g.n, g.tiles, g.op, g.m_fp32, g.bn, g.grid, err, s)) != cudaSuccess)
+            if ((e = launch_gemm_grouped(g.descs, g.n, g.tiles, g.op, g.mt, g.bn, g.grid, err, s)) != cudaSuccess)
                 return e;
         for (const OutGroup& g : out_groups)
-            if ((e = launch_output_transform_grouped(g.xf, g.m_fp32, g.descs, g.n, g.blocks, err, s)) != cudaSuccess) return e;
+            if ((e = launch_output_transform_grouped(g.xf, g.mt, g.descs, g.n, g.blocks, err, s)) != cudaSuccess) return e;
         for (int i : fused) {
             Plan& p = *plans[i];
             const void* x_end =
@@ -124,8 +124,8 @@ int batch_create(const problem_t* problems, int count, const conv2d_options_t* o
         b->plans.push_back(std::move(p));
     }
     // group the problems and lay out their descriptors
-    std::map<std::pair<int, int>, std::vector<int>> in_keys, out_keys;        // (xform, op|mfp32) -> problems
-    std::map<std::tuple<int, int, int>, std::vector<int>> gemm_keys;          // (bn, m_fp32, op) -> problems
+    std::map<std::pair<int, int>, std::vector<int>> in_keys, out_keys;        // (xform, op | M type) -> problems
+    std::map<std::tuple<int, int, int>, std::vector<int>> gemm_keys;          // (bn, M type, op) -> problems
     for (int i = 0; i < count; ++i) {
         Plan& p = *b->plans[i];
         if (p.single_kernel()) {
@@ -134,8 +134,8 @@ int batch_create(const problem_t* problems, int count, const conv2d_options_t* o
         }
         if (p.scaling) b->scaled.push_back(i);
         in_keys[{static_cast<int>(p.xf), static_cast<int>(p.op)}].push_back(i);
-        out_keys[{static_cast<int>(p.xf), p.m_fp32 ? 1 : 0}].push_back(i);
-        gemm_keys[{p.gemm_full.bn, p.m_fp32 ? 1 : 0, static_cast<int>(p.op)}].push_back(i);
+        out_keys[{static_cast<int>(p.xf), static_cast<int>(p.mt)}].push_back(i);
+        gemm_keys[{p.gemm_full.bn, static_cast<int>(p.mt), static_cast<int>(p.op)}].push_back(i);
     }
     std::vector<InDesc> in_descs;
     std::vector<OutDesc> out_descs;
@@ -168,7 +168,7 @@ int batch_create(const problem_t* problems, int count, const conv2d_options_t* o
         Range r{out_descs.size(), kv.second.size(), 0, 0, false};
         for (int i : kv.second) {
             Plan& p = *b->plans[i];
-            OutDesc d = make_out_desc(p.g, p.m_fp32, p.Mw, p.prob.out, p.scale);
+            OutDesc d = make_out_desc(p.g, p.mt, p.Mw, p.prob.out, p.scale);
             d.blk_begin = r.total;
             r.total += d.gx * d.gy;
             out_descs.push_back(d);
@@ -205,13 +205,13 @@ int batch_create(const problem_t* problems, int count, const conv2d_options_t* o
                                 reinterpret_cast<const InDesc*>(base + oI) + kr.second.first,
                                 static_cast<int>(kr.second.n), kr.second.total, kr.second.extra, kr.second.scaled});
     for (auto& kr : gemm_r)
-        b->gemm_groups.push_back({std::get<0>(kr.first), std::get<1>(kr.first) != 0,
+        b->gemm_groups.push_back({std::get<0>(kr.first), static_cast<MType>(std::get<1>(kr.first)),
                                   static_cast<OpType>(std::get<2>(kr.first)),
                                   reinterpret_cast<const GemmDesc*>(base + oG) + kr.second.first,
                                   static_cast<int>(kr.second.n), kr.second.total,
                                   static_cast<int>(std::min<long long>(kr.second.total, sms))});
     for (auto& kr : out_r)
-        b->out_groups.push_back({static_cast<Xform>(kr.first.first), kr.first.second != 0,
+        b->out_groups.push_back({static_cast<Xform>(kr.first.first), static_cast<MType>(kr.first.second),
                                  reinterpret_cast<const OutDesc*>(base + oO) + kr.second.first,
                                  static_cast<int>(kr.second.n), kr.second.total});
     int single = 0;   // launches of the problems run by their own kernels

@@ -99,7 +99,11 @@ int validate_problem(const problem_t* pr) {
 
 int options_default(conv2d_options_t* o) {
     std::memset(o, 0, sizeof(*o));
-    o->algo = env_algo(CONV2D_ALGO_REFERENCE);
+    // the per-shape autotuner by default: among the reference's three
+    // algorithms (and the row F(4x3) kernel) the fastest measured for the
+    // shape, the reference rule's pick unless another is >3% faster;
+    // WG_CONV2D_ALGO=ref keeps the reference rule itself
+    o->algo = env_algo(CONV2D_ALGO_AUTO);
     o->operand_bf16 = env_int("WG_CONV2D_BF16", 0) ? 1 : 0;
     o->tile_scaling = env_int("WG_CONV2D_TILE_SCALING", 0) ? 1 : 0;
     o->f4_points = env_int("WG_CONV2D_F4_REFERENCE_POINTS", 0) ? 1 : 0;
@@ -109,6 +113,7 @@ int options_default(conv2d_options_t* o) {
     o->l2_chunk_bytes = (l2 && *l2) ? std::atoll(l2) : 0;
     o->io_bf16 = env_int("WG_CONV2D_IO_BF16", 0) ? 1 : 0;
     o->layout_nhwc = env_int("WG_CONV2D_NHWC", 0) ? 1 : 0;
+    o->m_fp32 = env_int("WG_CONV2D_M_FP32", 0) ? 1 : 0;
     return CONV2D_OK;
 }
 
@@ -202,7 +207,16 @@ int Plan::build(const problem_t* pr, const conv2d_options_t* opt_in) {
     // range), fp16 operands with per-tile scaling for F(4x3) (bf16 operands
     // lose ~10x accuracy there); M in fp32 either way
     if (opt.io_bf16) op = m == 2 ? OpType::BF16 : OpType::F16;
-    m_fp32 = ((m == 4) || opt.io_bf16) && algo != CONV2D_ALGO_4X3_ROW;
+    // M: 24-bit for F(4x3) with fp16 operands (fp16 M would add ~1e-2
+    // through A^T m A), fp32 where asked, for bf16 operands, for channels-last
+    // output (row-major M) and for F(2x3) with bf16 tensors, fp16 for F(2x3)
+    // otherwise
+    if (algo == CONV2D_ALGO_4X3_ROW)
+        mt = MType::F16;   // no M
+    else if (m == 4)
+        mt = (nhwc || opt.m_fp32 || op == OpType::BF16) ? MType::F32 : MType::F24;
+    else
+        mt = opt.io_bf16 ? MType::F32 : MType::F16;
     scaling = (m == 4) && (opt.tile_scaling || opt.io_bf16) && algo != CONV2D_ALGO_4X3_ROW;
     g = make_geom(pr->n, pr->c, pr->h, pr->w, pr->k, pr->p, pr->q, m);
     const int E = g.alpha * g.alpha;
@@ -217,8 +231,8 @@ int Plan::build(const problem_t* pr, const conv2d_options_t* opt_in) {
     // image chunking keeps V and M of one chunk L2-resident between kernels
     chunk_n = static_cast<int>(pr->n);
     if (!single_kernel() && opt.l2_chunk_bytes > 0) {
-        const long long per_img = static_cast<long long>(E) * g.tiles_h * g.tiles_w *
-                                  (g.cp * op_bytes + g.kp * (m_fp32 ? 4LL : 2LL));
+        const long long tiles_img = static_cast<long long>(g.tiles_h) * g.tiles_w;
+        const long long per_img = static_cast<long long>(E) * tiles_img * g.cp * op_bytes + m_bytes(mt, E, tiles_img, g.kp);
         chunk_n = static_cast<int>(std::max(1LL, std::min<long long>(pr->n, opt.l2_chunk_bytes / std::max(1LL, per_img))));
     }
     const long long Pc = static_cast<long long>(chunk_n) * g.tiles_h * g.tiles_w;
@@ -230,7 +244,7 @@ int Plan::build(const problem_t* pr, const conv2d_options_t* opt_in) {
     long long bV = 0, bM = 0, bS = 0;
     if (!single_kernel()) {
         bV = al(static_cast<long long>(E) * round_rows(Pc) * g.cp * op_bytes);
-        bM = al(static_cast<long long>(E) * Pc * g.kp * (m_fp32 ? 4 : 2));
+        bM = al(m_bytes(mt, E, Pc, g.kp));
         if (scaling) bS = al(Pc * 4);
     }
     const long long bE = 256;
@@ -281,14 +295,14 @@ int Plan::build(const problem_t* pr, const conv2d_options_t* opt_in) {
             if (ce != cudaSuccess) return cuda_fail(ce, "NHWC tensor map");
         }
         const int bn = opt.gemm_bn ? opt.gemm_bn : default_bn(g.k);
-        ce = plan_gemm(gemm_full, op, E, Pc, g.k, g.kp, g.cp, V, U, Mw, m_fp32, bn, num_sms, nhwc);
+        ce = plan_gemm(gemm_full, op, E, Pc, g.k, g.kp, g.cp, V, U, Mw, mt, bn, num_sms, nhwc);
         if (ce != cudaSuccess) return cuda_fail(ce, "GEMM plan (tensor maps)");
         n_chunks = (static_cast<int>(pr->n) + chunk_n - 1) / chunk_n;
         const int tail_n = static_cast<int>(pr->n) - (n_chunks - 1) * chunk_n;
         has_tail = tail_n != chunk_n;
         if (has_tail) {
             const long long Pt = static_cast<long long>(tail_n) * g.tiles_h * g.tiles_w;
-            ce = plan_gemm(gemm_tail, op, E, Pt, g.k, g.kp, g.cp, V, U, Mw, m_fp32, bn, num_sms, nhwc);
+            ce = plan_gemm(gemm_tail, op, E, Pt, g.k, g.kp, g.cp, V, U, Mw, mt, bn, num_sms, nhwc);
             if (ce != cudaSuccess) return cuda_fail(ce, "GEMM plan (tail)");
         }
         launches = n_chunks * (3 + (scaling ? 1 : 0));
@@ -342,7 +356,7 @@ int Plan::run_range(int n0, int nc, const GemmPlan* gp, cudaStream_t s) {
         ce = launch_gemm(*gp, err, s);
         if (ce != cudaSuccess) return cuda_fail(ce, "GEMM launch");
         mark(s);
-        ce = launch_nhwc_output_transform(xf, m_fp32, make_nhwc_out_desc(gc, Mw, yout), s);
+        ce = launch_nhwc_output_transform(xf, mt, make_nhwc_out_desc(gc, Mw, yout), s);
         if (ce != cudaSuccess) return cuda_fail(ce, "NHWC output transform launch");
         mark(s);
         return CONV2D_OK;
@@ -358,7 +372,7 @@ int Plan::run_range(int n0, int nc, const GemmPlan* gp, cudaStream_t s) {
     ce = launch_gemm(*gp, err, s);
     if (ce != cudaSuccess) return cuda_fail(ce, "GEMM launch");
     mark(s);
-    ce = launch_output_transform(xf, m_fp32, gc, Mw, yout, scale, err, s, opt.io_bf16 != 0);
+    ce = launch_output_transform(xf, mt, gc, Mw, yout, scale, err, s, opt.io_bf16 != 0);
     if (ce != cudaSuccess) return cuda_fail(ce, "output transform launch");
     mark(s);
     return CONV2D_OK;
@@ -443,7 +457,7 @@ const GemmPlan* Plan::host_gemm_for(int nc) {
     if (n_host_plans == kMaxHostPlans) return nullptr;
     const int E = g.alpha * g.alpha;
     GemmPlan& gp = host_gemm[n_host_plans];
-    if (plan_gemm(gp, op, E, static_cast<long long>(nc) * g.tiles_h * g.tiles_w, g.k, g.kp, g.cp, V, U, Mw, m_fp32,
+    if (plan_gemm(gp, op, E, static_cast<long long>(nc) * g.tiles_h * g.tiles_w, g.k, g.kp, g.cp, V, U, Mw, mt,
                   gemm_full.bn, num_sms, nhwc) != cudaSuccess)
         return nullptr;
     host_plan_n[n_host_plans++] = nc;

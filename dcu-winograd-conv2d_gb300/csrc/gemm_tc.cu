@@ -28,6 +28,7 @@
 
 #include <algorithm>
 #include <cstdlib>
+#include <type_traits>
 
 #include "wg_kernels.h"
 #include "wg_launch.h"
@@ -87,6 +88,36 @@ __device__ __forceinline__ void store32<float>(float* Mw, const uint32_t (&r)[32
         if (g0 + j < kg_count)
             st_hint_v4(Mw + ((static_cast<long long>(e) * kg_count + g0 + j) * P + p) * 4,
                        make_uint4(r[4 * j], r[4 * j + 1], r[4 * j + 2], r[4 * j + 3]), pol);
+}
+
+// 24-bit M: tag type of the split-plane storage (upper 16 bits of each
+// rounded fp32 value in H[e][Kp/8][P][8], next 8 bits in L[e][Kp/8][Pp][8]).
+struct M24 {};
+
+// 24-bit M: 32 accumulator columns (four granules of 8 channels) of tile row
+// p.  Each fp32 value is rounded to nearest at bit 8 (ties away from zero;
+// a carry into the exponent is the correct rounding, and the largest finite
+// values round to infinity as at any precision); bytes 2-3 go to the high
+// plane (one 16-byte store per granule), byte 1 to the low plane (one 8-byte
+// store per granule).
+__device__ __forceinline__ void store32_m24(unsigned char* Mb, const uint32_t (&r)[32], long long P, long long p,
+                                            int k0, int kg_count, int e, long long m_lo, long long m_pp, uint64_t pol) {
+    const int g0 = k0 / 8;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        if (g0 + j >= kg_count) break;
+        uint32_t v[8];
+#pragma unroll
+        for (int i = 0; i < 8; ++i) v[i] = r[8 * j + i] + 0x80u;
+        const uint4 hi = make_uint4(__byte_perm(v[0], v[1], 0x7632), __byte_perm(v[2], v[3], 0x7632),
+                                    __byte_perm(v[4], v[5], 0x7632), __byte_perm(v[6], v[7], 0x7632));
+        const uint32_t l01 = __byte_perm(v[0], v[1], 0x5151), l23 = __byte_perm(v[2], v[3], 0x5151);
+        const uint32_t l45 = __byte_perm(v[4], v[5], 0x5151), l67 = __byte_perm(v[6], v[7], 0x5151);
+        const uint2 lo = make_uint2(__byte_perm(l01, l23, 0x5410), __byte_perm(l45, l67, 0x5410));
+        const long long gi = static_cast<long long>(e) * kg_count + g0 + j;
+        st_hint_v4(Mb + (gi * P + p) * 16, hi, pol);
+        st_hint_v2(Mb + m_lo + (gi * m_pp + p) * 8, lo, pol);
+    }
 }
 
 // Row-major M[e][P][Kp] (the NHWC output path): 4 consecutive columns of
@@ -265,6 +296,7 @@ __device__ __forceinline__ void gemm_body(const GemmDesc* __restrict__ descs, in
             const long long P = d.P;
             const int kg_count = d.kg_count;
             const int m_row = d.m_row, kp = d.kp;
+            const long long m_lo = d.m_lo, m_pp = d.m_pp;
             if (!mbar_wait(&tfull[acc], acc_phase, abort_flag, err, ERR_SITE_TMEM_FULL)) break;
             tc_fence_after();
             const long long p = static_cast<long long>(it.mb) * kBM + row;
@@ -280,7 +312,7 @@ __device__ __forceinline__ void gemm_body(const GemmDesc* __restrict__ descs, in
 #pragma unroll
             for (int ch = 0; ch < kChunks; ++ch) {
                 if (ch + 1 < kChunks) tmem_ld_x32(taddr + (ch + 1) * 32, r[(ch + 1) & 1]);
-                if (m_row) {
+                if (!std::is_same<MT, M24>::value && m_row) {
                     // row-major M: transpose the warp's 32 rows x 32 columns
                     // through shared memory (XOR-swizzled, conflict-free) so
                     // that 8 lanes write one row's 128 contiguous bytes
@@ -297,11 +329,16 @@ __device__ __forceinline__ void gemm_body(const GemmDesc* __restrict__ descs, in
 #pragma unroll
                         for (int j = 0; j < 4; ++j) v[j] = xp[row_w * 32 + ((c0 + j) ^ row_w)];
                         const long long pr = static_cast<long long>(it.mb) * kBM + quarter * 32 + row_w;
-                        if (pr < P && k0 < kp) store4_row<MT>(Mw, v, P, pr, k0, kp, it.e, m_pol);
+                        if constexpr (!std::is_same<MT, M24>::value)
+                            if (pr < P && k0 < kp) store4_row<MT>(Mw, v, P, pr, k0, kp, it.e, m_pol);
                     }
                     __syncwarp();
                 } else if (p < P) {
-                    store32<MT>(Mw, r[ch & 1], P, p, it.nb * BN + col0 + ch * 32, kg_count, it.e, m_pol);
+                    if constexpr (std::is_same<MT, M24>::value)
+                        store32_m24(static_cast<unsigned char*>(d.Mw), r[ch & 1], P, p, it.nb * BN + col0 + ch * 32,
+                                    kg_count, it.e, m_lo, m_pp, m_pol);
+                    else
+                        store32<MT>(Mw, r[ch & 1], P, p, it.nb * BN + col0 + ch * 32, kg_count, it.e, m_pol);
                 }
                 if (ch + 1 < kChunks) tc_wait_ld(r[(ch + 1) & 1]);
             }
@@ -372,28 +409,36 @@ cudaError_t gemm_grouped_launch(const GemmDesc* descs, int ndesc, long long tota
 
 // One template instance per (BN, operand type, M type); `single` selects the
 // one-problem kernel (descriptor by value) or the grouped one (device array).
-template <int BN>
-cudaError_t dispatch_types(bool bf, bool m_fp32, bool single, const GemmDesc* d, int ndesc, long long total, int grid,
-                           DevErr* err, cudaStream_t s) {
-    if (single) {
-        if (m_fp32)
-            return bf ? gemm_launch<BN, true, float>(*d, grid, err, s) : gemm_launch<BN, false, float>(*d, grid, err, s);
-        return bf ? gemm_launch<BN, true, __half>(*d, grid, err, s) : gemm_launch<BN, false, __half>(*d, grid, err, s);
-    }
-    if (m_fp32)
-        return bf ? gemm_grouped_launch<BN, true, float>(d, ndesc, total, grid, err, s)
-                  : gemm_grouped_launch<BN, false, float>(d, ndesc, total, grid, err, s);
-    return bf ? gemm_grouped_launch<BN, true, __half>(d, ndesc, total, grid, err, s)
-              : gemm_grouped_launch<BN, false, __half>(d, ndesc, total, grid, err, s);
+// 24-bit M is written by fp16-operand GEMMs only (F(4x3) with fp16 tensors).
+template <int BN, class MT>
+cudaError_t dispatch_single_or_grouped(bool bf, bool single, const GemmDesc* d, int ndesc, long long total, int grid,
+                                       DevErr* err, cudaStream_t s) {
+    if (single) return bf ? gemm_launch<BN, true, MT>(*d, grid, err, s) : gemm_launch<BN, false, MT>(*d, grid, err, s);
+    return bf ? gemm_grouped_launch<BN, true, MT>(d, ndesc, total, grid, err, s)
+              : gemm_grouped_launch<BN, false, MT>(d, ndesc, total, grid, err, s);
 }
 
-cudaError_t dispatch(int bn, bool bf, bool m_fp32, bool single, const GemmDesc* d, int ndesc, long long total, int grid,
+template <int BN>
+cudaError_t dispatch_types(bool bf, MType mt, bool single, const GemmDesc* d, int ndesc, long long total, int grid,
+                           DevErr* err, cudaStream_t s) {
+    switch (mt) {
+        case MType::F32: return dispatch_single_or_grouped<BN, float>(bf, single, d, ndesc, total, grid, err, s);
+        case MType::F16: return dispatch_single_or_grouped<BN, __half>(bf, single, d, ndesc, total, grid, err, s);
+        case MType::F24:
+            if (bf) return cudaErrorNotSupported;
+            return single ? gemm_launch<BN, false, M24>(*d, grid, err, s)
+                          : gemm_grouped_launch<BN, false, M24>(d, ndesc, total, grid, err, s);
+    }
+    return cudaErrorInvalidValue;
+}
+
+cudaError_t dispatch(int bn, bool bf, MType mt, bool single, const GemmDesc* d, int ndesc, long long total, int grid,
                      DevErr* err, cudaStream_t s) {
     switch (bn) {
-        case 32: return dispatch_types<32>(bf, m_fp32, single, d, ndesc, total, grid, err, s);
-        case 64: return dispatch_types<64>(bf, m_fp32, single, d, ndesc, total, grid, err, s);
-        case 128: return dispatch_types<128>(bf, m_fp32, single, d, ndesc, total, grid, err, s);
-        case 256: return dispatch_types<256>(bf, m_fp32, single, d, ndesc, total, grid, err, s);
+        case 32: return dispatch_types<32>(bf, mt, single, d, ndesc, total, grid, err, s);
+        case 64: return dispatch_types<64>(bf, mt, single, d, ndesc, total, grid, err, s);
+        case 128: return dispatch_types<128>(bf, mt, single, d, ndesc, total, grid, err, s);
+        case 256: return dispatch_types<256>(bf, mt, single, d, ndesc, total, grid, err, s);
     }
     return cudaErrorInvalidValue;
 }
@@ -427,12 +472,15 @@ int gemm_smem_bytes(int bn) {
 }
 
 cudaError_t make_gemm_desc(GemmDesc& d, OpType op, int E, long long P, int K, int Kp, int Cp, const void* V,
-                           const void* U, void* Mw, bool m_fp32, int bn, bool m_row) {
+                           const void* U, void* Mw, MType mt, int bn, bool m_row) {
     if (bn != 32 && bn != 64 && bn != 128 && bn != 256) return cudaErrorInvalidValue;
     if (P <= 0 || P > 0x7fffffffLL || Cp % 8 != 0 || Kp % 8 != 0) return cudaErrorInvalidValue;
+    if (mt == MType::F24 && (m_row || op != OpType::F16)) return cudaErrorNotSupported;
     d.Mw = Mw;
     d.P = static_cast<int>(P);
-    d.kg_count = m_fp32 ? Kp / 4 : Kp / 8;
+    d.kg_count = mt == MType::F32 ? Kp / 4 : Kp / 8;
+    d.m_lo = m24_lo_offset(E, P, Kp);
+    d.m_pp = static_cast<int>(round_rows(P));
     d.m_row = m_row ? 1 : 0;
     d.kp = Kp;
     d.keep_m = 0;   // plan_gemm decides for single launches; grouped ones stream M
@@ -474,31 +522,31 @@ cudaError_t make_gemm_desc(GemmDesc& d, OpType op, int E, long long P, int K, in
 }
 
 cudaError_t plan_gemm(GemmPlan& gp, OpType op, int E, long long P, int K, int Kp, int Cp, const void* V,
-                      const void* U, void* Mw, bool m_fp32, int bn, int num_sms, bool m_row) {
-    cudaError_t e = make_gemm_desc(gp.desc, op, E, P, K, Kp, Cp, V, U, Mw, m_fp32, bn, m_row);
+                      const void* U, void* Mw, MType mt, int bn, int num_sms, bool m_row) {
+    cudaError_t e = make_gemm_desc(gp.desc, op, E, P, K, Kp, Cp, V, U, Mw, mt, bn, m_row);
     if (e != cudaSuccess) return e;
     // M of this launch within the L2 size: kept there for the output transform
-    // that reads it next (cfg3 F(4x3): 116 MB); larger M is streamed out
-    gp.desc.keep_m = static_cast<long long>(E) * P * Kp * (m_fp32 ? 4 : 2) <= l2_cache_bytes();
+    // that reads it next (cfg3 F(4x3): 116 MB in fp32); larger M is streamed out
+    gp.desc.keep_m = m_bytes(mt, E, P, Kp) <= l2_cache_bytes();
     // V has one reader per tile when one block covers all output channels;
     // WG_CONV2D_KEEP_WORKSPACE=1 keeps it (to read the workspace back)
     const char* keep_ws = std::getenv("WG_CONV2D_KEEP_WORKSPACE");
     gp.desc.discard_v = gp.desc.n_blocks == 1 && !(keep_ws && std::atoi(keep_ws) != 0);
     gp.op = op;
     gp.bn = bn;
-    gp.m_fp32 = m_fp32;
+    gp.mt = mt;
     gp.grid = static_cast<int>(std::min<long long>(gp.desc.tiles, num_sms));
     gp.smem_bytes = gemm_smem_bytes(bn);
     return cudaSuccess;
 }
 
 cudaError_t launch_gemm(const GemmPlan& gp, DevErr* err, cudaStream_t stream) {
-    return dispatch(gp.bn, gp.op == OpType::BF16, gp.m_fp32, true, &gp.desc, 1, gp.desc.tiles, gp.grid, err, stream);
+    return dispatch(gp.bn, gp.op == OpType::BF16, gp.mt, true, &gp.desc, 1, gp.desc.tiles, gp.grid, err, stream);
 }
 
-cudaError_t launch_gemm_grouped(const GemmDesc* descs, int ndesc, long long total_tiles, OpType op, bool m_fp32, int bn,
+cudaError_t launch_gemm_grouped(const GemmDesc* descs, int ndesc, long long total_tiles, OpType op, MType mt, int bn,
                                 int grid, DevErr* err, cudaStream_t stream) {
-    return dispatch(bn, op == OpType::BF16, m_fp32, false, descs, ndesc, total_tiles, grid, err, stream);
+    return dispatch(bn, op == OpType::BF16, mt, false, descs, ndesc, total_tiles, grid, err, stream);
 }
 
 }  // namespace wg

@@ -359,7 +359,9 @@ NhwcOutDesc make_nhwc_out_desc(const Geom& g, const void* Mw, void* out) {
     return d;
 }
 
-cudaError_t launch_nhwc_output_transform(Xform xf, bool m_fp32, const NhwcOutDesc& dd, cudaStream_t s) {
+cudaError_t launch_nhwc_output_transform(Xform xf, MType mt, const NhwcOutDesc& dd, cudaStream_t s) {
+    if (mt == MType::F24) return cudaErrorNotSupported;   // row-major M is fp16 or fp32
+    const bool m_fp32 = mt == MType::F32;
     const long long blocks = (dd.P + dd.tpc - 1) / dd.tpc;
     if (blocks <= 0) return cudaSuccess;
     if (blocks > 0x7fffffffLL) return cudaErrorInvalidValue;

@@ -115,7 +115,7 @@ extern "C" int conv2d_fp16_noalloc(const problem_t* problem, void* stream) {
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
     GemmPlan gp;
-    if (plan_gemm(gp, OpType::F16, 16, g.P, g.k, g.kp, g.cp, V, U, Mw, false, default_bn(g.k), sms > 0 ? sms : 1) !=
+    if (plan_gemm(gp, OpType::F16, 16, g.P, g.k, g.kp, g.cp, V, U, Mw, MType::F16, default_bn(g.k), sms > 0 ? sms : 1) !=
         cudaSuccess)
         return noalloc_fail(CONV2D_ERR_CUDA, "tensor map encoding failed");
     // the error word starts every call at zero; U, V and M are rewritten in
@@ -126,7 +126,7 @@ extern "C" int conv2d_fp16_noalloc(const problem_t* problem, void* stream) {
     if (launch_filter_transform(Xform::F2, OpType::F16, problem->weight, U, g.k, g.c, g.cp, s) != cudaSuccess ||
         launch_input_transform(Xform::F2, OpType::F16, g, problem->in, x_end, V, nullptr, err, s) != cudaSuccess ||
         launch_gemm(gp, err, s) != cudaSuccess ||
-        launch_output_transform(Xform::F2, false, g, Mw, problem->out, nullptr, err, s) != cudaSuccess)
+        launch_output_transform(Xform::F2, MType::F16, g, Mw, problem->out, nullptr, err, s) != cudaSuccess)
         return noalloc_fail(CONV2D_ERR_CUDA, "kernel launch failed");
     return CONV2D_OK;
 }

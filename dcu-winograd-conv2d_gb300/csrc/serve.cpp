@@ -17,6 +17,15 @@
 // up, and their batch runs concurrently with the ones still in flight.
 // A request's arithmetic does not depend on what else is in its batch, so its
 // result is bit-identical alone and in the mix.
+//
+// With `per_request` set the server is instead the plain per-call path the
+// batching is measured against: every request's own kernels (the single-
+// problem launches conv2d_fp16_ex makes: input transform, GEMM, output
+// transform) are queued on one stream as the request is submitted, in
+// arrival order, with no batching and no wait for earlier requests; since
+// they run in stream order they share one workspace region.  Completion is
+// observed the same way in both modes (an event per request or batch, polled
+// by the scheduler thread).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -115,6 +124,7 @@ struct Request {
 
 struct Slot {
     cudaStream_t stream = nullptr;
+    cudaEvent_t start = nullptr;   // timing events: the batch's device interval
     cudaEvent_t done = nullptr;
     void* desc_dev = nullptr;
     void* desc_host = nullptr;   // pinned staging
@@ -147,14 +157,33 @@ struct Server {
     long long completed = 0;
     double flops_done = 0;
     int batches = 0, batch_requests = 0, max_inflight = 0;
+    // device intervals [start, done] of completed batches (ms from t0_ev)
+    cudaEvent_t t0_ev = nullptr;
+    std::vector<std::pair<float, float>> intervals;
+    // plain per-request mode: one stream, requests in flight in stream order
+    cudaStream_t plain_stream = nullptr;
+    struct Inflight {
+        long long id;
+        cudaEvent_t ev;
+    };
+    std::deque<Inflight> plain_inflight;
+    std::vector<cudaEvent_t> event_pool;
 
     ~Server() {
         stop = true;
         cv.notify_all();
         if (sched.joinable()) sched.join();
+        if (plain_stream) {
+            cudaStreamSynchronize(plain_stream);
+            cudaStreamDestroy(plain_stream);
+        }
+        for (Inflight& f : plain_inflight) cudaEventDestroy(f.ev);
+        for (cudaEvent_t e : event_pool) cudaEventDestroy(e);
+        if (t0_ev) cudaEventDestroy(t0_ev);
         for (Slot& s : slots) {
             if (s.stream) cudaStreamSynchronize(s.stream);
             if (s.stream) cudaStreamDestroy(s.stream);
+            if (s.start) cudaEventDestroy(s.start);
             if (s.done) cudaEventDestroy(s.done);
             if (s.desc_dev) cudaFree(s.desc_dev);
             if (s.desc_host) cudaFreeHost(s.desc_host);
@@ -164,10 +193,13 @@ struct Server {
         if (err) cudaFree(err);
     }
 
+    // M storage: 24-bit for F(4x3), fp16 for F(2x3) (as a plan of the shape has it)
+    static MType mtype_for(int m) { return m == 4 ? MType::F24 : MType::F16; }
+
     static size_t ws_bytes_for(const Geom& g) {
         const long long E = g.alpha * g.alpha;
         const size_t v = static_cast<size_t>(E * round_rows(g.P) * g.cp * 2);
-        const size_t m = static_cast<size_t>(E * g.P * g.kp * (g.m == 4 ? 4 : 2));
+        const size_t m = static_cast<size_t>(m_bytes(mtype_for(g.m), E, g.P, g.kp));
         return (v + 255) / 256 * 256 + (m + 255) / 256 * 256;
     }
 
@@ -197,10 +229,10 @@ struct Server {
             const void* x_end = static_cast<const uint16_t*>(r.in) + static_cast<long long>(r.n) * L.c * L.h * L.w;
             int smem = 0;
             InDesc di = make_in_desc(g, r.in, x_end, V, nullptr, &smem);
-            OutDesc dout = make_out_desc(g, r.m == 4, Mw, r.out, nullptr);
+            OutDesc dout = make_out_desc(g, mtype_for(r.m), Mw, r.out, nullptr);
             GemmDesc dg;
             const int bn = default_bn(static_cast<int>(L.k));
-            if (make_gemm_desc(dg, OpType::F16, E, g.P, L.k, g.kp, g.cp, V, r.m == 4 ? L.U4 : L.U2, Mw, r.m == 4, bn) !=
+            if (make_gemm_desc(dg, OpType::F16, E, g.P, L.k, g.kp, g.cp, V, r.m == 4 ? L.U4 : L.U2, Mw, mtype_for(r.m), bn) !=
                 cudaSuccess)
                 return set_last_error(CONV2D_ERR_CUDA, "tensor map encoding failed");
             if (r.m == 2) {
@@ -256,6 +288,7 @@ struct Server {
         off += out4.size() * sizeof(OutDesc);
         cudaStream_t s = slot.stream;
         char* d = static_cast<char*>(slot.desc_dev);
+        cudaEventRecord(slot.start, s);
         if (cudaMemcpyAsync(d, h, off, cudaMemcpyHostToDevice, s) != cudaSuccess)
             return set_last_error(CONV2D_ERR_CUDA, "descriptor copy failed");
         cudaError_t e = cudaSuccess;
@@ -267,18 +300,68 @@ struct Server {
                                                static_cast<int>(in4.size()), blk_in4, smem4, false, err, s);
         for (const GG& g : gg)
             if (e == cudaSuccess)
-                e = launch_gemm_grouped(reinterpret_cast<const GemmDesc*>(d + g.off), g.n, g.tiles, OpType::F16, g.m == 4,
+                e = launch_gemm_grouped(reinterpret_cast<const GemmDesc*>(d + g.off), g.n, g.tiles, OpType::F16, mtype_for(g.m),
                                         g.bn, static_cast<int>(std::min<long long>(g.tiles, num_sms)), err, s);
         if (!out2.empty() && e == cudaSuccess)
-            e = launch_output_transform_grouped(Xform::F2, false, reinterpret_cast<const OutDesc*>(d + o_out2),
+            e = launch_output_transform_grouped(Xform::F2, MType::F16, reinterpret_cast<const OutDesc*>(d + o_out2),
                                                 static_cast<int>(out2.size()), blk_out2, err, s);
         if (!out4.empty() && e == cudaSuccess)
-            e = launch_output_transform_grouped(Xform::F4, true, reinterpret_cast<const OutDesc*>(d + o_out4),
+            e = launch_output_transform_grouped(Xform::F4, MType::F24, reinterpret_cast<const OutDesc*>(d + o_out4),
                                                 static_cast<int>(out4.size()), blk_out4, err, s);
         if (e == cudaSuccess) e = cudaEventRecord(slot.done, s);
         if (e != cudaSuccess) return set_last_error(CONV2D_ERR_CUDA, cudaGetErrorString(e));
         return CONV2D_OK;
     }
+
+    // Plain per-request mode: the request's own single-problem launches on the
+    // plain stream (the same launches conv2d_fp16_ex makes for this shape),
+    // then an event that marks its completion.  Caller holds `mu`.
+    int launch_plain(Request& r) {
+        const Layer& L = layers[r.layer];
+        const Geom g = make_geom(r.n, L.c, L.h, L.w, L.k, L.p, L.q, r.m);
+        const int E = g.alpha * g.alpha;
+        // requests run in stream order: all of them use the arena's start
+        char* V = static_cast<char*>(arena_base);
+        char* Mw = V + (static_cast<size_t>(E) * round_rows(g.P) * g.cp * 2 + 255) / 256 * 256;
+        const Xform xf = r.m == 4 ? Xform::F4 : Xform::F2;
+        GemmPlan gp;
+        if (plan_gemm(gp, OpType::F16, E, g.P, L.k, g.kp, g.cp, V, r.m == 4 ? L.U4 : L.U2, Mw, mtype_for(r.m),
+                      default_bn(static_cast<int>(L.k)), num_sms) != cudaSuccess)
+            return set_last_error(CONV2D_ERR_CUDA, "tensor map encoding failed");
+        const void* x_end = static_cast<const uint16_t*>(r.in) + static_cast<long long>(r.n) * L.c * L.h * L.w;
+        cudaError_t e = launch_input_transform(xf, OpType::F16, g, r.in, x_end, V, nullptr, err, plain_stream);
+        if (e == cudaSuccess) e = launch_gemm(gp, err, plain_stream);
+        if (e == cudaSuccess) e = launch_output_transform(xf, mtype_for(r.m), g, Mw, r.out, nullptr, err, plain_stream);
+        cudaEvent_t ev = nullptr;
+        if (e == cudaSuccess) {
+            if (event_pool.empty()) {
+                e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+            } else {
+                ev = event_pool.back();
+                event_pool.pop_back();
+            }
+        }
+        if (e == cudaSuccess) e = cudaEventRecord(ev, plain_stream);
+        if (e != cudaSuccess) {
+            if (ev) event_pool.push_back(ev);
+            return set_last_error(CONV2D_ERR_CUDA, cudaGetErrorString(e));
+        }
+        plain_inflight.push_back({r.id, ev});
+        ++batches;
+        ++batch_requests;
+        max_inflight = std::max(max_inflight, static_cast<int>(plain_inflight.size()));
+        return CONV2D_OK;
+    }
+
+    void complete(Request& r, double t) {
+        r.t_done = t;
+        r.done = true;
+        const Layer& L = layers[r.layer];
+        flops_done += 2.0 * r.n * L.k * (L.h + 2.0 * L.p - 2) * (L.w + 2.0 * L.q - 2) * L.c * 9;
+        ++completed;
+    }
+
+    bool per_request() const { return cfg.per_request != 0; }
 
     void loop() {
         cudaSetDevice(device);
@@ -286,19 +369,26 @@ struct Server {
             std::unique_lock<std::mutex> lk(mu);
             // completions
             int inflight = 0;
+            while (!plain_inflight.empty() && cudaEventQuery(plain_inflight.front().ev) == cudaSuccess) {
+                complete(reqs[plain_inflight.front().id], now_us());
+                event_pool.push_back(plain_inflight.front().ev);
+                plain_inflight.pop_front();
+                cv.notify_all();
+            }
+            inflight += static_cast<int>(plain_inflight.size());
             for (Slot& s : slots) {
                 if (!s.busy) continue;
                 if (cudaEventQuery(s.done) == cudaSuccess) {
                     const double t = now_us();
                     for (long long id : s.reqs) {
                         Request& r = reqs[id];
-                        r.t_done = t;
-                        r.done = true;
                         arena.release(r.ws_off, r.ws_bytes);
-                        const Layer& L = layers[r.layer];
-                        flops_done += 2.0 * r.n * L.k * (L.h + 2.0 * L.p - 2) * (L.w + 2.0 * L.q - 2) * L.c * 9;
-                        ++completed;
+                        complete(r, t);
                     }
+                    float a = 0.f, b = 0.f;
+                    if (cudaEventElapsedTime(&a, t0_ev, s.start) == cudaSuccess &&
+                        cudaEventElapsedTime(&b, t0_ev, s.done) == cudaSuccess)
+                        intervals.emplace_back(a, b);
                     s.reqs.clear();
                     s.busy = false;
                     cv.notify_all();
@@ -388,11 +478,15 @@ int conv2d_server_create(const conv2d_server_config_t* cfg, conv2d_server_t** ou
     sv->arena.init(static_cast<size_t>(cfg->hbm_budget_bytes));
     if (cudaMalloc(&sv->err, 256) != cudaSuccess) return set_last_error(CONV2D_ERR_NOMEM, "allocation failed");
     cudaMemset(sv->err, 0, 256);
-    sv->slots.resize(cfg->slots);
+    if (cudaEventCreate(&sv->t0_ev) != cudaSuccess || cudaEventRecord(sv->t0_ev, nullptr) != cudaSuccess)
+        return set_last_error(CONV2D_ERR_CUDA, "event setup failed");
+    if (cfg->per_request && cudaStreamCreateWithFlags(&sv->plain_stream, cudaStreamNonBlocking) != cudaSuccess)
+        return set_last_error(CONV2D_ERR_CUDA, "stream setup failed");
+    sv->slots.resize(cfg->per_request ? 0 : cfg->slots);
     for (Slot& s : sv->slots) {
         s.desc_bytes = static_cast<size_t>(cfg->max_batch) * kDescBytesPerRequest + 4096;
         if (cudaStreamCreateWithFlags(&s.stream, cudaStreamNonBlocking) != cudaSuccess ||
-            cudaEventCreateWithFlags(&s.done, cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventCreate(&s.start) != cudaSuccess || cudaEventCreate(&s.done) != cudaSuccess ||
             cudaMalloc(&s.desc_dev, s.desc_bytes) != cudaSuccess ||
             cudaMallocHost(&s.desc_host, s.desc_bytes) != cudaSuccess)
             return set_last_error(CONV2D_ERR_NOMEM, "slot setup failed");
@@ -448,8 +542,22 @@ int conv2d_server_submit(conv2d_server_t* server, int layer, unsigned n, const v
     if (Server::ws_bytes_for(g) > sv->arena.capacity())
         return set_last_error(CONV2D_ERR_BUSY, "request workspace exceeds the server's HBM budget");
     sv->reqs[r.id] = r;
-    sv->pending.push_back(r.id);
     if (request) *request = r.id;
+    if (sv->per_request()) {
+        // plain path: the request's kernels are queued now, behind the
+        // requests submitted before it
+        DeviceGuard dg(sv->device);
+        Request& q = sv->reqs[r.id];
+        q.t_start = q.t_arrive;
+        const int st = sv->launch_plain(q);
+        if (st) {
+            sv->reqs.erase(r.id);
+            return st;
+        }
+        sv->cv.notify_all();
+        return CONV2D_OK;
+    }
+    sv->pending.push_back(r.id);
     sv->cv.notify_all();
     return CONV2D_OK;
 }
@@ -470,7 +578,7 @@ int conv2d_server_wait_all(conv2d_server_t* server) {
     if (!sv) return set_last_error(CONV2D_ERR_INVALID, "null server");
     std::unique_lock<std::mutex> lk(sv->mu);
     sv->cv.wait(lk, [sv] {
-        if (!sv->pending.empty()) return false;
+        if (!sv->pending.empty() || !sv->plain_inflight.empty()) return false;
         for (const Slot& s : sv->slots)
             if (s.busy) return false;
         return true;
@@ -513,6 +621,27 @@ int conv2d_server_stats(conv2d_server_t* server, conv2d_server_stats_t* st) {
     st->max_inflight_batches = sv->max_inflight;
     st->arena_used_bytes = static_cast<long long>(sv->arena.used());
     st->flops = sv->flops_done;
+    // sweep the completed batches' device intervals: time covered by at
+    // least one batch, and by two or more at once
+    std::vector<std::pair<float, int>> edges;
+    edges.reserve(2 * sv->intervals.size());
+    for (const auto& iv : sv->intervals) {
+        edges.emplace_back(iv.first, 1);
+        edges.emplace_back(iv.second, -1);
+    }
+    std::sort(edges.begin(), edges.end());
+    double busy = 0, overlap = 0;
+    int depth = 0;
+    for (size_t i = 0; i < edges.size(); ++i) {
+        if (i > 0) {
+            const double dt = edges[i].first - edges[i - 1].first;
+            if (depth >= 1) busy += dt;
+            if (depth >= 2) overlap += dt;
+        }
+        depth += edges[i].second;
+    }
+    st->busy_us = busy * 1e3;
+    st->overlap_us = overlap * 1e3;
     return CONV2D_OK;
 }
 

@@ -615,6 +615,157 @@ __global__ void __launch_bounds__(kOsThreads, 3)
     output_staged_body<TF, MT, YB>(&d, 1, total, err);
 }
 
+// 24-bit M (high plane H[e][KG][P][8] of 16-bit words, low plane
+// L[e][KG][Pp][8] of bytes): a work item is 64 tiles x one granule of 8
+// channels; warp 8 stages the item's E high runs (up to 1 KB) and E low runs
+// (up to 512 B) into one half of a double buffer while warps 0-7 transform the
+// previous item: thread = (tile, channel pair), so a warp reads 128
+// contiguous bytes of the high run and 64 of the low run per element and
+// rebuilds each value as high << 16 | low << 8.
+constexpr int kOs24Threads = 32 * 9;
+template <class TF> __host__ __device__ constexpr int os24_item_bytes() { return TF::ALPHA * TF::ALPHA * kOsTiles * (16 + 8); }
+template <class TF> __host__ __device__ constexpr int os24_smem_bytes() { return 128 + 2 * os24_item_bytes<TF>(); }
+
+template <class TF, bool YB>
+__device__ __forceinline__ void output_staged_body_m24(const OutDesc* descs, int ndesc, long long total, DevErr* err) {
+    using YT = typename IO<YB>::T;
+    constexpr int M = TF::M, A = TF::ALPHA, E = A * A;
+    constexpr int kItemBytes = os24_item_bytes<TF>();
+    constexpr int kLoBase = E * kOsTiles * 16;   // low runs after the E high runs
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    uint64_t* full = reinterpret_cast<uint64_t*>(smem_raw);
+    uint64_t* empty = full + 2;
+    volatile int* abort_flag = reinterpret_cast<volatile int*>(full + 4);
+    unsigned char* bufs = smem_raw + 128;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < 2; ++i) {
+            mbar_init(&full[i], 32);
+            mbar_init(&empty[i], 8);
+        }
+        *abort_flag = 0;
+        fence_barrier_init();
+    }
+    pdl_wait();     // M written, earlier readers of the output done
+    pdl_trigger();
+    __syncthreads();
+    if (warp == 8) {
+        int k = 0;
+        for (long long gitem = blockIdx.x; gitem < total; gitem += gridDim.x, ++k) {
+            const int b = k & 1;
+            if (!mbar_wait(&empty[b], ((k >> 1) & 1) ^ 1u, abort_flag, err, ERR_SITE_EMPTY)) break;
+            const OutDesc& d = out_desc_of(descs, ndesc, gitem);
+            const long long item = gitem - d.blk_begin;
+            const long long P = d.P;
+            const int KG = d.KG;
+            const unsigned char* Mb = static_cast<const unsigned char*>(d.Mw);
+            const long long p0 = (item / KG) * kOsTiles;
+            const int g = static_cast<int>(item % KG);
+            const long long nt = min(static_cast<long long>(kOsTiles), P - p0);
+            const uint32_t hbytes = static_cast<uint32_t>(nt) * 16u;
+            // the low plane's rows are padded to a multiple of 8 tiles: an
+            // even tile count keeps the copy a multiple of 16 bytes
+            const uint32_t lbytes = static_cast<uint32_t>((nt + 1) & ~1LL) * 8u;
+            uint32_t mine = 0;
+            for (int e = lane; e < E; e += 32) mine += hbytes + lbytes;
+            if (mine) fence_proxy_async_smem();  // earlier reads of this buffer before the async writes
+            mbar_arrive_expect_tx(&full[b], mine);
+            const uint64_t drop = l2_evict_first();   // M is read once
+            for (int e = lane; e < E; e += 32) {
+                const long long gi = static_cast<long long>(e) * KG + g;
+                bulk_g2s_hint(bufs + b * kItemBytes + e * (kOsTiles * 16), Mb + (gi * P + p0) * 16, hbytes, &full[b],
+                              drop);
+                bulk_g2s_hint(bufs + b * kItemBytes + kLoBase + e * (kOsTiles * 8), Mb + d.m_lo + (gi * d.m_pp + p0) * 8,
+                              lbytes, &full[b], drop);
+            }
+        }
+    } else {
+        const int t = threadIdx.x >> 2, qd = threadIdx.x & 3;
+        int k = 0;
+        for (long long gitem = blockIdx.x; gitem < total; gitem += gridDim.x, ++k) {
+            const int b = k & 1;
+            if (!mbar_wait(&full[b], (k >> 1) & 1, abort_flag, err, ERR_SITE_FULL)) break;
+            const OutDesc& d = out_desc_of(descs, ndesc, gitem);
+            const long long item = gitem - d.blk_begin;
+            const long long P = d.P;
+            const int KG = d.KG;
+            const int K = d.K, OH = d.OH, OW = d.OW, tiles_h = d.tiles_h, tiles_w = d.tiles_w;
+            YT* __restrict__ out = reinterpret_cast<YT*>(d.out);
+            const long long p = (item / KG) * kOsTiles + t;
+            const int g = static_cast<int>(item % KG);
+            if (p < P) {
+                const int tw = static_cast<int>(p % tiles_w);
+                const long long r = p / tiles_w;
+                const int th = static_cast<int>(r % tiles_h);
+                const long long n = r / tiles_h;
+                const int oh0 = th * M, ow0 = tw * M;
+                const int vr = min(M, OH - oh0), vc = min(M, OW - ow0);
+                const float inv = d.scale ? 1.f / d.scale[p] : 1.f;  // exact: scale is a power of two
+                const unsigned char* hsrc = bufs + b * kItemBytes + t * 16 + qd * 4;
+                const unsigned char* lsrc = bufs + b * kItemBytes + kLoBase + t * 8 + qd * 2;
+                float m0[E], m1[E];
+#pragma unroll
+                for (int e = 0; e < E; ++e) {
+                    const uint32_t h = *reinterpret_cast<const uint32_t*>(hsrc + e * (kOsTiles * 16));
+                    const uint32_t l = *reinterpret_cast<const uint16_t*>(lsrc + e * (kOsTiles * 8));
+                    m0[e] = __uint_as_float((h << 16) | ((l & 0xffu) << 8));
+                    m1[e] = __uint_as_float((h & 0xffff0000u) | (l & 0xff00u));
+                }
+#pragma unroll
+                for (int ch = 0; ch < 2; ++ch) {
+                    const int kc = g * 8 + qd * 2 + ch;
+                    if (kc >= K) break;
+                    float y[M * M];
+                    if (ch == 0)
+                        output_tile_transform<TF>(m0, y);
+                    else
+                        output_tile_transform<TF>(m1, y);
+                    YT* o = out + ((n * K + kc) * OH + oh0) * static_cast<long long>(OW) + ow0;
+#pragma unroll
+                    for (int i = 0; i < M; ++i)
+                        if (i < vr) store_row<M>(o + static_cast<long long>(i) * OW, &y[i * M], vc, inv);
+                }
+            }
+            if (d.discard_m) {
+                // the item's runs are in shared memory and nothing reads them
+                // again: drop the 128-byte lines that lie wholly inside them
+                const long long p0 = (item / KG) * kOsTiles;
+                const long long nt = min(static_cast<long long>(kOsTiles), P - p0);
+                const unsigned char* Mb = static_cast<const unsigned char*>(d.Mw);
+                for (int i = threadIdx.x; i < E * 12; i += 256) {
+                    const int e = i / 12, l = i % 12;
+                    const long long gi = static_cast<long long>(e) * KG + g;
+                    const bool hi = l < 8;
+                    const long long s0 = hi ? (gi * P + p0) * 16 : d.m_lo + (gi * d.m_pp + p0) * 8;
+                    const long long nbytes = hi ? nt * 16 : nt * 8;
+                    const long long first = (s0 + 127) & ~127LL, end = (s0 + nbytes) & ~127LL;
+                    const int li = hi ? l : l - 8;
+                    if (first + (li + 1) * 128LL <= end) discard_l2_line(Mb + first + li * 128LL);
+                }
+            }
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&empty[b]);
+        }
+    }
+    if (*abort_flag) {
+        const unsigned long long t0 = globaltimer_ns();
+        while (globaltimer_ns() - t0 < 2000000ull) {
+        }
+    }
+}
+
+template <class TF, bool YB>
+__global__ void __launch_bounds__(kOs24Threads, 2)
+    output_transform_staged_m24(const __grid_constant__ OutDesc d, long long total, DevErr* err) {
+    output_staged_body_m24<TF, YB>(&d, 1, total, err);
+}
+
+template <class TF>
+__global__ void __launch_bounds__(kOs24Threads, 2)
+    output_transform_staged_m24_grouped(const OutDesc* __restrict__ descs, int ndesc, long long total, DevErr* err) {
+    output_staged_body_m24<TF, false>(descs, ndesc, total, err);
+}
+
 template <class TF, class MT>
 __global__ void __launch_bounds__(kOsThreads, 3)
     output_transform_staged_grouped(const OutDesc* __restrict__ descs, int ndesc, long long total, DevErr* err) {
@@ -720,6 +871,31 @@ cudaError_t output_launch(const OutDesc& d, DevErr* err, cudaStream_t s) {
     return launch_pdl(kern, dim3(static_cast<unsigned>(grid)), dim3(kOsThreads), smem, s, d, total, err);
 }
 
+template <class TF, bool YB = false>
+cudaError_t output_launch_m24(const OutDesc& d, DevErr* err, cudaStream_t s) {
+    const long long total = (d.P + kOsTiles - 1) / kOsTiles * d.KG;
+    if (total <= 0) return cudaSuccess;
+    auto kern = output_transform_staged_m24<TF, YB>;
+    constexpr int smem = os24_smem_bytes<TF>();
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return e;
+    const int per_sm = std::max(1, std::min(2, 233472 / (smem + 1024)));
+    const long long grid = std::min<long long>(total, static_cast<long long>(sm_count()) * per_sm);
+    return launch_pdl(kern, dim3(static_cast<unsigned>(grid)), dim3(kOs24Threads), smem, s, d, total, err);
+}
+
+template <class TF>
+cudaError_t output_grouped_launch_m24(const OutDesc* descs, int ndesc, long long blocks, DevErr* err, cudaStream_t s) {
+    if (blocks <= 0) return cudaSuccess;
+    auto kern = output_transform_staged_m24_grouped<TF>;
+    constexpr int smem = os24_smem_bytes<TF>();
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return e;
+    const int per_sm = std::max(1, std::min(2, 233472 / (smem + 1024)));
+    const long long grid = std::min<long long>(blocks, static_cast<long long>(sm_count()) * per_sm);
+    return launch_pdl(kern, dim3(static_cast<unsigned>(grid)), dim3(kOs24Threads), smem, s, descs, ndesc, blocks, err);
+}
+
 template <class TF, class MT>
 cudaError_t output_grouped_launch(const OutDesc* descs, int ndesc, long long blocks, DevErr* err, cudaStream_t s) {
     if (blocks <= 0) return cudaSuccess;
@@ -814,14 +990,16 @@ InDesc make_in_desc(const Geom& g, const void* x, const void* x_end, void* V, co
     return d;
 }
 
-OutDesc make_out_desc(const Geom& g, bool m_fp32, const void* Mw, void* out, const float* scale) {
+OutDesc make_out_desc(const Geom& g, MType mt, const void* Mw, void* out, const float* scale) {
     OutDesc d{};
     d.Mw = Mw;
     d.out = static_cast<__half*>(out);
     d.scale = scale;
     d.K = g.k; d.OH = g.oh; d.OW = g.ow; d.tiles_h = g.tiles_h; d.tiles_w = g.tiles_w;
     d.P = g.P;
-    d.KG = m_fp32 ? g.kp / 4 : g.kp / 8;
+    d.KG = mt == MType::F32 ? g.kp / 4 : g.kp / 8;
+    d.m_lo = m24_lo_offset(static_cast<long long>(g.alpha) * g.alpha, g.P, g.kp);
+    d.m_pp = round_rows(g.P);
     d.gx = (g.P + kOsTiles - 1) / kOsTiles;
     d.gy = d.KG;
     d.blk_begin = 0;
@@ -831,8 +1009,8 @@ OutDesc make_out_desc(const Geom& g, bool m_fp32, const void* Mw, void* out, con
     // costs time (cfg3, 116 MB: 22.5 -> 23.8 us).  WG_CONV2D_KEEP_WORKSPACE=1
     // keeps M readable after the call.
     const char* keep_ws = std::getenv("WG_CONV2D_KEEP_WORKSPACE");
-    const long long m_bytes = static_cast<long long>(g.alpha) * g.alpha * d.KG * g.P * 16;
-    d.discard_m = !(keep_ws && std::atoi(keep_ws) != 0) && m_bytes > l2_cache_bytes();
+    d.discard_m = !(keep_ws && std::atoi(keep_ws) != 0) &&
+                  m_bytes(mt, static_cast<long long>(g.alpha) * g.alpha, g.P, g.kp) > l2_cache_bytes();
     return d;
 }
 
@@ -900,10 +1078,20 @@ cudaError_t launch_input_transform_grouped(Xform xf, OpType op, const InDesc* de
     return cudaErrorInvalidValue;
 }
 
-cudaError_t launch_output_transform(Xform xf, bool m_fp32, const Geom& g, const void* Mw, void* out,
+cudaError_t launch_output_transform(Xform xf, MType mt, const Geom& g, const void* Mw, void* out,
                                     const float* scale, DevErr* err, cudaStream_t stream, bool y_bf16) {
-    const OutDesc d = make_out_desc(g, m_fp32, Mw, out, scale);
-    if (y_bf16) {  // bf16 tensors: M is fp32 for both transforms
+    const OutDesc d = make_out_desc(g, mt, Mw, out, scale);
+    if (mt == MType::F24) {  // F(4x3) only
+        switch (xf) {
+            case Xform::F2: return cudaErrorNotSupported;
+            case Xform::F4: return y_bf16 ? output_launch_m24<F4, true>(d, err, stream) : output_launch_m24<F4>(d, err, stream);
+            case Xform::F4Ref:
+                return y_bf16 ? output_launch_m24<F4Ref, true>(d, err, stream) : output_launch_m24<F4Ref>(d, err, stream);
+        }
+        return cudaErrorInvalidValue;
+    }
+    const bool m_fp32 = mt == MType::F32;
+    if (y_bf16) {  // bf16 tensors: fp32 or 24-bit M
         if (!m_fp32) return cudaErrorNotSupported;
         switch (xf) {
             case Xform::F2: return output_launch<F2, float, true>(d, err, stream);
@@ -923,8 +1111,17 @@ cudaError_t launch_output_transform(Xform xf, bool m_fp32, const Geom& g, const 
     return cudaErrorInvalidValue;
 }
 
-cudaError_t launch_output_transform_grouped(Xform xf, bool m_fp32, const OutDesc* descs, int ndesc, long long blocks,
+cudaError_t launch_output_transform_grouped(Xform xf, MType mt, const OutDesc* descs, int ndesc, long long blocks,
                                             DevErr* err, cudaStream_t stream) {
+    if (mt == MType::F24) {
+        switch (xf) {
+            case Xform::F2: return cudaErrorNotSupported;
+            case Xform::F4: return output_grouped_launch_m24<F4>(descs, ndesc, blocks, err, stream);
+            case Xform::F4Ref: return output_grouped_launch_m24<F4Ref>(descs, ndesc, blocks, err, stream);
+        }
+        return cudaErrorInvalidValue;
+    }
+    const bool m_fp32 = mt == MType::F32;
     switch (xf) {
         case Xform::F2:
             return m_fp32 ? output_grouped_launch<F2, float>(descs, ndesc, blocks, err, stream)

@@ -24,6 +24,20 @@ inline int xform_alpha(Xform x) { return xform_m(x) + 2; }
 
 enum class OpType : int { F16 = 0, BF16 = 1 };
 
+// Storage of the GEMM result M (fp32 accumulators):
+//   F16  M[e][Kp/8][P][8] fp16 (F(2x3));
+//   F32  M[e][Kp/4][P][4] fp32 (granule layout), or M[e][P][Kp] row-major for
+//        the channels-last output path;
+//   F24  each fp32 value rounded to nearest at 24 bits and split in two
+//        planes: its upper 16 bits in H[e][Kp/8][P][8] (16-byte granules of 8
+//        channels, the fp16 layout) and its next 8 bits in
+//        L[e][Kp/8][Pp][8] (8-byte granules, Pp = P rounded up to 8), L
+//        right after H.  Relative rounding 2^-17 (fp16 M: 2^-12) for 3/4 of
+//        the fp32 bytes; the F(4x3) default.
+enum class MType : int { F16 = 0, F32 = 1, F24 = 2 };
+
+inline const char* mtype_name(MType t) { return t == MType::F16 ? "fp16" : t == MType::F32 ? "fp32" : "24-bit"; }
+
 // Geometry of one convolution as the Winograd path sees it.
 struct Geom {
     int n, c, h, w, k;   // NCHW input, K output channels
@@ -41,6 +55,15 @@ Geom make_geom(int n, int c, int h, int w, int k, int pad_h, int pad_w, int m);
 // Rows of V per element and granule: P rounded up to 8 (TMA reads V in
 // 128-byte rows of 8 tiles).
 inline long long round_rows(long long P) { return (P + 7) / 8 * 8; }
+
+// Bytes of M for E elements, P tiles and Kp (a multiple of 8) channels.
+inline long long m_bytes(MType t, long long E, long long P, long long Kp) {
+    if (t == MType::F16) return E * P * Kp * 2;
+    if (t == MType::F32) return E * P * Kp * 4;
+    return E * P * Kp * 2 + E * round_rows(P) * Kp;
+}
+// Byte offset of the low plane of 24-bit M.
+inline long long m24_lo_offset(long long E, long long P, long long Kp) { return E * P * Kp * 2; }
 
 // U[e][Cp/8][Kp][8] = G g G^T, from KCRS fp16 weights; fp32 arithmetic, result
 // in the operand type; zero for c >= C or k >= K.
@@ -83,23 +106,25 @@ struct OutDesc {
     int gy;               // work items along granules
     long long blk_begin;
     int discard_m;        // M is read once here: drop its L2 lines without write-back
+    long long m_lo;       // 24-bit M: byte offset of the low plane from Mw
+    long long m_pp;       // 24-bit M: rows of the low plane per granule (P rounded up to 8)
 };
 
 // Descriptor of one problem's input transform and the dynamic shared memory
 // of its (persistent, double-buffered) launch.
 InDesc make_in_desc(const Geom& g, const void* x, const void* x_end, void* V, const float* scale, int* smem);
-OutDesc make_out_desc(const Geom& g, bool m_fp32, const void* Mw, void* out, const float* scale);
+OutDesc make_out_desc(const Geom& g, MType mt, const void* Mw, void* out, const float* scale);
 // Grouped launches: `blocks` = sum of gx*gy work items; descs device-resident,
 // sorted by blk_begin; smem = the largest of the problems' *smem; `scaled` when
 // any problem has a per-tile scale.
 cudaError_t launch_input_transform_grouped(Xform xf, OpType op, const InDesc* descs, int ndesc, long long blocks,
                                            int smem, bool scaled, DevErr* err, cudaStream_t stream);
-cudaError_t launch_output_transform_grouped(Xform xf, bool m_fp32, const OutDesc* descs, int ndesc, long long blocks,
+cudaError_t launch_output_transform_grouped(Xform xf, MType mt, const OutDesc* descs, int ndesc, long long blocks,
                                             DevErr* err, cudaStream_t stream);
 
-// out[N][K][OH][OW] = A^T M A from M[e][Kp/8][P][8] (fp16, m_fp32 false) or
-// M[e][Kp/4][P][4] (fp32); divides by scale[p] when scale is not null.
-cudaError_t launch_output_transform(Xform xf, bool m_fp32, const Geom& g, const void* Mw, void* out,
+// out[N][K][OH][OW] = A^T M A from M stored as `mt` (granule layouts above);
+// divides by scale[p] when scale is not null.
+cudaError_t launch_output_transform(Xform xf, MType mt, const Geom& g, const void* Mw, void* out,
                                     const float* scale, DevErr* err, cudaStream_t stream, bool y_bf16 = false);
 
 // ---- tcgen05 batched GEMM: M_e[P][K] = V_e[P][Cp] * U_e[K][Cp]^T -----------
@@ -113,6 +138,8 @@ struct alignas(64) GemmDesc {
     int P, kg_count, m_blocks, n_blocks, k_blocks, E;
     int m_row;           // 1: M[e][P][Kp] (rows of output channels, NHWC output path)
     int kp;
+    long long m_lo;      // 24-bit M: byte offset of the low plane from Mw
+    int m_pp;            // 24-bit M: rows of the low plane per granule
     int keep_m;          // M fits in L2: store it with the evict_last priority
     // V[E][v_cg][v_pp][8] is read by this GEMM only (one block of output
     // channels): its lines are discarded from L2 once a tile is done, so the
@@ -128,19 +155,19 @@ struct GemmPlan {
     int bn;              // 32, 64, 128 or 256
     int grid;
     int smem_bytes;
-    bool m_fp32;
+    MType mt;
     OpType op;
 };
 
 // Builds the tensor maps; V, U, M must stay at these addresses.
 cudaError_t make_gemm_desc(GemmDesc& d, OpType op, int E, long long P, int K, int Kp, int Cp, const void* V,
-                           const void* U, void* Mw, bool m_fp32, int bn, bool m_row = false);
+                           const void* U, void* Mw, MType mt, int bn, bool m_row = false);
 cudaError_t plan_gemm(GemmPlan& gp, OpType op, int E, long long P, int K, int Kp, int Cp, const void* V,
-                      const void* U, void* Mw, bool m_fp32, int bn, int num_sms, bool m_row = false);
+                      const void* U, void* Mw, MType mt, int bn, int num_sms, bool m_row = false);
 cudaError_t launch_gemm(const GemmPlan& gp, DevErr* err, cudaStream_t stream);
 // Many problems (same BN, operand and M types) in one persistent launch; descs
 // device-resident (64-byte aligned), sorted by tile_begin.
-cudaError_t launch_gemm_grouped(const GemmDesc* descs, int ndesc, long long total_tiles, OpType op, bool m_fp32, int bn,
+cudaError_t launch_gemm_grouped(const GemmDesc* descs, int ndesc, long long total_tiles, OpType op, MType mt, int bn,
                                 int grid, DevErr* err, cudaStream_t stream);
 int gemm_smem_bytes(int bn);
 
@@ -173,7 +200,7 @@ struct NhwcOutDesc {
     int discard_m;        // drop M's lines from L2 once read (set by the launcher)
 };
 NhwcOutDesc make_nhwc_out_desc(const Geom& g, const void* Mw, void* out);
-cudaError_t launch_nhwc_output_transform(Xform xf, bool m_fp32, const NhwcOutDesc& d, cudaStream_t stream);
+cudaError_t launch_nhwc_output_transform(Xform xf, MType mt, const NhwcOutDesc& d, cudaStream_t stream);
 
 // ---- fused F(2x3): input transform + tcgen05 GEMM + output transform ------
 struct FusedPlan {

@@ -34,7 +34,7 @@ struct Plan {
     int algo = 0;
     Xform xf = Xform::F2;
     OpType op = OpType::F16;
-    bool m_fp32 = false;
+    MType mt = MType::F16;  // storage of the GEMM result M
     bool scaling = false;
     Geom g{};
     int chunk_n = 1, n_chunks = 1;

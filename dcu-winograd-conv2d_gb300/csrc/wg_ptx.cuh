@@ -173,6 +173,9 @@ __device__ __forceinline__ void st_hint_v4(void* ptr, uint4 v, uint64_t pol) {
     asm volatile("st.global.L2::cache_hint.v4.b32 [%0], {%1, %2, %3, %4}, %5;" ::"l"(ptr), "r"(v.x), "r"(v.y),
                  "r"(v.z), "r"(v.w), "l"(pol));
 }
+__device__ __forceinline__ void st_hint_v2(void* ptr, uint2 v, uint64_t pol) {
+    asm volatile("st.global.L2::cache_hint.v2.b32 [%0], {%1, %2}, %3;" ::"l"(ptr), "r"(v.x), "r"(v.y), "l"(pol));
+}
 
 // Non-tensor bulk copy global -> shared: both addresses 16-byte aligned,
 // `bytes` a multiple of 16; completion counted on `bar` as transaction bytes.

@@ -99,7 +99,19 @@ enum {
 };
 
 /* Options for getkernelInfo_ex.  conv2d_options_default() gives the values
- * getkernelInfo uses, after applying the WG_CONV2D_* environment overrides. */
+ * getkernelInfo uses, after applying the WG_CONV2D_* environment overrides.
+ *
+ * ALGORITHM CHOICE.  getkernelInfo picks the algorithm with the per-shape
+ * autotuner (algo = CONV2D_ALGO_AUTO): the first time a shape is seen it
+ * times the candidates (the reference's three algorithms and the row F(4x3)
+ * kernel) on the device, reading the problem's input and weights and writing
+ * a scratch output, and keeps the reference rule's pick unless another is
+ * more than 3% faster; the choice is cached per shape (and in
+ * WG_CONV2D_TUNE_FILE).  On GB300 the reference rule's fused F(2x3) pick is
+ * several times slower than the alternatives for wide K (e.g. 392 against
+ * 121 us on 32x256x56^2 -> 256).  algo = CONV2D_ALGO_REFERENCE, or
+ * WG_CONV2D_ALGO=ref, applies the reference rule (src/conv2d.cpp:83-114)
+ * exactly; conv2d_get_algo reports what was chosen. */
 typedef struct
 {
     int algo;            /* CONV2D_ALGO_* */
@@ -113,7 +125,10 @@ typedef struct
                             operands, F(4x3) fp16 operands with per-tile scaling, both an fp32 M */
     int layout_nhwc;     /* 1: input and output tensors are NHWC (channels last; filter stays KCRS);
                             non-fused F(2x3)/F(4x3), fp16 tensors, images up to ~250 columns */
-    int reserved[2];
+    int m_fp32;          /* F(4x3) non-fused: 1 stores the GEMM result M in fp32; 0 (default) in 24 bits
+                            (each fp32 accumulator rounded to its upper 24 bits: relative rounding
+                            2^-17, 3/4 of the fp32 bytes).  NHWC tensors always use fp32 M */
+    int reserved[1];
 } conv2d_options_t;
 
 /* reference include/conv2d.h:39-42 */
@@ -210,8 +225,8 @@ int conv2d_batch_destroy(conv2d_batch_t* batch);
  * admitted requests packed into batches of at most `max_batch` and launched
  * as grouped kernels on one of `slots` streams, so batches overlap on the
  * device (continuous batching).  A request's result does not depend on what
- * else is in its batch.  slots = 1, max_batch = 1 gives the plain per-request
- * path. */
+ * else is in its batch.  per_request = 1 gives the plain per-call path: each
+ * request's own kernels queued at submission on one stream. */
 typedef struct conv2d_server conv2d_server_t;
 typedef struct
 {
@@ -219,7 +234,10 @@ typedef struct
     int max_batch;               /* requests per batch (default 64) */
     int slots;                   /* batches in flight (default 3) */
     int algo;                    /* CONV2D_ALGO_AUTO (shape rule), _2X3_NON_FUSED or _4X3_NON_FUSED */
-    int reserved[4];
+    int per_request;             /* 1: the plain per-call path instead of batching: each request's own
+                                    kernels queued on one stream when it is submitted, in arrival
+                                    order, no wait for earlier requests (slots and max_batch unused) */
+    int reserved[3];
 } conv2d_server_config_t;
 typedef struct
 {
@@ -229,6 +247,8 @@ typedef struct
     int max_inflight_batches;
     long long arena_used_bytes;
     double flops;                /* direct-convolution FLOPs of completed requests */
+    double busy_us;              /* device time with at least one batch between its start and end events */
+    double overlap_us;           /* device time with two or more batches in flight at once */
 } conv2d_server_stats_t;
 int conv2d_server_config_default(conv2d_server_config_t* cfg);
 int conv2d_server_create(const conv2d_server_config_t* cfg, conv2d_server_t** server);

@@ -152,3 +152,19 @@ def test_code_written_for_reference_header_links(wg, tmp_path):
     assert r.returncode == 0, r.stderr
     r = subprocess.run([str(exe)], capture_output=True, text=True)
     assert r.returncode == 0 and r.stdout.split() == ["1", "2"], r.stdout + r.stderr
+
+
+def test_default_selection_is_the_autotuner_and_ref_is_strict(wg, monkeypatch):
+    """getkernelInfo's default options pick the algorithm per shape with the
+    autotuner; WG_CONV2D_ALGO=ref gives the reference's own rule."""
+    monkeypatch.delenv("WG_CONV2D_ALGO", raising=False)
+    assert wg.default_options().algo == wg.ALGO_AUTO
+    monkeypatch.setenv("WG_CONV2D_ALGO", "ref")
+    assert wg.default_options().algo == wg.ALGO_REFERENCE
+    monkeypatch.setenv("WG_CONV2D_ALGO", "4x3")
+    assert wg.default_options().algo == wg.ALGO_4X3
+    # 24-bit M is the F(4x3) default; WG_CONV2D_M_FP32=1 asks for fp32
+    monkeypatch.delenv("WG_CONV2D_M_FP32", raising=False)
+    assert wg.default_options().m_fp32 == 0
+    monkeypatch.setenv("WG_CONV2D_M_FP32", "1")
+    assert wg.default_options().m_fp32 == 1

@@ -105,15 +105,33 @@ def _dev_array(wg, ptr, count, dtype):
     return out
 
 
-@pytest.mark.parametrize("algo,variant", [(1, "F2"), (0, "F4"), (0, "F4Ref")])
-def test_transform_kernels_elementwise(wg, monkeypatch, algo, variant):
+def read_m(wg, ptr, E, P, kp, mtype):
+    """M read back from the workspace as float64 [E][P][Kp]: fp16
+    M[E][Kp/8][P][8], fp32 M[E][Kp/4][P][4], or 24-bit M (upper 16 bits of
+    each rounded fp32 value in H[E][Kp/8][P][8], the next 8 bits in
+    L[E][Kp/8][Pp][8] right after H)."""
+    if mtype == "fp16":
+        Mw = _dev_array(wg, ptr, E * P * kp, np.float16).reshape(E, kp // 8, P, 8)
+    elif mtype == "fp32":
+        Mw = _dev_array(wg, ptr, E * P * kp, np.float32).reshape(E, kp // 4, P, 4)
+    else:
+        Pp = (P + 7) // 8 * 8
+        raw = _dev_array(wg, ptr, 2 * E * P * kp + E * Pp * kp, np.uint8)
+        hi = raw[:2 * E * P * kp].view(np.uint16).reshape(E, kp // 8, P, 8).astype(np.uint32)
+        lo = raw[2 * E * P * kp:].reshape(E, kp // 8, Pp, 8)[:, :, :P].astype(np.uint32)
+        Mw = ((hi << 16) | (lo << 8)).view(np.float32)
+    return Mw.transpose(0, 2, 1, 3).reshape(E, P, kp).astype(np.float64)
+
+
+@pytest.mark.parametrize("algo,variant,mfp32", [(1, "F2", 0), (0, "F4", 0), (0, "F4", 1), (0, "F4Ref", 0)])
+def test_transform_kernels_elementwise(wg, monkeypatch, algo, variant, mfp32):
     """U, V and M read back from the workspace, each against its restatement
     (the GEMM otherwise drops V from L2 once it is read, leaving its memory
-    undefined)."""
+    undefined).  F(4x3) stores M in 24 bits by default, in fp32 on request."""
     monkeypatch.setenv("WG_CONV2D_KEEP_WORKSPACE", "1")
     n, c, h, w, k = 2, 20, 11, 13, 24
     x, wt = O.uniform_inputs(31, n, c, h, w, k)
-    opts = opts_for(wg, algo, f4_points=1 if variant == "F4Ref" else 0)
+    opts = opts_for(wg, algo, f4_points=1 if variant == "F4Ref" else 0, m_fp32=mfp32)
     y, op = run(wg, x, wt, 1, 1, opts)
     m = O.XFORMS[variant][0]
     E = (m + 2) ** 2
@@ -128,10 +146,8 @@ def test_transform_kernels_elementwise(wg, monkeypatch, algo, variant):
     U = U[:, :k].reshape(E, k, cp).astype(np.float64)
     V = _dev_array(wg, Vp, E * Pp * cp, np.float16).reshape(E, cp // 8, Pp, 8).transpose(0, 2, 1, 3)
     V = V[:, :P].reshape(E, P, cp).astype(np.float64)
-    mdt = np.float32 if m == 4 else np.float16
-    gr = 4 if m == 4 else 8
-    Mw = _dev_array(wg, Mp, E * P * kp, mdt).reshape(E, kp // gr, P, gr).transpose(0, 2, 1, 3)
-    Mw = Mw.reshape(E, P, kp).astype(np.float64)
+    mtype = "fp16" if m == 2 else ("fp32" if mfp32 else "24-bit")
+    Mw = read_m(wg, Mp, E, P, kp, mtype)
 
     U_ref = O.filter_transform(wt.astype(np.float64), m, variant)
     V_ref = O.input_transform(x.astype(np.float64), m, 1, 1, variant)
@@ -146,7 +162,8 @@ def test_transform_kernels_elementwise(wg, monkeypatch, algo, variant):
     # GEMM of exactly the stored operands, fp32 accumulation
     M_ref = np.einsum("epc,ekc->epk", V, U)
     scale = np.einsum("epc,ekc->epk", np.abs(V), np.abs(U)) + 1e-30
-    tol = 2.0 ** -10 if mdt == np.float16 else 1e-5
+    # fp32 accumulation, then the storage rounding: fp16 2^-11, 24 bits 2^-17
+    tol = {"fp16": 2.0 ** -10, "fp32": 1e-5, "24-bit": 2.0 ** -16}[mtype]
     assert np.all(np.abs(Mw[:, :, :k] - M_ref) <= scale * tol)
     # output transform of exactly the stored M
     y_ref = O.output_transform(Mw[:, :, :k], m, n, k, oh, ow, variant)
@@ -167,14 +184,17 @@ def test_repeat_calls_bit_identical(wg, algo):
     assert torch.equal(first, y)
 
 
-def test_reference_harness_replay_cfg1(wg):
-    """1x64x56x56 -> 64, reference-style inputs, the reference's own selection
-    (F(4x3)), checked as the reference benchmark checks it."""
+@pytest.mark.parametrize("selection", ["reference", "default"])
+def test_reference_harness_replay_cfg1(wg, selection):
+    """1x64x56x56 -> 64, reference-style inputs, with the reference's own
+    selection (F(4x3)) and with the default (autotuned) selection, checked as
+    the reference benchmark checks it."""
     _, x, wt, p, q, ref = golden_case("refstyle_cfg1")
-    y, op = run(wg, x, wt, p, q, None)
-    assert op.algo == 0
+    y, op = run(wg, x, wt, p, q, opts_for(wg, wg.ALGO_REFERENCE) if selection == "reference" else None)
+    if selection == "reference":
+        assert op.algo == 0
     assert O.reference_criterion_failures(y, ref) == 0
-    assert O.rel_errors(y, ref)[0] <= TOL[4]
+    assert O.rel_errors(y, ref)[0] <= TOL[algo_m(op.algo)]
 
 
 # The reference benchmark's contest shapes (N, C, H = W, K), its pre.sh and
@@ -186,16 +206,19 @@ CONTEST_SHAPES = [
 ]
 
 
+@pytest.mark.parametrize("selection", ["reference", "default"])
 @pytest.mark.parametrize("n,c,hw,k", CONTEST_SHAPES)
-def test_contest_shapes_as_the_reference_checks_them(wg, n, c, hw, k):
-    """Each contest shape through the drop-in API with the reference's
-    selection and its input fill (glibc rand, src/main.cpp:36-44), checked
-    with the reference benchmark's criterion and against FP64 on image 0 and
-    up to 8 output channels spread over K (the share of the output the CPU
-    oracle computes in about a second)."""
+def test_contest_shapes_as_the_reference_checks_them(wg, n, c, hw, k, selection):
+    """Each contest shape through the drop-in API, with the reference's
+    selection rule and with the default (autotuned) selection, on the
+    reference's input fill (glibc rand, src/main.cpp:36-44), checked with the
+    reference benchmark's criterion and against FP64 on image 0 and up to 8
+    output channels spread over K (the share of the output the CPU oracle
+    computes in about a second)."""
     x, wt = O.reference_style_inputs(n, c, hw, hw, k)
-    y, op = run(wg, x, wt, 1, 1, None)
-    assert op.algo == O.select_reference(n, c, hw, hw, k)
+    y, op = run(wg, x, wt, 1, 1, opts_for(wg, wg.ALGO_REFERENCE) if selection == "reference" else None)
+    if selection == "reference":
+        assert op.algo == O.select_reference(n, c, hw, hw, k)
     ks = np.unique(np.linspace(0, k - 1, min(k, 8)).round().astype(int))
     ref16, r64 = O.conv2d_direct(x[:1], wt[ks], nthreads=8)
     got = y[:1, ks]
@@ -372,10 +395,11 @@ NHWC_SHAPES = [(2, 24, 16, 16, 32, 1), (1, 16, 13, 11, 27, 1), (3, 40, 9, 30, 36
 def test_nhwc_matches_nchw_bit_for_bit(wg, algo, shape):
     """Channels-last input and output (filter KCRS): the same V, M and output
     arithmetic as the NCHW path, so the result is the NCHW result transposed,
-    bit for bit (the fused selection runs F(2x3) non-fused for NHWC)."""
+    bit for bit (the fused selection runs F(2x3) non-fused for NHWC).  NHWC
+    stores F(4x3)'s M in fp32, so the NCHW call is asked for fp32 M too."""
     n, c, h, w, k, pad = shape
     x, wt = O.uniform_inputs(41 + algo, n, c, h, w, k)
-    y_nchw, op1 = run(wg, x, wt, pad, pad, opts_for(wg, 1 if algo == 2 else algo))
+    y_nchw, op1 = run(wg, x, wt, pad, pad, opts_for(wg, 1 if algo == 2 else algo, m_fp32=1))
     xt = torch.from_numpy(np.ascontiguousarray(x.transpose(0, 2, 3, 1))).cuda()
     wtt = torch.from_numpy(wt).cuda()
     oh, ow = h + 2 * pad - 2, w + 2 * pad - 2

@@ -106,3 +106,49 @@ def test_oversized_request_is_refused(wg):
         srv.submit(li, 8, x.data_ptr(), y.data_ptr())
     assert ei.value.status == wg.ERR_BUSY
     srv.destroy()
+
+
+def test_plain_per_request_path_gives_the_served_bits(wg):
+    """The plain per-call path (each request's own kernels queued on one stream
+    at submission) and the batching server compute every request the same
+    way, bit for bit."""
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    plain = wg.Server(per_request=1, hbm_budget_bytes=1 << 30)
+    rng, k1, host = _setup(wg, plain, 8)
+    reqs = _requests(rng, 12)
+    a = _run(wg, plain, reqs, together=True)
+    st = plain.stats()
+    plain.destroy()
+    assert st["completed"] == len(reqs) and st["mean_batch"] == 1.0
+    served = wg.Server(slots=3, max_batch=4, hbm_budget_bytes=1 << 30)
+    _setup(wg, served, 8)
+    b = _run(wg, served, reqs, together=True)
+    served.destroy()
+    for (li, n, x), ya, yb in zip(reqs, a, b):
+        assert np.array_equal(ya.view(np.uint16), yb.view(np.uint16))
+
+
+def test_batches_overlap_on_the_device(wg):
+    """Under a burst of requests the server keeps several batches in flight
+    at once, and their device intervals (start and end events on the slots'
+    streams) overlap."""
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    srv = wg.Server(slots=3, max_batch=4, hbm_budget_bytes=4 << 30)
+    rng, keep, host = _setup(wg, srv, 9)
+    bufs = []
+    for li, (c, k, h, w) in enumerate(LAYERS):
+        x = (torch.rand((8, c, h, w), device="cuda") * 2 - 1).half()
+        y = torch.empty((8, k, h, w), dtype=torch.float16, device="cuda")
+        bufs.append((x, y))
+    torch.cuda.synchronize()
+    for i in range(200):
+        li = i % len(LAYERS)
+        srv.submit(li, 8, bufs[li][0].data_ptr(), bufs[li][1].data_ptr())
+    srv.wait_all()
+    st = srv.stats()
+    srv.destroy()
+    assert st["completed"] == 200
+    assert st["max_inflight_batches"] > 1
+    assert st["overlap_us"] > 0.0 and st["busy_us"] > 0.0
