@@ -308,7 +308,7 @@ def make_inputs(torch, workload, device, seed):
     return x, wt
 
 
-def algorithmic_work(name, geo):
+def algorithmic_work(name, geo, m_bytes_per_value=None):
     """Per-launch work of one kernel (P tiles, E = (m+2)^2 Winograd elements,
     fp16 tensors and operands).
 
@@ -324,12 +324,14 @@ def algorithmic_work(name, geo):
       fused2x3          x + U + y;                   FLOPs 2*16*P*C*K
       row4x3            x + U1 (2*18*C*K) + y;       FLOPs 2*18*RT*C*K over
                         RT = N*OH*ceil(OW/4) row tiles
+    M is counted at `m_bytes_per_value` bytes per value (3 for the 24-bit
+    F(4x3) default, 4 for fp32, 2 for fp16).
     Returns (algorithmic bytes, design bytes, FLOPs, formula)."""
     n, c, h, w, k, m = geo
     oh, ow = h, w  # pad 1
     tiles = n * math.ceil(oh / m) * math.ceil(ow / m)
     E = (m + 2) ** 2
-    mb = 4.0 if m == 4 else 2.0
+    mb = m_bytes_per_value or (3.0 if m == 4 else 2.0)
     x_b, y_b = 2.0 * n * c * h * w, 2.0 * n * k * oh * ow
     v_b, u_b, m_b = 2.0 * E * tiles * c, 2.0 * E * c * k, mb * E * tiles * k
     if name == "gemm_tcgen05":
@@ -347,13 +349,13 @@ def algorithmic_work(name, geo):
     return y_b, m_b + y_b, 0.0, f"y (design adds M {m_b / 1e6:.1f} MB)"
 
 
-def roofline_for(name, wg, geo, ms, pk, pk_kind):
+def roofline_for(name, wg, geo, ms, pk, pk_kind, m_bytes_per_value=None):
     """Roofline of one kernel from its algorithmic work per launch and its
     CUDA-event duration `ms`.  A kernel with FLOPs is bound by the roof its
     arithmetic intensity puts it under (machine balance = peak FLOP/s / peak
     bytes/s); `frac` is the bound's time over the measured time, i.e. the
     larger of the two fractions."""
-    byts, design, flops, formula = algorithmic_work(name, geo)
+    byts, design, flops, formula = algorithmic_work(name, geo, m_bytes_per_value)
     peak_bw, peak_fl = pk["hbm_gbs"], pk["bf16_tflops"]
     out = {"kernel": name}
     if flops and flops / byts > peak_fl * 1e12 / (peak_bw * 1e9):
@@ -576,7 +578,8 @@ def our_arm(args):
     dom_ms = tot[dominant] / launches_of_dom
     m = 4 if algo in (wg.ALGO_4X3, wg.ALGO_4X3_ROW) else 2
     pk, pk_kind = peaks()
-    roof = roofline_for(dominant, wg, (n, c, h, w, k, m), dom_ms, pk, pk_kind)
+    mbv = 2.0 if m == 2 else (4.0 if (args.m_fp32 or args.nhwc) else 3.0)
+    roof = roofline_for(dominant, wg, (n, c, h, w, k, m), dom_ms, pk, pk_kind, mbv)
     traffic = committed_traffic(dominant, args.workload)
     roof["traffic"] = traffic
     roof["traffic_over_algorithmic"] = traffic / roof["algorithmic_bytes"] if traffic else None
@@ -586,7 +589,7 @@ def our_arm(args):
     kernel_roofline = {nm: {key: r[key] for key in ("bound", "frac", "hbm_frac", "tensor_frac", "design_bytes_frac",
                                                   "algorithmic_per_launch") if key in r}
                        for nm, r in ((nm, roofline_for(nm, wg, (n, c, h, w, k, m), sum(kt[nm]) / len(kt[nm]), pk,
-                                                       pk_kind)) for nm in kt)}
+                                                       pk_kind, mbv)) for nm in kt)}
 
     # accuracy of what was timed: the last timed step's output against FP64
     last = (args.steps - 1) % nsets

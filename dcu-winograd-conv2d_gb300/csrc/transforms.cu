@@ -615,6 +615,42 @@ __global__ void __launch_bounds__(kOsThreads, 3)
     output_staged_body<TF, MT, YB>(&d, 1, total, err);
 }
 
+// A^T m A on a channel pair in packed fp32x2 (one instruction for both
+// channels): the F(4x3) output transforms of both point sets, same matrices
+// as TF::at.
+template <class TF> struct At2;
+template <> struct At2<F4> {   // points 0, +-1, 1/2, -2
+    __device__ __forceinline__ static void run(const float2* m, int sm, float2* o, int so) {
+        const float2 m0 = m[0], m1 = m[sm], m2 = m[2 * sm], m3 = m[3 * sm], m4 = m[4 * sm], m5 = m[5 * sm];
+        const float2 a = __fadd2_rn(m1, m2), b = sub2(m1, m2);
+        o[0] = __fadd2_rn(__fadd2_rn(m0, a), __fadd2_rn(m3, m4));
+        o[so] = fma2(m4, f2(-2.f), fma2(m3, f2(0.5f), b));
+        o[2 * so] = fma2(m4, f2(4.f), fma2(m3, f2(0.25f), a));
+        o[3 * so] = __fadd2_rn(fma2(m4, f2(-8.f), fma2(m3, f2(0.125f), b)), m5);
+    }
+};
+template <> struct At2<F4Ref> {   // points 0, +-1, +-2
+    __device__ __forceinline__ static void run(const float2* m, int sm, float2* o, int so) {
+        const float2 m0 = m[0], m1 = m[sm], m2 = m[2 * sm], m3 = m[3 * sm], m4 = m[4 * sm], m5 = m[5 * sm];
+        const float2 a = __fadd2_rn(m1, m2), b = sub2(m1, m2), c = __fadd2_rn(m3, m4), d = sub2(m3, m4);
+        o[0] = __fadd2_rn(__fadd2_rn(m0, a), c);
+        o[so] = fma2(d, f2(2.f), b);
+        o[2 * so] = fma2(c, f2(4.f), a);
+        o[3 * so] = __fadd2_rn(fma2(d, f2(8.f), b), m5);
+    }
+};
+
+template <class TF>
+__device__ __forceinline__ void output_tile_transform2(const float2 (&m)[TF::ALPHA * TF::ALPHA],
+                                                       float2 (&y)[TF::M * TF::M]) {
+    constexpr int A = TF::ALPHA, M = TF::M;
+    float2 t[M * A];
+#pragma unroll
+    for (int j = 0; j < A; ++j) At2<TF>::run(&m[j], A, &t[j], A);      // A^T m
+#pragma unroll
+    for (int i = 0; i < M; ++i) At2<TF>::run(&t[i * A], 1, &y[i * M], 1);  // (A^T m) A
+}
+
 // 24-bit M (high plane H[e][KG][P][8] of 16-bit words, low plane
 // L[e][KG][Pp][8] of bytes): a work item is 64 tiles x one granule of 8
 // channels; warp 8 stages the item's E high runs (up to 1 KB) and E low runs
@@ -703,23 +739,26 @@ __device__ __forceinline__ void output_staged_body_m24(const OutDesc* descs, int
                 const float inv = d.scale ? 1.f / d.scale[p] : 1.f;  // exact: scale is a power of two
                 const unsigned char* hsrc = bufs + b * kItemBytes + t * 16 + qd * 4;
                 const unsigned char* lsrc = bufs + b * kItemBytes + kLoBase + t * 8 + qd * 2;
-                float m0[E], m1[E];
+                // value bits = high 16 | low 8 << 8: one byte permute per
+                // value, the zero byte taken from the zero-extended 16-bit
+                // load of the low pair
+                float2 m[E];
 #pragma unroll
                 for (int e = 0; e < E; ++e) {
                     const uint32_t h = *reinterpret_cast<const uint32_t*>(hsrc + e * (kOsTiles * 16));
                     const uint32_t l = *reinterpret_cast<const uint16_t*>(lsrc + e * (kOsTiles * 8));
-                    m0[e] = __uint_as_float((h << 16) | ((l & 0xffu) << 8));
-                    m1[e] = __uint_as_float((h & 0xffff0000u) | (l & 0xff00u));
+                    m[e] = make_float2(__uint_as_float(__byte_perm(l, h, 0x5403)),
+                                       __uint_as_float(__byte_perm(l, h, 0x7613)));
                 }
+                float2 y2[M * M];
+                output_tile_transform2<TF>(m, y2);
 #pragma unroll
                 for (int ch = 0; ch < 2; ++ch) {
                     const int kc = g * 8 + qd * 2 + ch;
                     if (kc >= K) break;
                     float y[M * M];
-                    if (ch == 0)
-                        output_tile_transform<TF>(m0, y);
-                    else
-                        output_tile_transform<TF>(m1, y);
+#pragma unroll
+                    for (int i = 0; i < M * M; ++i) y[i] = ch == 0 ? y2[i].x : y2[i].y;
                     YT* o = out + ((n * K + kc) * OH + oh0) * static_cast<long long>(OW) + ow0;
 #pragma unroll
                     for (int i = 0; i < M; ++i)
