@@ -42,13 +42,19 @@ constexpr int kBM = 128;
 constexpr int kBK = 64;                 // 8 granules of 8 channels per stage
 constexpr int kTileABytes = kBM * kBK * 2;
 
-template <int BN>
+// RESB: the U block of a work item (BN rows x all Cp channels) stays in
+// shared memory across consecutive work items that use it, and only V goes
+// through the stage ring (single-problem launches whose U block fits).
+constexpr int kResBBytes = 128 * 1024;
+
+template <int BN, bool RESB = false>
 struct GemmCfg {
     static constexpr int kTileB = BN * kBK * 2;
-    static constexpr int kStageBytes = kTileABytes + kTileB;
-    static constexpr int kStages = std::min(8, (200 * 1024) / kStageBytes);
+    static constexpr int kStageBytes = kTileABytes + (RESB ? 0 : kTileB);
+    static constexpr int kBRegion = RESB ? kResBBytes : 0;   // + the ring's B tiles, below
+    static constexpr int kStages = std::min(8, (200 * 1024 - kBRegion) / kStageBytes);
     static constexpr int kTmemCols = (2 * BN < 32) ? 32 : 2 * BN;  // two accumulators
-    static constexpr int kSmem = kStages * kStageBytes + 1024 /*align*/ + 256 /*barriers*/;
+    static constexpr int kSmem = kStages * kStageBytes + kBRegion + 1024 /*align*/ + 256 /*barriers*/;
     // + the row-major epilogue's transpose blocks (32x32 fp32 per epilogue
     // warp), only in launches that write row-major M
     static constexpr int kSmemRow = kSmem + 8 * 32 * 32 * 4;
@@ -154,12 +160,32 @@ __device__ __forceinline__ Item locate(const GemmDesc* __restrict__ descs, int n
     return it;
 }
 
+// Resident-U order (one problem): tile block fastest, then channel block,
+// then element, so the items of one (element, channel block) -- one U block --
+// are consecutive; each CTA takes a contiguous range of them.
+__device__ __forceinline__ Item locate_resb(const GemmDesc& d, long long t) {
+    Item it;
+    it.mb = static_cast<int>(t % d.m_blocks);
+    const long long rest = t / d.m_blocks;
+    it.nb = static_cast<int>(rest % d.n_blocks);
+    it.e = static_cast<int>(rest / d.n_blocks);
+    return it;
+}
+
+template <bool RESB>
+__device__ __forceinline__ Item locate_item(const GemmDesc* __restrict__ descs, int ndesc, long long t, int& pi) {
+    if constexpr (RESB)
+        return locate_resb(descs[0], t);
+    else
+        return locate(descs, ndesc, t, pi);
+}
+
 constexpr int kGemmThreads = 320;  // TMA warp, MMA warp, 8 epilogue warps
 
-template <int BN, bool BF16, class MT>
+template <int BN, bool BF16, class MT, bool RESB>
 __device__ __forceinline__ void gemm_body(const GemmDesc* __restrict__ descs, int ndesc, long long total_tiles,
                                           DevErr* err) {
-    using Cfg = GemmCfg<BN>;
+    using Cfg = GemmCfg<BN, RESB>;
     constexpr int S = Cfg::kStages;
     constexpr int kEpiHalves = BN >= 64 ? 2 : 1;  // epilogue warps per TMEM lane quarter
     constexpr uint32_t kIdesc = make_idesc_f16(kBM, BN, BF16);
@@ -169,14 +195,21 @@ __device__ __forceinline__ void gemm_body(const GemmDesc* __restrict__ descs, in
     // hide that this is shared memory and turn every access generic)
     unsigned char* smem = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
     unsigned char* sA = smem;
-    unsigned char* sB = smem + S * kTileABytes;
-    uint64_t* bars = reinterpret_cast<uint64_t*>(smem + S * Cfg::kStageBytes);
+    unsigned char* sB = smem + S * kTileABytes;   // B ring stages, or the resident U block
+    unsigned char* after = smem + S * Cfg::kStageBytes + Cfg::kBRegion;
+    uint64_t* bars = reinterpret_cast<uint64_t*>(after);
     uint64_t* full = bars;
     uint64_t* empty = bars + S;
     uint64_t* tfull = bars + 2 * S;
     uint64_t* tempty = bars + 2 * S + 2;
-    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * S + 4);
-    uint32_t* xpose = reinterpret_cast<uint32_t*>(smem + S * Cfg::kStageBytes + 256);  // [8 warps][32][32]
+    uint64_t* bfull = bars + 2 * S + 4;    // resident U loaded
+    uint64_t* bempty = bars + 2 * S + 5;   // the MMAs reading the resident U are done
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * S + 6);
+    uint32_t* xpose = reinterpret_cast<uint32_t*>(after + 256);  // [8 warps][32][32]
+    // items: round robin over the grid, or a contiguous range per CTA (RESB)
+    const long long t_lo = RESB ? static_cast<long long>(blockIdx.x) * total_tiles / gridDim.x : blockIdx.x;
+    const long long t_hi = RESB ? static_cast<long long>(blockIdx.x + 1) * total_tiles / gridDim.x : total_tiles;
+    const long long t_step = RESB ? 1 : gridDim.x;
     volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -190,6 +223,8 @@ __device__ __forceinline__ void gemm_body(const GemmDesc* __restrict__ descs, in
             mbar_init(&tfull[i], 1);
             mbar_init(&tempty[i], 128 * kEpiHalves);
         }
+        mbar_init(bfull, 1);
+        mbar_init(bempty, 1);
         *abort_flag = 0;
         fence_barrier_init();
     }
@@ -207,8 +242,10 @@ __device__ __forceinline__ void gemm_body(const GemmDesc* __restrict__ descs, in
             int stage = 0;
             uint32_t phase = 0;
             int pi = 0, prefetched = -1;
-            for (long long t = blockIdx.x; t < total_tiles; t += gridDim.x) {
-                const Item it = locate(descs, ndesc, t, pi);
+            int bkey = -1;          // (element, channel block) of the resident U
+            uint32_t bphase = 0;
+            for (long long t = t_lo; t < t_hi; t += t_step) {
+                const Item it = locate_item<RESB>(descs, ndesc, t, pi);
                 const GemmDesc& d = descs[pi];
                 if (prefetched != pi) {
                     tma_prefetch_desc(&d.tmA);
@@ -216,6 +253,20 @@ __device__ __forceinline__ void gemm_body(const GemmDesc* __restrict__ descs, in
                     prefetched = pi;
                 }
                 bool ok = true;
+                if constexpr (RESB) {
+                    const int key = it.e * d.n_blocks + it.nb;
+                    if (key != bkey) {
+                        // replace the resident U once the MMAs reading it are done
+                        if (bkey >= 0) {
+                            if (!mbar_wait(bempty, bphase, abort_flag, err, ERR_SITE_EMPTY)) break;
+                            bphase ^= 1u;
+                        }
+                        mbar_arrive_expect_tx(bfull, static_cast<uint32_t>(d.k_blocks) * Cfg::kTileB);
+                        for (int kb = 0; kb < d.k_blocks; ++kb)
+                            tma_load_4d(sB + kb * Cfg::kTileB, &d.tmB, bfull, 0, it.nb * (BN / 8), kb * 8, it.e);
+                        bkey = key;
+                    }
+                }
                 for (int kb = 0; kb < d.k_blocks; ++kb) {
                     if (!mbar_wait(&empty[stage], phase ^ 1u, abort_flag, err, ERR_SITE_EMPTY)) {
                         ok = false;
@@ -225,7 +276,8 @@ __device__ __forceinline__ void gemm_body(const GemmDesc* __restrict__ descs, in
                     // V: dropped from L2 by its last reader (the last N block)
                     tma_load_4d_hint(sA + stage * kTileABytes, &d.tmA, &full[stage], 0, it.mb * (kBM / 8), kb * 8, it.e,
                                      it.nb == d.n_blocks - 1 ? drop : keep_as_is);
-                    tma_load_4d(sB + stage * Cfg::kTileB, &d.tmB, &full[stage], 0, it.nb * (BN / 8), kb * 8, it.e);
+                    if constexpr (!RESB)
+                        tma_load_4d(sB + stage * Cfg::kTileB, &d.tmB, &full[stage], 0, it.nb * (BN / 8), kb * 8, it.e);
                     if (++stage == S) {
                         stage = 0;
                         phase ^= 1u;
@@ -241,10 +293,20 @@ __device__ __forceinline__ void gemm_body(const GemmDesc* __restrict__ descs, in
             int acc = 0;
             uint32_t acc_phase = 0;
             int pi = 0;
-            for (long long t = blockIdx.x; t < total_tiles; t += gridDim.x) {
-                locate(descs, ndesc, t, pi);
+            int bkey = -1;
+            uint32_t bphase = 0;
+            for (long long t = t_lo; t < t_hi; t += t_step) {
+                const Item it = locate_item<RESB>(descs, ndesc, t, pi);
                 const int k_blocks = descs[pi].k_blocks;
                 if (!mbar_wait(&tempty[acc], acc_phase ^ 1u, abort_flag, err, ERR_SITE_TMEM_EMPTY)) break;
+                if constexpr (RESB) {
+                    const int key = it.e * descs[0].n_blocks + it.nb;
+                    if (key != bkey) {
+                        if (!mbar_wait(bfull, bphase, abort_flag, err, ERR_SITE_FULL)) break;
+                        bphase ^= 1u;
+                        bkey = key;
+                    }
+                }
                 tc_fence_after();
                 const uint32_t d_tmem = tmem_base + static_cast<uint32_t>(acc * BN);
                 bool ok = true;
@@ -255,7 +317,7 @@ __device__ __forceinline__ void gemm_body(const GemmDesc* __restrict__ descs, in
                     }
                     tc_fence_after();
                     const uint32_t a_base = smem_u32(sA + stage * kTileABytes);
-                    const uint32_t b_base = smem_u32(sB + stage * Cfg::kTileB);
+                    const uint32_t b_base = smem_u32(sB + (RESB ? kb : stage) * Cfg::kTileB);
                     // K = 16 per MMA = 2 granules: core matrices at +0 and +LBO
 #pragma unroll
                     for (int k = 0; k < kBK / 16; ++k) {
@@ -271,6 +333,14 @@ __device__ __forceinline__ void gemm_body(const GemmDesc* __restrict__ descs, in
                 }
                 if (!ok) break;
                 tc_commit(&tfull[acc]);
+                if constexpr (RESB) {
+                    // the next item reads another U block: free this one when
+                    // the MMAs issued so far are done
+                    if (t + 1 < t_hi) {
+                        const Item nx = locate_resb(descs[0], t + 1);
+                        if (nx.e * descs[0].n_blocks + nx.nb != bkey) tc_commit(bempty);
+                    }
+                }
                 if (++acc == 2) {
                     acc = 0;
                     acc_phase ^= 1u;
@@ -289,8 +359,8 @@ __device__ __forceinline__ void gemm_body(const GemmDesc* __restrict__ descs, in
         int acc = 0;
         uint32_t acc_phase = 0;
         int pi = 0;
-        for (long long t = blockIdx.x; t < total_tiles; t += gridDim.x) {
-            const Item it = locate(descs, ndesc, t, pi);
+        for (long long t = t_lo; t < t_hi; t += t_step) {
+            const Item it = locate_item<RESB>(descs, ndesc, t, pi);
             const GemmDesc& d = descs[pi];
             MT* Mw = static_cast<MT*>(d.Mw);
             const long long P = d.P;
@@ -377,24 +447,29 @@ __device__ __forceinline__ void gemm_body(const GemmDesc* __restrict__ descs, in
     }
 }
 
-template <int BN, bool BF16, class MT>
+template <int BN, bool BF16, class MT, bool RESB>
 __global__ void __launch_bounds__(kGemmThreads, 1) wino_gemm_kernel(const __grid_constant__ GemmDesc d, DevErr* err) {
-    gemm_body<BN, BF16, MT>(&d, 1, d.tiles, err);
+    gemm_body<BN, BF16, MT, RESB>(&d, 1, d.tiles, err);
 }
 
 template <int BN, bool BF16, class MT>
 __global__ void __launch_bounds__(kGemmThreads, 1)
     wino_gemm_grouped(const GemmDesc* __restrict__ descs, int ndesc, long long total_tiles, DevErr* err) {
-    gemm_body<BN, BF16, MT>(descs, ndesc, total_tiles, err);
+    gemm_body<BN, BF16, MT, false>(descs, ndesc, total_tiles, err);
+}
+
+template <int BN, bool BF16, class MT, bool RESB>
+cudaError_t gemm_launch_r(const GemmDesc& d, int grid, DevErr* err, cudaStream_t s) {
+    using Cfg = GemmCfg<BN, RESB>;
+    auto kern = wino_gemm_kernel<BN, BF16, MT, RESB>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, Cfg::kSmemRow);
+    if (e != cudaSuccess) return e;
+    return launch_pdl(kern, dim3(grid), dim3(kGemmThreads), d.m_row ? Cfg::kSmemRow : Cfg::kSmem, s, d, err);
 }
 
 template <int BN, bool BF16, class MT>
 cudaError_t gemm_launch(const GemmDesc& d, int grid, DevErr* err, cudaStream_t s) {
-    auto kern = wino_gemm_kernel<BN, BF16, MT>;
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, GemmCfg<BN>::kSmemRow);
-    if (e != cudaSuccess) return e;
-    return launch_pdl(kern, dim3(grid), dim3(kGemmThreads), d.m_row ? GemmCfg<BN>::kSmemRow : GemmCfg<BN>::kSmem, s, d,
-                      err);
+    return d.resb ? gemm_launch_r<BN, BF16, MT, true>(d, grid, err, s) : gemm_launch_r<BN, BF16, MT, false>(d, grid, err, s);
 }
 
 template <int BN, bool BF16, class MT>
@@ -488,6 +563,7 @@ cudaError_t make_gemm_desc(GemmDesc& d, OpType op, int E, long long P, int K, in
     d.v_cg = Cp / 8;
     d.v_pp = static_cast<int>(round_rows(P));
     d.discard_v = 0;
+    d.resb = 0;      // plan_gemm decides for single launches; grouped ones hand out items round robin
     d.m_blocks = static_cast<int>((P + kBM - 1) / kBM);
     d.n_blocks = (K + bn - 1) / bn;
     d.k_blocks = (Cp + kBK - 1) / kBK;
@@ -532,6 +608,14 @@ cudaError_t plan_gemm(GemmPlan& gp, OpType op, int E, long long P, int K, int Kp
     // WG_CONV2D_KEEP_WORKSPACE=1 keeps it (to read the workspace back)
     const char* keep_ws = std::getenv("WG_CONV2D_KEEP_WORKSPACE");
     gp.desc.discard_v = gp.desc.n_blocks == 1 && !(keep_ws && std::atoi(keep_ws) != 0);
+    // U block of one (element, channel block) within the resident budget: it
+    // stays in shared memory over consecutive tile blocks instead of being
+    // reloaded from L2 for every work item (32 x 256 x 56^2 -> 256: 226 of
+    // the 339 MB of operand loads); WG_CONV2D_GEMM_RESIDENT_U=0 turns it off
+    const char* res = std::getenv("WG_CONV2D_GEMM_RESIDENT_U");
+    gp.desc.resb = !(res && res[0] == '0') &&
+                   static_cast<long long>(gp.desc.k_blocks) * bn * kBK * 2 <= kResBBytes &&
+                   gp.desc.tiles >= num_sms;
     gp.op = op;
     gp.bn = bn;
     gp.mt = mt;

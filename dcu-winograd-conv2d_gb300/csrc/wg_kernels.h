@@ -146,6 +146,7 @@ struct alignas(64) GemmDesc {
     // dirty lines are never written back to HBM
     const void* V;
     int v_cg, v_pp, discard_v;
+    int resb;            // single launches: U block resident in shared memory, contiguous item ranges per CTA
     long long tile_begin;
     long long tiles;     // E * m_blocks * n_blocks
 };
