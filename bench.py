@@ -601,29 +601,44 @@ def our_arm(args):
     if args.workload == "cfg2" and not args.nhwc and world == 1:
         f2x3 = f2x3_paths(wg, torch, xs, ys, wt, (n, c, h, w, k), sptr, device, reps, pk, pk_kind)
 
-    # end to end through the host-buffer entry point
+    # end to end through the host-buffer entry points: every step copies its
+    # input in from pinned host memory and its output back out
     e2e = None
     if not args.no_e2e:
-        hin = torch.empty(tuple(xs[0].shape), dtype=torch.float16).pin_memory()
-        hin.copy_(xs[0].cpu())
-        hout = torch.empty(tuple(ys[0].shape), dtype=torch.float16).pin_memory()
+        hins = [torch.empty(tuple(xs[0].shape), dtype=torch.float16).pin_memory() for _ in range(2)]
+        for hb, src in zip(hins, xs[:2]):
+            hb.copy_(src.cpu())
+        houts = [torch.empty(tuple(ys[0].shape), dtype=torch.float16).pin_memory() for _ in range(2)]
         e_steps = max(3, min(args.steps, 20))
+        ins = [hins[i % 2].data_ptr() for i in range(e_steps)]
+        outs = [houts[i % 2].data_ptr() for i in range(e_steps)]
         for i in range(2):
-            ops[0].host(hin.data_ptr(), hout.data_ptr(), sptr)
+            ops[0].host(ins[i], outs[i], sptr)
+        ops[0].host_steps(ins[:3], outs[:3], sptr)
         torch.cuda.synchronize(device)
-        if dist:
-            dist.barrier()
-        t0 = time.perf_counter()
-        for i in range(e_steps):
-            ops[0].host(hin.data_ptr(), hout.data_ptr(), sptr)
-        el = time.perf_counter() - t0
-        if dist:
-            tt = torch.tensor([el], device=device)
-            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-            el = float(tt.item())
+
+        def wall(fn):
+            if dist:
+                dist.barrier()
+            t0 = time.perf_counter()
+            fn()
+            el = time.perf_counter() - t0
+            if dist:
+                tt = torch.tensor([el], device=device)
+                dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+                el = float(tt.item())
+            return el
+
+        # one pipelined call over the e_steps batches (conv2d_fp16_host_steps)
+        el = wall(lambda: ops[0].host_steps(ins, outs, sptr))
+        # one blocking call per batch (conv2d_fp16_host)
+        el1 = wall(lambda: [ops[0].host(ins[i], outs[i], sptr) for i in range(e_steps)])
         e2e = {"value": world * flops * e_steps / el / 1e12, "unit": "TFLOP/s", "h2d_bytes_per_step": in_bytes,
                "d2h_bytes_per_step": out_bytes, "ms_per_step": el / e_steps * 1e3, "steps": e_steps,
-               "path": "conv2d_fp16_host (pinned host in/out, stream sync per call)"}
+               "path": "conv2d_fp16_host_steps: consecutive pinned host batches in one call, each copied in and "
+                       "out in full, copies of consecutive batches overlapping",
+               "per_call": {"value": world * flops * e_steps / el1 / 1e12, "ms_per_step": el1 / e_steps * 1e3,
+                            "path": "conv2d_fp16_host: one blocking call per batch (stream sync per call)"}}
 
     # CPU baseline on the host cores (rank 0 of a 1-GPU run only)
     cpu = None

@@ -46,7 +46,7 @@ class Options(ctypes.Structure):
 # every symbol include/conv2d.h declares
 EXPORTS = [
     "getParamsize", "getkernelInfo", "conv2d_fp16", "wg_getParamsize", "wg_getkernelInfo",
-    "conv2d_options_default", "getkernelInfo_ex", "conv2d_fp16_ex", "conv2d_fp16_host",
+    "conv2d_options_default", "getkernelInfo_ex", "conv2d_fp16_ex", "conv2d_fp16_host", "conv2d_fp16_host_steps",
     "conv2d_refresh_filter", "conv2d_destroy", "conv2d_get_algo", "conv2d_workspace_bytes",
     "conv2d_launches_per_call", "conv2d_check_device", "conv2d_last_error", "conv2d_last_error_message",
     "conv2d_status_string", "conv2d_select_reference", "conv2d_copy_to_host", "conv2d_fp16_timed",
@@ -96,6 +96,7 @@ def lib():
         L.conv2d_fp16.restype = None
         L.conv2d_fp16_ex.argtypes = [vp, vp]
         L.conv2d_fp16_host.argtypes = [vp, vp, vp, vp]
+        L.conv2d_fp16_host_steps.argtypes = [vp, ctypes.c_int, ctypes.POINTER(vp), ctypes.POINTER(vp), vp]
         L.conv2d_refresh_filter.argtypes = [vp, vp]
         L.conv2d_destroy.argtypes = [vp]
         L.conv2d_get_algo.argtypes = [vp]
@@ -189,6 +190,12 @@ class Conv2d:
     def host(self, host_in: int, host_out: int, stream: int | None = None):
         _check(lib().conv2d_fp16_host(self.ptr, ctypes.c_void_p(host_in), ctypes.c_void_p(host_out),
                                       ctypes.c_void_p(stream or 0)))
+
+    def host_steps(self, host_ins, host_outs, stream: int | None = None):
+        """Consecutive host batches through one pipelined call."""
+        n = len(host_ins)
+        _check(lib().conv2d_fp16_host_steps(self.ptr, n, (ctypes.c_void_p * n)(*host_ins),
+                                            (ctypes.c_void_p * n)(*host_outs), ctypes.c_void_p(stream or 0)))
 
     def timed(self, stream: int | None = None, max_kernels: int = 64):
         """One call; per-kernel durations in ms (CUDA events on the stream)."""

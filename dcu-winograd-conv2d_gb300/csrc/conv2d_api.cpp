@@ -473,12 +473,7 @@ const GemmPlan* Plan::host_gemm_for(int nc) {
 // the copies run and the first copies start at once, while a graph launch
 // front-loads its set-up (on the 32 x 256 x 56^2 layer: 413-418 us per call
 // queued directly, 434-437 us replayed).
-int Plan::run_host(const void* host_in, void* host_out, cudaStream_t s) {
-    DeviceGuard dg(device);
-    if (!filter_ready || opt.filter_policy == 1) {
-        int st = filter(s);
-        if (st) return st;
-    }
+int Plan::host_setup() {
     if (!host_in_stream) {
         if (cudaStreamCreateWithFlags(&host_in_stream, cudaStreamNonBlocking) != cudaSuccess ||
             cudaStreamCreateWithFlags(&host_out_stream, cudaStreamNonBlocking) != cudaSuccess ||
@@ -488,6 +483,16 @@ int Plan::run_host(const void* host_in, void* host_out, cudaStream_t s) {
             if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess)
                 return fail(CONV2D_ERR_CUDA, "event creation failed");
     }
+    return CONV2D_OK;
+}
+
+int Plan::run_host(const void* host_in, void* host_out, cudaStream_t s) {
+    DeviceGuard dg(device);
+    if (!filter_ready || opt.filter_policy == 1) {
+        int st = filter(s);
+        if (st) return st;
+    }
+    if (const int st = host_setup()) return st;
     if (host_graph && (graph_in != host_in || graph_out != host_out)) {
         cudaGraphExecDestroy(host_graph);
         host_graph = nullptr;
@@ -495,7 +500,7 @@ int Plan::run_host(const void* host_in, void* host_out, cudaStream_t s) {
     const bool use_graph = env_int("WG_CONV2D_HOST_GRAPH", 0) != 0;
     if (use_graph && !host_graph &&
         cudaStreamBeginCapture(host_cap_stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
-        const int st = enqueue_host(host_in, host_out, host_cap_stream);
+        const int st = enqueue_host(&host_in, &host_out, 1, host_cap_stream);
         cudaGraph_t graph = nullptr;
         const cudaError_t ce = cudaStreamEndCapture(host_cap_stream, &graph);
         if (st == CONV2D_OK && ce == cudaSuccess && graph &&
@@ -512,7 +517,7 @@ int Plan::run_host(const void* host_in, void* host_out, cudaStream_t s) {
         const cudaError_t ce = cudaGraphLaunch(host_graph, s);
         if (ce != cudaSuccess) return cuda_fail(ce, "host pipeline graph launch");
     } else {
-        const int st = enqueue_host(host_in, host_out, s);
+        const int st = enqueue_host(&host_in, &host_out, 1, s);
         if (st) return st;
     }
     const cudaError_t ce = cudaStreamSynchronize(s);
@@ -520,7 +525,26 @@ int Plan::run_host(const void* host_in, void* host_out, cudaStream_t s) {
     return CONV2D_OK;
 }
 
-int Plan::enqueue_host(const void* host_in, void* host_out, cudaStream_t s) {
+int Plan::run_host_steps(const void* const* host_in, void* const* host_out, int steps, cudaStream_t s) {
+    DeviceGuard dg(device);
+    if (!filter_ready || opt.filter_policy == 1) {
+        int st = filter(s);
+        if (st) return st;
+    }
+    if (const int st = host_setup()) return st;
+    if (const int st = enqueue_host(host_in, host_out, steps, s)) return st;
+    const cudaError_t ce = cudaStreamSynchronize(s);
+    if (ce != cudaSuccess) return cuda_fail(ce, "stream sync");
+    return CONV2D_OK;
+}
+
+// Steps run one after another through the same device buffers; chunk i of a
+// step is ordered only against chunk i of the step before: its input copy
+// after that step's compute of chunk i (which read the same input rows), its
+// compute after that step's output copy of chunk i (which read the same output
+// rows).  So the output copies of one step overlap the input copies of the
+// next, and the link carries both directions at once across step boundaries.
+int Plan::enqueue_host(const void* const* host_in, void* const* host_out, int steps, cudaStream_t s) {
     const int n = static_cast<int>(prob.n);
     const long long in_img_b = static_cast<long long>(g.c) * g.h * g.w * 2;
     const long long out_img_b = static_cast<long long>(g.k) * g.oh * g.ow * 2;
@@ -529,9 +553,10 @@ int Plan::enqueue_host(const void* host_in, void* host_out, cudaStream_t s) {
     // the non-fused workspace holds chunk_n images: a host chunk runs as
     // ranges of at most that many
     const int cap = single_kernel() ? n : chunk_n;
-    cudaEvent_t* ev_in = host_ev;                     // [kMaxHostChunks]
-    cudaEvent_t* ev_done = host_ev + kMaxHostChunks;  // [kMaxHostChunks]
-    cudaEvent_t ev_start = host_ev[2 * kMaxHostChunks], ev_end = host_ev[2 * kMaxHostChunks + 1];
+    cudaEvent_t* ev_in = host_ev;                         // [kMaxHostChunks]
+    cudaEvent_t* ev_done = host_ev + kMaxHostChunks;      // [kMaxHostChunks]
+    cudaEvent_t* ev_out = host_ev + 2 * kMaxHostChunks;   // [kMaxHostChunks]
+    cudaEvent_t ev_start = host_ev[3 * kMaxHostChunks], ev_end = host_ev[3 * kMaxHostChunks + 1];
     // the copies must not overwrite the input before earlier work on s is done
     cudaEventRecord(ev_start, s);
     cudaStreamWaitEvent(host_in_stream, ev_start, 0);
@@ -539,34 +564,42 @@ int Plan::enqueue_host(const void* host_in, void* host_out, cudaStream_t s) {
     int first[kMaxHostChunks + 1];
     first[0] = 0;
     for (int i = 0; i < nch; ++i) first[i + 1] = first[i] + sizes[i];
-    auto copy_in = [&](int i) {
+    // queue positions q = step * nch + chunk
+    auto copy_in = [&](int q) {
+        const int st = q / nch, i = q % nch;
+        if (st > 0) cudaStreamWaitEvent(host_in_stream, ev_done[i], 0);   // step st-1 read these rows
         const cudaError_t ce = cudaMemcpyAsync(static_cast<char*>(prob.in) + first[i] * in_img_b,
-                                               static_cast<const char*>(host_in) + first[i] * in_img_b,
+                                               static_cast<const char*>(host_in[st]) + first[i] * in_img_b,
                                                sizes[i] * in_img_b, cudaMemcpyHostToDevice, host_in_stream);
         cudaEventRecord(ev_in[i], host_in_stream);
         return ce;
     };
-    // input copies are queued three chunks ahead of the chunk being queued
-    constexpr int kAhead = 3;
-    for (int i = 0; i < std::min(kAhead, nch); ++i)
-        if (cudaError_t ce = copy_in(i); ce != cudaSuccess) return cuda_fail(ce, "input copy");
-    for (int i = 0, n0 = 0; i < nch; n0 += sizes[i], ++i) {
-        cudaError_t ce = i + kAhead < nch ? copy_in(i + kAhead) : cudaSuccess;
+    // input copies are queued up to three chunks ahead, never a whole step
+    // (each chunk's events are reused by the next step)
+    const int ahead = std::min(3, nch - 1), total = steps * nch;
+    for (int q = 0; q < std::min(ahead, total); ++q)
+        if (cudaError_t ce = copy_in(q); ce != cudaSuccess) return cuda_fail(ce, "input copy");
+    for (int q = 0; q < total; ++q) {
+        const int st = q / nch, i = q % nch, n0 = first[i];
+        cudaError_t ce = q + ahead < total && ahead > 0 ? copy_in(q + ahead) : cudaSuccess;
+        if (ahead == 0) ce = copy_in(q);
         if (ce != cudaSuccess) return cuda_fail(ce, "input copy");
         cudaStreamWaitEvent(s, ev_in[i], 0);
+        if (st > 0) cudaStreamWaitEvent(s, ev_out[i], 0);   // step st-1's output copy read these rows
         for (int r0 = n0; r0 < n0 + sizes[i]; r0 += cap) {
             const int nc = std::min(cap, n0 + sizes[i] - r0);
             const GemmPlan* gp = nullptr;
             if (!single_kernel() && !(gp = host_gemm_for(nc))) return fail(CONV2D_ERR_CUDA, "GEMM plan (host chunks) failed");
-            const int st = run_range(r0, nc, gp, s);
-            if (st) return st;
+            const int rs = run_range(r0, nc, gp, s);
+            if (rs) return rs;
         }
         cudaEventRecord(ev_done[i], s);
         cudaStreamWaitEvent(host_out_stream, ev_done[i], 0);
-        ce = cudaMemcpyAsync(static_cast<char*>(host_out) + n0 * out_img_b,
+        ce = cudaMemcpyAsync(static_cast<char*>(host_out[st]) + n0 * out_img_b,
                              static_cast<const char*>(prob.out) + n0 * out_img_b, sizes[i] * out_img_b,
                              cudaMemcpyDeviceToHost, host_out_stream);
         if (ce != cudaSuccess) return cuda_fail(ce, "output copy");
+        cudaEventRecord(ev_out[i], host_out_stream);
     }
     cudaEventRecord(ev_end, host_out_stream);
     cudaStreamWaitEvent(s, ev_end, 0);
@@ -677,6 +710,16 @@ int conv2d_fp16_host(const void* param_ptr, const void* host_in, void* host_out,
     if (!pl) return fail(CONV2D_ERR_INVALID, "param blob not set up by getkernelInfo");
     if (!host_in || !host_out) return fail(CONV2D_ERR_INVALID, "null host buffer");
     return pl->run_host(host_in, host_out, static_cast<cudaStream_t>(stream));
+}
+
+int conv2d_fp16_host_steps(const void* param_ptr, int steps, const void* const* host_in, void* const* host_out,
+                           void* stream) {
+    Plan* pl = plan_of(param_ptr);
+    if (!pl) return fail(CONV2D_ERR_INVALID, "param blob not set up by getkernelInfo");
+    if (steps <= 0 || !host_in || !host_out) return fail(CONV2D_ERR_INVALID, "bad step count or null buffer list");
+    for (int i = 0; i < steps; ++i)
+        if (!host_in[i] || !host_out[i]) return fail(CONV2D_ERR_INVALID, "null host buffer");
+    return pl->run_host_steps(host_in, host_out, steps, static_cast<cudaStream_t>(stream));
 }
 
 int conv2d_refresh_filter(const void* param_ptr, void* stream) {

@@ -73,7 +73,8 @@ struct Plan {
     const void* graph_in = nullptr;
     void* graph_out = nullptr;
     static constexpr int kMaxHostChunks = 16;
-    cudaEvent_t host_ev[2 * kMaxHostChunks + 2] = {};
+    // per chunk: input copied, computed, output copied; start and end
+    cudaEvent_t host_ev[3 * kMaxHostChunks + 2] = {};
 
     // one kernel per call, no Winograd-domain workspace
     bool single_kernel() const { return algo == CONV2D_ALGO_2X3_FUSED || algo == CONV2D_ALGO_4X3_ROW; }
@@ -86,8 +87,12 @@ struct Plan {
     int run_range(int n0, int nc, const GemmPlan* gp, cudaStream_t s);
     // host input -> device -> host output, copies overlapped with compute
     int run_host(const void* host_in, void* host_out, cudaStream_t s);
-    // queue the host-buffer pipeline with cs as the compute stream
-    int enqueue_host(const void* host_in, void* host_out, cudaStream_t cs);
+    // `steps` host batches one after another, copies of consecutive batches
+    // overlapping; waits for the stream at the end
+    int run_host_steps(const void* const* host_in, void* const* host_out, int steps, cudaStream_t s);
+    // queue the host-buffer pipeline of `steps` batches with cs as the compute stream
+    int enqueue_host(const void* const* host_in, void* const* host_out, int steps, cudaStream_t cs);
+    int host_setup();
     // GEMM plan for a host chunk of nc images (made once per size), or null
     const GemmPlan* host_gemm_for(int nc);
     void mark(cudaStream_t s);

@@ -159,6 +159,16 @@ int conv2d_fp16_ex(const void* param_ptr, void* stream);
  * streams); with pinned host memory the copies run at full link speed. */
 int conv2d_fp16_host(const void* param_ptr, const void* host_in, void* host_out, void* stream);
 
+/* `steps` end-to-end calls of the same layer on consecutive host batches
+ * (host_in[i] -> host_out[i], the same pointers may repeat), queued as one
+ * pipeline: chunk j of batch i waits only for chunk j of batch i-1, so the
+ * output copies of one batch overlap the input copies of the next and the
+ * host link carries both directions at once.  Waits for the stream at the
+ * end.  Every batch is copied in and out in full; results are those of
+ * `steps` conv2d_fp16_host calls. */
+int conv2d_fp16_host_steps(const void* param_ptr, int steps, const void* const* host_in, void* const* host_out,
+                           void* stream);
+
 /* Re-run the filter transform (after the caller changed the weights in place). */
 int conv2d_refresh_filter(const void* param_ptr, void* stream);
 

@@ -444,6 +444,37 @@ def test_nhwc_refuses_channels_not_a_multiple_of_8(wg):
     assert ei.value.status == wg.ERR_UNSUPPORTED
 
 
+@pytest.mark.parametrize("sizes", ["6", "2,2,2", "1,1,1,1,1,1"])
+@pytest.mark.parametrize("algo", [0, 1, 4])
+def test_host_steps_match_single_host_calls(wg, monkeypatch, algo, sizes):
+    """Consecutive host batches through one pipelined call (chunk i of batch
+    b ordered only against chunk i of batch b-1) give each batch the output of
+    its own conv2d_fp16_host call, bit for bit, with 1, 3 and 6 image chunks."""
+    monkeypatch.setenv("WG_CONV2D_HOST_SIZES", sizes)
+    n, c, h, k = 6, 40, 60, 48
+    wt = O.uniform_inputs(5, n, c, h, h, k)[1]
+    xs = [O.uniform_inputs(100 + i, n, c, h, h, k)[0] for i in range(3)]
+    xt = torch.empty((n, c, h, h), dtype=torch.float16, device="cuda")
+    wtt = torch.from_numpy(wt).cuda()
+    y = torch.empty((n, k, h, h), dtype=torch.float16, device="cuda")
+    op = wg.Conv2d(wg.make_problem(xt.data_ptr(), wtt.data_ptr(), y.data_ptr(), n, c, h, h, k), opts_for(wg, algo))
+    s = torch.cuda.current_stream().cuda_stream
+    hins = [torch.from_numpy(x).pin_memory() for x in xs]
+    single = []
+    for hin in hins:
+        hout = torch.empty((n, k, h, h), dtype=torch.float16).pin_memory()
+        op.host(hin.data_ptr(), hout.data_ptr(), s)
+        single.append(hout.numpy().copy())
+    houts = [torch.full((n, k, h, h), float("nan"), dtype=torch.float16).pin_memory() for _ in xs]
+    op.host_steps([hi.data_ptr() for hi in hins], [ho.data_ptr() for ho in houts], s)
+    assert op.check_device()[0] == wg.OK
+    for a, b in zip(single, houts):
+        assert np.array_equal(a.view(np.uint16), b.numpy().view(np.uint16))
+    _, r64 = O.conv2d_direct(xs[2], wt, nthreads=8)
+    assert O.rel_errors(houts[2].numpy(), r64)[0] <= TOL[algo_m(algo)]
+    op.destroy()
+
+
 @pytest.mark.parametrize("algo", [0, 1, 2, 4])
 def test_host_chunks_of_unaligned_images(wg, algo):
     """Images of 1,202,850 bytes: every host chunk after the first starts off
