@@ -677,6 +677,15 @@ def our_arm(args):
             served, _ = serving_run(wg, torch, device, args.line_requests, [0.9])
         except Exception as e:
             served = {"error": f"{type(e).__name__}: {e}"[:300]}
+    precision = None
+    if args.workload == "cfg2" and world == 1 and not args.no_precision:
+        for op in ops:
+            op.destroy()
+        ops = []
+        try:
+            precision = precision_line(wg, torch, device)
+        except Exception as e:
+            precision = {"error": f"{type(e).__name__}: {e}"[:300]}
     served_vs_percall = None
     if batched or served:
         served_vs_percall = {
@@ -715,6 +724,7 @@ def our_arm(args):
         "served_vs_percall": served_vs_percall,
         "batched": batched,
         "served": served,
+        "precision": precision,
         "clocks": clocks,
         "gpu_launches": args.steps * launches_per_call,
     }
@@ -885,6 +895,49 @@ def precision_arm(args):
     print(json.dumps({"study": "F(4x3) precision vs FP64 direct convolution", "shape": [n, c, h, h, k],
                       "metric": "max/mean of |y-ref|/max(|ref|,rms(ref))", "rows": rows}), flush=True)
     return 0
+
+
+def precision_line(wg, torch, device, images=2):
+    """The precision study in compact form for the default line: `images`
+    images of the N=32, C=512, H=W=28, K=512 shape, seeded N(0,1) inputs and
+    the same with 1% of entries x64, filters N(0, 1/sqrt(9C)); max / mean
+    relative error against an FP64 direct convolution (numpy, every output
+    channel) for the default F(4x3) path with and without per-tile scaling,
+    F(4x3) with bf16 operands and with the reference's points, and F(2x3)."""
+    import numpy as np
+    n, c, h, k = images, 512, 28, 512
+    gen = torch.Generator().manual_seed(2027)
+    w = torch.randn((k, c, 3, 3), generator=gen, dtype=torch.float64) / math.sqrt(9 * c)
+    wt16 = w.half()
+    w64 = wt16.double().numpy()
+    rows = []
+    t0 = time.time()
+    for dist in ("normal", "heavy"):
+        x = torch.randn((n, c, h, h), generator=gen, dtype=torch.float64)
+        if dist == "heavy":
+            x = torch.where(torch.rand(x.shape, generator=gen, dtype=torch.float64) < 0.01, x * 64, x)
+        x16 = x.half()
+        xp = np.zeros((n, c, h + 2, h + 2))
+        xp[:, :, 1:h + 1, 1:h + 1] = x16.double().numpy()
+        ref = np.zeros((n, k, h, h))
+        for r in range(3):
+            for s_ in range(3):
+                ref += np.einsum("kc,nchw->nkhw", w64[:, :, r, s_], xp[:, :, r:r + h, s_:s_ + h], optimize=True)
+        rms = math.sqrt(float(np.mean(ref * ref)))
+        xd, wd = x16.to(device), wt16.to(device)
+        for algo, bf16, scaling, points in ((0, 0, 0, 0), (0, 0, 1, 0), (0, 1, 0, 0), (0, 0, 0, 1), (1, 0, 0, 0)):
+            opts = wg.default_options(algo=algo, operand_bf16=bf16, tile_scaling=scaling, f4_points=points)
+            y, op = wg.conv2d_torch(xd, wd, 1, 1, opts)
+            torch.cuda.synchronize()
+            rel = np.abs(y.double().cpu().numpy() - ref) / np.maximum(np.abs(ref), rms)
+            rows.append({"input": dist, "algo": wg.ALGO_NAMES[algo],
+                         "points": ("reference 0,+-1,+-2" if points else "0,+-1,1/2,-2") if algo == 0 else "-",
+                         "operands": "bf16" if bf16 else "fp16", "tile_scaling": bool(scaling),
+                         "max": float(rel.max()), "mean": float(rel.mean())})
+            op.destroy()
+    return {"shape": [n, c, h, h, k], "against": "FP64 direct convolution, every output value",
+            "measure": "|y - ref| / max(|ref|, rms(ref))", "bound": 2e-2, "rows": rows,
+            "seconds": round(time.time() - t0, 1)}
 
 
 def serve_layers(seed=20261203):
@@ -1080,6 +1133,8 @@ def main():
     ap.add_argument("--nhwc", action="store_true", help="channels-last input and output tensors")
     ap.add_argument("--m-fp32", action="store_true", help="F(4x3): store the GEMM result M in fp32 instead of 24 bits")
     ap.add_argument("--images", type=int, default=4, help="images of the precision study")
+    ap.add_argument("--no-precision", action="store_true",
+                    help="skip the default line's precision record (2 images of N=32 C=512 28x28 K=512)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
