@@ -1,5 +1,6 @@
-"""Full-size properties (the headline workloads, too large for the CPU oracle
-to check whole).
+"""Full-size checks of the headline workloads, too large for the CPU oracle to
+check whole: every output value against a float64 convolution on the GPU, and
+a scaling property.
 
 Scaling by two: with inputs on a 2^-8 grid in [-1, 1] every Winograd-domain
 value of the input side is a normal fp16 number or zero, and every rounding on
@@ -54,3 +55,30 @@ def test_doubling_the_input_doubles_the_output(wg, shape, algo):
     assert torch.equal(y2.float()[normal], twice[normal])
     if (~normal).any():
         assert float((y2.float()[~normal] - twice[~normal]).abs().max()) <= 2.0 ** -23
+
+
+def _rel_err_fp64(y, x, wt):
+    """max and mean of |y - ref| / max(|ref|, rms(ref)) over every output
+    value; ref is torch's float64 convolution (pad 1) of the same fp16 values
+    on the GPU, code that is not this library's."""
+    ref = torch.nn.functional.conv2d(x.double(), wt.double(), padding=1)
+    rms = ref.pow(2).mean().sqrt()
+    rel = (y.double() - ref).abs() / torch.maximum(ref.abs(), rms)
+    return float(rel.max()), float(rel.mean())
+
+
+@pytest.mark.parametrize("shape,algo", [(CFG2, 0), (CFG2, 1), (CFG2, 2), (CFG2, 4), (CFG3, 0), (CFG3, 1), (CFG3, 4)])
+def test_every_output_against_fp64(wg, shape, algo):
+    """The whole output tensor of each headline workload against an FP64
+    direct convolution of the same inputs (U[-1,1] input, N(0, 1/sqrt(9C))
+    filter), at the bounds the operator is held to: 1e-2 for F(2x3) (non-fused
+    and fused), 2e-2 for F(4x3) (non-fused and row)."""
+    n, c, h, w, k = shape
+    g = torch.Generator(device="cuda").manual_seed(7 + sum(shape) + algo)
+    x = (torch.rand((n, c, h, w), generator=g, device="cuda") * 2 - 1).half()
+    wt = (torch.randn((k, c, 3, 3), generator=g, device="cuda") / (3 * c ** 0.5)).half()
+    y = _conv(wg, x, wt, algo)
+    mx, mean = _rel_err_fp64(y, x, wt)
+    bound = 1e-2 if algo in (1, 2) else 2e-2
+    assert mx <= bound, (mx, mean)
+    assert mean <= bound / 5, (mx, mean)
