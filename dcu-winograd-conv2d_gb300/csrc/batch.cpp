@@ -14,6 +14,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <memory>
@@ -33,6 +34,7 @@ struct Batch {
     struct InGroup {
         Xform xf;
         OpType op;
+        int bn;    // GEMM tile of the chain this group starts
         const InDesc* descs;
         int n;
         long long blocks;
@@ -43,6 +45,7 @@ struct Batch {
         int bn;
         MType mt;
         OpType op;
+        Xform xf;
         const GemmDesc* descs;
         int n;
         long long tiles;
@@ -51,6 +54,7 @@ struct Batch {
     struct OutGroup {
         Xform xf;
         MType mt;
+        int bn;
         const OutDesc* descs;
         int n;
         long long blocks;
@@ -66,35 +70,87 @@ struct Batch {
     ~Batch() {
         if (graph) cudaGraphExecDestroy(graph);
         if (dev) cudaFree(dev);
+        for (int i = 0; i < kSides; ++i) {
+            if (side[i]) cudaStreamDestroy(side[i]);
+            if (join[i]) cudaEventDestroy(join[i]);
+        }
+        if (fork) cudaEventDestroy(fork);
+    }
+
+    // Independent branches of the graph: each chain of grouped launches (one
+    // per transform, or per transform and GEMM tile: its tile scales, input
+    // transforms, GEMMs and output transforms; bn 0 = every tile) and each
+    // problem run by its own kernel (row
+    // F(4x3), fused F(2x3)) is a unit; units go to kSides + 1 streams forked
+    // from the caller's, largest first to the least loaded, so that one
+    // branch's CTAs fill the others' tails.  Without side streams
+    // (WG_CONV2D_BATCH_BRANCH=0) the units run one after another on one stream.
+    static constexpr int kSides = 5;
+    cudaStream_t side[kSides] = {};
+    cudaEvent_t fork = nullptr, join[kSides] = {};
+    struct Unit {
+        Xform xf;      // chain: transform and GEMM tile
+        int bn;
+        int single;    // or the problem run by its own kernel (>= 0)
+        double flops;  // direct-convolution work
+        int stream;    // 0: the caller's stream, k: side[k - 1]
+    };
+    std::vector<Unit> units;
+
+    cudaError_t launch_chain(Xform xf, int bn, cudaStream_t s) {
+        cudaError_t e = cudaSuccess;
+        for (int i : scaled) {
+            Plan& p = *plans[i];
+            if (p.xf == xf && (bn == 0 || p.gemm_full.bn == bn) &&
+                (e = launch_tile_scale(p.g, p.prob.in, p.scale, s)) != cudaSuccess)
+                return e;
+        }
+        for (const InGroup& g : in_groups)
+            if (g.xf == xf && g.bn == bn &&
+                (e = launch_input_transform_grouped(g.xf, g.op, g.descs, g.n, g.blocks, g.smem, g.scaled, err, s)) !=
+                    cudaSuccess)
+                return e;
+        for (const GemmGroup& g : gemm_groups)
+            if (g.xf == xf && (bn == 0 || g.bn == bn) &&
+                (e = launch_gemm_grouped(g.descs, g.n, g.tiles, g.op, g.mt, g.bn, g.grid, err, s)) != cudaSuccess)
+                return e;
+        for (const OutGroup& g : out_groups)
+            if (g.xf == xf && g.bn == bn &&
+                (e = launch_output_transform_grouped(g.xf, g.mt, g.descs, g.n, g.blocks, err, s)) != cudaSuccess)
+                return e;
+        return cudaSuccess;
+    }
+
+    cudaError_t launch_unit(const Unit& u, cudaStream_t s) {
+        return u.single >= 0 ? launch_single(u.single, s) : launch_chain(u.xf, u.bn, s);
     }
 
     cudaError_t launch_grouped(cudaStream_t s) {
         cudaError_t e = cudaSuccess;
-        for (int i : scaled) {
-            Plan& p = *plans[i];
-            if ((e = launch_tile_scale(p.g, p.prob.in, p.scale, s)) != cudaSuccess) return e;
+        if (!side[0]) {
+            for (const Unit& u : units)
+                if ((e = launch_unit(u, s)) != cudaSuccess) return e;
+            return cudaSuccess;
         }
-        for (const InGroup& g : in_groups)
-            if ((e = launch_input_transform_grouped(g.xf, g.op, g.descs, g.n, g.blocks, g.smem, g.scaled, err, s)) != cudaSuccess)
+        if ((e = cudaEventRecord(fork, s)) != cudaSuccess) return e;
+        for (int i = 0; i < kSides; ++i)
+            if ((e = cudaStreamWaitEvent(side[i], fork, 0)) != cudaSuccess) return e;
+        for (const Unit& u : units)
+            if ((e = launch_unit(u, u.stream ? side[u.stream - 1] : s)) != cudaSuccess) return e;
+        for (int i = 0; i < kSides; ++i)
+            if ((e = cudaEventRecord(join[i], side[i])) != cudaSuccess || (e = cudaStreamWaitEvent(s, join[i], 0)) != cudaSuccess)
                 return e;
-        for (const GemmGroup& g : gemm_groups)
-            if ((e = launch_gemm_grouped(g.descs, g.n, g.tiles, g.op, g.mt, g.bn, g.grid, err, s)) != cudaSuccess)
-                return e;
-        for (const OutGroup& g : out_groups)
-            if ((e = launch_output_transform_grouped(g.xf, g.mt, g.descs, g.n, g.blocks, err, s)) != cudaSuccess) return e;
-        for (int i : fused) {
-            Plan& p = *plans[i];
-            const void* x_end =
-                static_cast<const uint16_t*>(p.prob.in) + static_cast<long long>(p.prob.n) * p.g.c * p.g.h * p.g.w;
-            if (p.algo == CONV2D_ALGO_4X3_ROW) {
-                if ((e = launch_row4x3(p.row, p.prob.in, x_end, p.prob.out, static_cast<int>(p.prob.n), err, s)) !=
-                    cudaSuccess)
-                    return e;
-            } else if ((e = launch_fused2x3(p.fused, p.g, p.prob.in, x_end, p.prob.out, err, s)) != cudaSuccess) {
-                return e;
-            }
-        }
         return cudaSuccess;
+    }
+
+    // a problem run by its own kernel
+    cudaError_t launch_single(int i, cudaStream_t s) {
+        Plan& p = *plans[i];
+        const void* x_end =
+            static_cast<const uint16_t*>(p.prob.in) + static_cast<long long>(p.prob.n) * p.g.c * p.g.h * p.g.w;
+        if (p.algo == CONV2D_ALGO_4X3_ROW)
+            return launch_row4x3(p.row, p.prob.in, x_end, p.prob.out, static_cast<int>(p.prob.n), err, s);
+        return launch_fused2x3(p.fused, p.g, p.prob.in, x_end, p.prob.out, err, s);
     }
 };
 
@@ -124,8 +180,12 @@ int batch_create(const problem_t* problems, int count, const conv2d_options_t* o
         b->plans.push_back(std::move(p));
     }
     // group the problems and lay out their descriptors
-    std::map<std::pair<int, int>, std::vector<int>> in_keys, out_keys;        // (xform, op | M type) -> problems
-    std::map<std::tuple<int, int, int>, std::vector<int>> gemm_keys;          // (bn, M type, op) -> problems
+    // one chain of grouped launches per transform: input transform, GEMM
+    // and output transform groups of the same problems
+    std::map<std::tuple<int, int, int>, std::vector<int>> in_keys, out_keys;  // (xform, op | M type, bn) -> problems
+    const char* sb = std::getenv("WG_CONV2D_BATCH_SPLIT_BN");
+    const bool split_bn = sb && sb[0] == '1';
+    std::map<std::tuple<int, int, int, int>, std::vector<int>> gemm_keys;     // (bn, M type, op, xform) -> problems
     for (int i = 0; i < count; ++i) {
         Plan& p = *b->plans[i];
         if (p.single_kernel()) {
@@ -133,9 +193,12 @@ int batch_create(const problem_t* problems, int count, const conv2d_options_t* o
             continue;
         }
         if (p.scaling) b->scaled.push_back(i);
-        in_keys[{static_cast<int>(p.xf), static_cast<int>(p.op)}].push_back(i);
-        out_keys[{static_cast<int>(p.xf), static_cast<int>(p.mt)}].push_back(i);
-        gemm_keys[{p.gemm_full.bn, static_cast<int>(p.mt), static_cast<int>(p.op)}].push_back(i);
+        // WG_CONV2D_BATCH_SPLIT_BN=1: one chain per (transform, GEMM tile)
+        // instead of one per transform
+        const int cbn = split_bn ? p.gemm_full.bn : 0;
+        in_keys[{static_cast<int>(p.xf), static_cast<int>(p.op), cbn}].push_back(i);
+        out_keys[{static_cast<int>(p.xf), static_cast<int>(p.mt), cbn}].push_back(i);
+        gemm_keys[{p.gemm_full.bn, static_cast<int>(p.mt), static_cast<int>(p.op), static_cast<int>(p.xf)}].push_back(i);
     }
     std::vector<InDesc> in_descs;
     std::vector<OutDesc> out_descs;
@@ -146,8 +209,8 @@ int batch_create(const problem_t* problems, int count, const conv2d_options_t* o
         int extra;
         bool scaled;
     };
-    std::vector<std::pair<std::pair<int, int>, Range>> in_r, out_r;
-    std::vector<std::pair<std::tuple<int, int, int>, Range>> gemm_r;
+    std::vector<std::pair<std::tuple<int, int, int>, Range>> in_r, out_r;
+    std::vector<std::pair<std::tuple<int, int, int, int>, Range>> gemm_r;
     for (auto& kv : in_keys) {
         Range r{in_descs.size(), kv.second.size(), 0, 0, false};
         for (int i : kv.second) {
@@ -201,24 +264,62 @@ int batch_create(const problem_t* problems, int count, const conv2d_options_t* o
     if (!out_descs.empty()) cudaMemcpy(base + oO, out_descs.data(), out_descs.size() * sizeof(OutDesc), cudaMemcpyHostToDevice);
     int sms = b->plans[0]->num_sms;
     for (auto& kr : in_r)
-        b->in_groups.push_back({static_cast<Xform>(kr.first.first), static_cast<OpType>(kr.first.second),
-                                reinterpret_cast<const InDesc*>(base + oI) + kr.second.first,
+        b->in_groups.push_back({static_cast<Xform>(std::get<0>(kr.first)), static_cast<OpType>(std::get<1>(kr.first)),
+                                std::get<2>(kr.first), reinterpret_cast<const InDesc*>(base + oI) + kr.second.first,
                                 static_cast<int>(kr.second.n), kr.second.total, kr.second.extra, kr.second.scaled});
     for (auto& kr : gemm_r)
         b->gemm_groups.push_back({std::get<0>(kr.first), static_cast<MType>(std::get<1>(kr.first)),
-                                  static_cast<OpType>(std::get<2>(kr.first)),
+                                  static_cast<OpType>(std::get<2>(kr.first)), static_cast<Xform>(std::get<3>(kr.first)),
                                   reinterpret_cast<const GemmDesc*>(base + oG) + kr.second.first,
                                   static_cast<int>(kr.second.n), kr.second.total,
                                   static_cast<int>(std::min<long long>(kr.second.total, sms))});
     for (auto& kr : out_r)
-        b->out_groups.push_back({static_cast<Xform>(kr.first.first), static_cast<MType>(kr.first.second),
-                                 reinterpret_cast<const OutDesc*>(base + oO) + kr.second.first,
+        b->out_groups.push_back({static_cast<Xform>(std::get<0>(kr.first)), static_cast<MType>(std::get<1>(kr.first)),
+                                 std::get<2>(kr.first), reinterpret_cast<const OutDesc*>(base + oO) + kr.second.first,
                                  static_cast<int>(kr.second.n), kr.second.total});
     int single = 0;   // launches of the problems run by their own kernels
     for (int i : b->fused) single += b->plans[i]->launches;
     b->grouped_launches = static_cast<int>(b->scaled.size() + b->in_groups.size() + b->gemm_groups.size() +
                                            b->out_groups.size()) + single;
     if (cudaDeviceSynchronize() != cudaSuccess) return batch_fail(CONV2D_ERR_CUDA, "batch setup failed");
+    // work units (chains and single-kernel problems), largest first, each to
+    // the stream with the least direct-convolution work so far
+    auto flops = [&](int i) {
+        const Plan& p = *b->plans[i];
+        return 18.0 * p.prob.n * p.prob.k * p.g.oh * p.g.ow * p.prob.c;
+    };
+    for (const Batch::InGroup& g : b->in_groups) {
+        bool seen = false;   // one unit per chain, whatever its operand types
+        for (const Batch::Unit& v : b->units) seen = seen || (v.single < 0 && v.xf == g.xf && v.bn == g.bn);
+        if (seen) continue;
+        Batch::Unit u{g.xf, g.bn, -1, 0.0, 0};
+        for (int i = 0; i < count; ++i) {
+            const Plan& p = *b->plans[i];
+            if (!p.single_kernel() && p.xf == g.xf && (g.bn == 0 || p.gemm_full.bn == g.bn)) u.flops += flops(i);
+        }
+        b->units.push_back(u);
+    }
+    for (int i : b->fused) b->units.push_back({Xform::F2, 0, i, flops(i), 0});
+    std::stable_sort(b->units.begin(), b->units.end(),
+                     [](const Batch::Unit& x, const Batch::Unit& y) { return x.flops > y.flops; });
+    {
+        double load[Batch::kSides + 1] = {};
+        for (Batch::Unit& u : b->units) {
+            int best = 0;
+            for (int k = 1; k <= Batch::kSides; ++k)
+                if (load[k] < load[best]) best = k;
+            u.stream = best;
+            load[best] += u.flops;
+        }
+    }
+    const char* br = std::getenv("WG_CONV2D_BATCH_BRANCH");
+    if (!(br && br[0] == '0')) {
+        bool ok = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) == cudaSuccess;
+        for (int i = 0; i < Batch::kSides && ok; ++i)
+            ok = cudaStreamCreateWithFlags(&b->side[i], cudaStreamNonBlocking) == cudaSuccess &&
+                 cudaEventCreateWithFlags(&b->join[i], cudaEventDisableTiming) == cudaSuccess;
+        if (!ok) return batch_fail(CONV2D_ERR_CUDA, "side streams of the batch graph");
+    }
     *out = b.release();
     return CONV2D_OK;
 }

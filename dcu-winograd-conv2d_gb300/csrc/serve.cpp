@@ -124,6 +124,9 @@ struct Request {
 
 struct Slot {
     cudaStream_t stream = nullptr;
+    // a batch's F(2x3) chain runs on stream2, beside its F(4x3) chain
+    cudaStream_t stream2 = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr;
     cudaEvent_t start = nullptr;   // timing events: the batch's device interval
     cudaEvent_t done = nullptr;
     void* desc_dev = nullptr;
@@ -183,6 +186,10 @@ struct Server {
         for (Slot& s : slots) {
             if (s.stream) cudaStreamSynchronize(s.stream);
             if (s.stream) cudaStreamDestroy(s.stream);
+            if (s.stream2) cudaStreamSynchronize(s.stream2);
+            if (s.stream2) cudaStreamDestroy(s.stream2);
+            if (s.fork) cudaEventDestroy(s.fork);
+            if (s.join) cudaEventDestroy(s.join);
             if (s.start) cudaEventDestroy(s.start);
             if (s.done) cudaEventDestroy(s.done);
             if (s.desc_dev) cudaFree(s.desc_dev);
@@ -292,22 +299,37 @@ struct Server {
         if (cudaMemcpyAsync(d, h, off, cudaMemcpyHostToDevice, s) != cudaSuccess)
             return set_last_error(CONV2D_ERR_CUDA, "descriptor copy failed");
         cudaError_t e = cudaSuccess;
+        // with requests of both transforms, the F(2x3) chain goes to stream2
+        // (forked after the descriptor copy, joined before `done`) and runs
+        // beside the F(4x3) chain
+        const bool both = !in2.empty() && !in4.empty();
+        cudaStream_t s2 = both ? slot.stream2 : s;
+        if (both) {
+            if ((e = cudaEventRecord(slot.fork, s)) == cudaSuccess) e = cudaStreamWaitEvent(s2, slot.fork, 0);
+        }
         if (!in2.empty() && e == cudaSuccess)
             e = launch_input_transform_grouped(Xform::F2, OpType::F16, reinterpret_cast<const InDesc*>(d + o_in2),
-                                               static_cast<int>(in2.size()), blk_in2, smem2, false, err, s);
+                                               static_cast<int>(in2.size()), blk_in2, smem2, false, err, s2);
+        for (const GG& g : gg)
+            if (g.m == 2 && e == cudaSuccess)
+                e = launch_gemm_grouped(reinterpret_cast<const GemmDesc*>(d + g.off), g.n, g.tiles, OpType::F16, mtype_for(g.m),
+                                        g.bn, static_cast<int>(std::min<long long>(g.tiles, num_sms)), err, s2);
+        if (!out2.empty() && e == cudaSuccess)
+            e = launch_output_transform_grouped(Xform::F2, MType::F16, reinterpret_cast<const OutDesc*>(d + o_out2),
+                                                static_cast<int>(out2.size()), blk_out2, err, s2);
         if (!in4.empty() && e == cudaSuccess)
             e = launch_input_transform_grouped(Xform::F4, OpType::F16, reinterpret_cast<const InDesc*>(d + o_in4),
                                                static_cast<int>(in4.size()), blk_in4, smem4, false, err, s);
         for (const GG& g : gg)
-            if (e == cudaSuccess)
+            if (g.m == 4 && e == cudaSuccess)
                 e = launch_gemm_grouped(reinterpret_cast<const GemmDesc*>(d + g.off), g.n, g.tiles, OpType::F16, mtype_for(g.m),
                                         g.bn, static_cast<int>(std::min<long long>(g.tiles, num_sms)), err, s);
-        if (!out2.empty() && e == cudaSuccess)
-            e = launch_output_transform_grouped(Xform::F2, MType::F16, reinterpret_cast<const OutDesc*>(d + o_out2),
-                                                static_cast<int>(out2.size()), blk_out2, err, s);
         if (!out4.empty() && e == cudaSuccess)
             e = launch_output_transform_grouped(Xform::F4, MType::F24, reinterpret_cast<const OutDesc*>(d + o_out4),
                                                 static_cast<int>(out4.size()), blk_out4, err, s);
+        if (both && e == cudaSuccess) {
+            if ((e = cudaEventRecord(slot.join, s2)) == cudaSuccess) e = cudaStreamWaitEvent(s, slot.join, 0);
+        }
         if (e == cudaSuccess) e = cudaEventRecord(slot.done, s);
         if (e != cudaSuccess) return set_last_error(CONV2D_ERR_CUDA, cudaGetErrorString(e));
         return CONV2D_OK;
@@ -486,6 +508,9 @@ int conv2d_server_create(const conv2d_server_config_t* cfg, conv2d_server_t** ou
     for (Slot& s : sv->slots) {
         s.desc_bytes = static_cast<size_t>(cfg->max_batch) * kDescBytesPerRequest + 4096;
         if (cudaStreamCreateWithFlags(&s.stream, cudaStreamNonBlocking) != cudaSuccess ||
+            cudaStreamCreateWithFlags(&s.stream2, cudaStreamNonBlocking) != cudaSuccess ||
+            cudaEventCreateWithFlags(&s.fork, cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventCreateWithFlags(&s.join, cudaEventDisableTiming) != cudaSuccess ||
             cudaEventCreate(&s.start) != cudaSuccess || cudaEventCreate(&s.done) != cudaSuccess ||
             cudaMalloc(&s.desc_dev, s.desc_bytes) != cudaSuccess ||
             cudaMallocHost(&s.desc_host, s.desc_bytes) != cudaSuccess)
