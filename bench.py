@@ -954,8 +954,8 @@ def serve_layers(seed=20261203):
 
 
 def serving_run(wg, torch, device, count, rates, with_clocks=False):
-    """One request trace through the continuous-batching server (3 slots, up
-    to 64 requests per batch) and through the plain per-call path (each
+    """One request trace through the continuous-batching server (6 slots, up
+    to 16 requests per batch: the library's defaults) and through the plain per-call path (each
     request's own kernels queued on one stream at its arrival, no batching,
     no wait for earlier requests), same kernels and same arithmetic in both.
     Saturated (every request arriving at once) and at Poisson arrival rates
@@ -978,7 +978,7 @@ def serving_run(wg, torch, device, count, rates, with_clocks=False):
     outs = [bufs[li][2].data_ptr() for li in req_layer]
 
     def make(served):
-        srv = (wg.Server(slots=3, max_batch=64, hbm_budget_bytes=40 << 30) if served
+        srv = (wg.Server(slots=6, max_batch=16, hbm_budget_bytes=40 << 30) if served
                else wg.Server(per_request=1, hbm_budget_bytes=40 << 30))
         for (c, k, h), (w, _, _) in zip(layers, bufs):
             srv.add_layer(c, k, h, h, w.data_ptr())

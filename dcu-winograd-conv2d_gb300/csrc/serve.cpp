@@ -479,8 +479,11 @@ int conv2d_server_config_default(conv2d_server_config_t* cfg) {
     if (!cfg) return set_last_error(CONV2D_ERR_INVALID, "null config");
     std::memset(cfg, 0, sizeof(*cfg));
     cfg->hbm_budget_bytes = 40ll << 30;
-    cfg->max_batch = 64;
-    cfg->slots = 3;
+    // measured on the 2,000-request trace of 16 layers (all arriving at once):
+    // 3 slots x 64 requests 864 TFLOP/s, 6 x 16 895, 8 x 16 897; smaller
+    // batches in more slots overlap better
+    cfg->max_batch = 16;
+    cfg->slots = 6;
     cfg->algo = CONV2D_ALGO_AUTO;
     return CONV2D_OK;
 }

@@ -241,8 +241,8 @@ typedef struct conv2d_server conv2d_server_t;
 typedef struct
 {
     long long hbm_budget_bytes;  /* workspace arena (default 40 GiB) */
-    int max_batch;               /* requests per batch (default 64) */
-    int slots;                   /* batches in flight (default 3) */
+    int max_batch;               /* requests per batch (default 16) */
+    int slots;                   /* batches in flight (default 6) */
     int algo;                    /* CONV2D_ALGO_AUTO (shape rule), _2X3_NON_FUSED or _4X3_NON_FUSED */
     int per_request;             /* 1: the plain per-call path instead of batching: each request's own
                                     kernels queued on one stream when it is submitted, in arrival
