@@ -602,7 +602,7 @@ cudaError_t plan_gemm(GemmPlan& gp, OpType op, int E, long long P, int K, int Kp
     cudaError_t e = make_gemm_desc(gp.desc, op, E, P, K, Kp, Cp, V, U, Mw, mt, bn, m_row);
     if (e != cudaSuccess) return e;
     // M of this launch within the L2 size: kept there for the output transform
-    // that reads it next (cfg3 F(4x3): 116 MB in fp32); larger M is streamed out
+    // that reads it next (32 x 512 x 28^2 -> 512 F(4x3): 87 MB in 24 bits); larger M is streamed out
     gp.desc.keep_m = m_bytes(mt, E, P, Kp) <= l2_cache_bytes();
     // V has one reader per tile when one block covers all output channels;
     // WG_CONV2D_KEEP_WORKSPACE=1 keeps it (to read the workspace back)

@@ -1043,10 +1043,11 @@ OutDesc make_out_desc(const Geom& g, MType mt, const void* Mw, void* out, const 
     d.gy = d.KG;
     d.blk_begin = 0;
     // M larger than L2 streams through it: its lines are dropped as soon as
-    // they are read (cfg2 F(4x3), 231 MB: output transform 48.4 -> 42.1 us on
-    // one box); M that fits stays in L2 for this kernel, where discarding only
-    // costs time (cfg3, 116 MB: 22.5 -> 23.8 us).  WG_CONV2D_KEEP_WORKSPACE=1
-    // keeps M readable after the call.
+    // they are read (32 x 256 x 56^2 -> 256 F(4x3), 231 MB of fp32 M: output
+    // transform 48.4 -> 42.1 us on one box); M that fits stays in L2 for this
+    // kernel, where discarding only costs time (32 x 512 x 28^2 -> 512, 116 MB:
+    // 22.5 -> 23.8 us).  WG_CONV2D_KEEP_WORKSPACE=1 keeps M readable after the
+    // call.
     const char* keep_ws = std::getenv("WG_CONV2D_KEEP_WORKSPACE");
     d.discard_m = !(keep_ws && std::atoi(keep_ws) != 0) &&
                   m_bytes(mt, static_cast<long long>(g.alpha) * g.alpha, g.P, g.kp) > l2_cache_bytes();
@@ -1058,9 +1059,10 @@ cudaError_t launch_input_transform(Xform xf, OpType op, const Geom& g, const voi
     int smem = 0;
     const InDesc d = make_in_desc(g, x, x_end, V, scale, &smem);
     // V of this launch within the L2 size: written with the evict_last
-    // priority, the GEMM that follows reads most of it from L2 (cfg2 F(4x3),
-    // 116 MB of V: 146 -> 140 us per call, same box); a larger V (F(2x3) on
-    // cfg2: 205 MB) would only push itself out.  fp16 unscaled paths only.
+    // priority, the GEMM that follows reads most of it from L2 (32 x 256 x
+    // 56^2 -> 256 F(4x3), 116 MB of V: 146 -> 140 us per call, same box); a
+    // larger V (F(2x3) on the same layer: 205 MB) would only push itself out.
+    // fp16 unscaled paths only.
     const long long v_bytes = static_cast<long long>(g.alpha) * g.alpha * d.CG * 8 * d.Pp * 2;
     const bool keep = v_bytes <= l2_cache_bytes();
     const bool bf = op == OpType::BF16, sc = scale != nullptr;
