@@ -144,6 +144,7 @@ __device__ __forceinline__ void store4_row(MT* Mw, const uint32_t (&v)[4], long 
 // Work item t -> problem index (advanced monotonically) and (e, mb, nb):
 // channel block fastest (the V tile is reused from L2), then tile block, then
 // element, so concurrent CTAs write M in long runs of a few element planes.
+// The divisions are multiply-shifts (a problem has fewer than 2^31 items).
 struct Item {
     int e, mb, nb;
 };
@@ -151,12 +152,13 @@ struct Item {
 __device__ __forceinline__ Item locate(const GemmDesc* __restrict__ descs, int ndesc, long long t, int& pi) {
     while (pi + 1 < ndesc && t >= descs[pi + 1].tile_begin) ++pi;
     const GemmDesc& d = descs[pi];
-    const long long local = t - d.tile_begin;
+    const uint32_t local = static_cast<uint32_t>(t - d.tile_begin);
     Item it;
-    it.nb = static_cast<int>(local % d.n_blocks);
-    const long long rest = local / d.n_blocks;
-    it.mb = static_cast<int>(rest % d.m_blocks);
-    it.e = static_cast<int>(rest / d.m_blocks);
+    const uint32_t rest = fast_div(d.fd_nb, local);
+    it.nb = static_cast<int>(local - rest * static_cast<uint32_t>(d.n_blocks));
+    const uint32_t e = fast_div(d.fd_mb, rest);
+    it.mb = static_cast<int>(rest - e * static_cast<uint32_t>(d.m_blocks));
+    it.e = static_cast<int>(e);
     return it;
 }
 
@@ -165,10 +167,12 @@ __device__ __forceinline__ Item locate(const GemmDesc* __restrict__ descs, int n
 // are consecutive; each CTA takes a contiguous range of them.
 __device__ __forceinline__ Item locate_resb(const GemmDesc& d, long long t) {
     Item it;
-    it.mb = static_cast<int>(t % d.m_blocks);
-    const long long rest = t / d.m_blocks;
-    it.nb = static_cast<int>(rest % d.n_blocks);
-    it.e = static_cast<int>(rest / d.n_blocks);
+    const uint32_t tu = static_cast<uint32_t>(t);
+    const uint32_t rest = fast_div(d.fd_mb, tu);
+    it.mb = static_cast<int>(tu - rest * static_cast<uint32_t>(d.m_blocks));
+    const uint32_t e = fast_div(d.fd_nb, rest);
+    it.nb = static_cast<int>(rest - e * static_cast<uint32_t>(d.n_blocks));
+    it.e = static_cast<int>(e);
     return it;
 }
 
@@ -570,6 +574,9 @@ cudaError_t make_gemm_desc(GemmDesc& d, OpType op, int E, long long P, int K, in
     d.E = E;
     d.tile_begin = 0;
     d.tiles = static_cast<long long>(E) * d.m_blocks * d.n_blocks;
+    if (d.tiles >= (1LL << 31)) return cudaErrorInvalidValue;
+    d.fd_mb = make_fastdiv(static_cast<uint32_t>(d.m_blocks));
+    d.fd_nb = make_fastdiv(static_cast<uint32_t>(d.n_blocks));
     const CUtensorMapDataType dt = op == OpType::BF16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT16;
     // V[E][CG][Pp][8] and U[E][CG][Kp][8] viewed as rows of 64 elements (8
     // tiles or output channels x one granule = 128 contiguous bytes): a box of

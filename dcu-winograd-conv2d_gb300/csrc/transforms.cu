@@ -220,10 +220,17 @@ struct InItem {
     int c0, th0, ntb, ylo, yhi, rows, nch;
 };
 
-__device__ __forceinline__ InItem in_item(const InDesc& d, int bx, int by, int M, int A) {
+// Work item `local` of a problem: (image, tile-row block) = local / gy and
+// channel block = local % gy, by multiply-shift division (a problem has
+// fewer than 2^31 items: N x tile-row blocks x channel blocks).
+__device__ __forceinline__ InItem in_item(const InDesc& d, long long local, int M, int A) {
     InItem it;
-    const int bh = bx % d.nbh;
-    it.n = bx / d.nbh;
+    const uint32_t lu = static_cast<uint32_t>(local);
+    const uint32_t bx = fast_div(d.fd_gy, lu);
+    const int by = static_cast<int>(lu - bx * static_cast<uint32_t>(d.gy));
+    const uint32_t n = fast_div(d.fd_nbh, bx);
+    const int bh = static_cast<int>(bx - n * static_cast<uint32_t>(d.nbh));
+    it.n = n;
     it.c0 = by * d.cb;
     it.th0 = bh * d.tb;
     it.ntb = min(d.tb, d.tiles_h - it.th0);
@@ -252,7 +259,7 @@ __device__ __forceinline__ const InDesc& in_desc_of(const InDesc* descs, int nde
 template <int M, int A>
 __device__ __forceinline__ void in_issue(const InDesc& d, long long local, unsigned char* buf, uint64_t* bar) {
     const int lane = threadIdx.x & 31;
-    const InItem it = in_item(d, static_cast<int>(local / d.gy), static_cast<int>(local % d.gy), M, A);
+    const InItem it = in_item(d, local, M, A);
     uint32_t bytes = 0;
     uintptr_t a16 = 0;
     unsigned char* dst = buf + static_cast<size_t>(lane) * d.stride_bytes;
@@ -282,7 +289,7 @@ __device__ __forceinline__ void in_compute(const InDesc& d, long long local, con
     constexpr int M = TF::M, A = TF::ALPHA;
     constexpr int Q = kInComputeWarps * 8;  // tiles in flight per granule
     const int lane = threadIdx.x & 31;
-    const InItem it = in_item(d, static_cast<int>(local / d.gy), static_cast<int>(local % d.gy), M, A);
+    const InItem it = in_item(d, local, M, A);
     const int W = d.W, tiles_w = d.tiles_w, rows = it.rows;
     const long long Pp = d.Pp;
     const long long plane2 = static_cast<long long>(d.H) * d.W * 2;
@@ -497,6 +504,31 @@ __device__ __forceinline__ const OutDesc& out_desc_of(const OutDesc* descs, int 
     return descs[lo];
 }
 
+// Work item -> (first tile p0, granule g), and tile -> (image, tile row,
+// tile column), by multiply-shift division.  The tile count P of a problem is
+// below 2^31 (the GEMM descriptor refuses more), and so is its item count
+// ceil(P/64) * KG for any M that fits in device memory (2^31 items would be
+// P * K >= 2^40, 10^14 bytes of M).
+struct OutItem {
+    uint32_t p0;
+    int g;
+};
+__device__ __forceinline__ OutItem out_item(const OutDesc& d, long long item) {
+    const uint32_t iu = static_cast<uint32_t>(item);
+    const uint32_t blk = fast_div(d.fd_kg, iu);
+    return OutItem{blk * static_cast<uint32_t>(kOsTiles), static_cast<int>(iu - blk * static_cast<uint32_t>(d.KG))};
+}
+struct OutTile {
+    uint32_t n;
+    int th, tw;
+};
+__device__ __forceinline__ OutTile out_tile(const OutDesc& d, uint32_t p) {
+    const uint32_t r = fast_div(d.fd_tw, p);
+    const uint32_t n = fast_div(d.fd_th, r);
+    return OutTile{n, static_cast<int>(r - n * static_cast<uint32_t>(d.tiles_h)),
+                   static_cast<int>(p - r * static_cast<uint32_t>(d.tiles_w))};
+}
+
 // descs: one problem (kernel parameter) or many (device array sorted by
 // blk_begin, items = ceil(P/64) * KG per problem, granule fastest).
 template <class TF, class MT, bool YB>
@@ -532,8 +564,9 @@ __device__ __forceinline__ void output_staged_body(const OutDesc* descs, int nde
             const long long P = d.P;
             const int KG = d.KG;
             const unsigned char* Mb = static_cast<const unsigned char*>(d.Mw);
-            const long long p0 = (item / KG) * kOsTiles;
-            const int g = static_cast<int>(item % KG);
+            const OutItem oi = out_item(d, item);
+            const long long p0 = oi.p0;
+            const int g = oi.g;
             const uint32_t bytes = static_cast<uint32_t>(min(static_cast<long long>(kOsTiles), P - p0)) * 16u;
             uint32_t mine = 0;
             for (int e = lane; e < E; e += 32) mine += bytes;
@@ -556,13 +589,13 @@ __device__ __forceinline__ void output_staged_body(const OutDesc* descs, int nde
             const int KG = d.KG;
             const int K = d.K, OH = d.OH, OW = d.OW, tiles_h = d.tiles_h, tiles_w = d.tiles_w;
             YT* __restrict__ out = reinterpret_cast<YT*>(d.out);
-            const long long p = (item / KG) * kOsTiles + t;
-            const int g = static_cast<int>(item % KG);
+            const OutItem oi = out_item(d, item);
+            const long long p = static_cast<long long>(oi.p0) + t;
+            const int g = oi.g;
             if (p < P) {
-                const int tw = static_cast<int>(p % tiles_w);
-                const long long r = p / tiles_w;
-                const int th = static_cast<int>(r % tiles_h);
-                const long long n = r / tiles_h;
+                const OutTile ot = out_tile(d, static_cast<uint32_t>(p));
+                const int tw = ot.tw, th = ot.th;
+                const long long n = ot.n;
                 const int oh0 = th * M, ow0 = tw * M;
                 const int vr = min(M, OH - oh0), vc = min(M, OW - ow0);
                 const float inv = d.scale ? 1.f / d.scale[p] : 1.f;  // exact: scale is a power of two
@@ -588,7 +621,7 @@ __device__ __forceinline__ void output_staged_body(const OutDesc* descs, int nde
                 // the item's M runs are in shared memory and nothing reads
                 // them again: drop the 128-byte lines that lie wholly inside
                 // them (a line shared with the next granule's rows stays)
-                const long long p0 = (item / KG) * kOsTiles;
+                const long long p0 = oi.p0;
                 const long long nbytes = min(static_cast<long long>(kOsTiles), P - p0) * 16;
                 const unsigned char* Mb = static_cast<const unsigned char*>(d.Mw);
                 for (int i = threadIdx.x; i < E * 8; i += 128) {
@@ -695,8 +728,9 @@ __device__ __forceinline__ void output_staged_body_m24(const OutDesc* descs, int
             const long long P = d.P;
             const int KG = d.KG;
             const unsigned char* Mb = static_cast<const unsigned char*>(d.Mw);
-            const long long p0 = (item / KG) * kOsTiles;
-            const int g = static_cast<int>(item % KG);
+            const OutItem oi = out_item(d, item);
+            const long long p0 = oi.p0;
+            const int g = oi.g;
             const long long nt = min(static_cast<long long>(kOsTiles), P - p0);
             const uint32_t hbytes = static_cast<uint32_t>(nt) * 16u;
             // the low plane's rows are padded to a multiple of 8 tiles: an
@@ -727,13 +761,13 @@ __device__ __forceinline__ void output_staged_body_m24(const OutDesc* descs, int
             const int KG = d.KG;
             const int K = d.K, OH = d.OH, OW = d.OW, tiles_h = d.tiles_h, tiles_w = d.tiles_w;
             YT* __restrict__ out = reinterpret_cast<YT*>(d.out);
-            const long long p = (item / KG) * kOsTiles + t;
-            const int g = static_cast<int>(item % KG);
+            const OutItem oi = out_item(d, item);
+            const long long p = static_cast<long long>(oi.p0) + t;
+            const int g = oi.g;
             if (p < P) {
-                const int tw = static_cast<int>(p % tiles_w);
-                const long long r = p / tiles_w;
-                const int th = static_cast<int>(r % tiles_h);
-                const long long n = r / tiles_h;
+                const OutTile ot = out_tile(d, static_cast<uint32_t>(p));
+                const int tw = ot.tw, th = ot.th;
+                const long long n = ot.n;
                 const int oh0 = th * M, ow0 = tw * M;
                 const int vr = min(M, OH - oh0), vc = min(M, OW - ow0);
                 const float inv = d.scale ? 1.f / d.scale[p] : 1.f;  // exact: scale is a power of two
@@ -768,7 +802,7 @@ __device__ __forceinline__ void output_staged_body_m24(const OutDesc* descs, int
             if (d.discard_m) {
                 // the item's runs are in shared memory and nothing reads them
                 // again: drop the 128-byte lines that lie wholly inside them
-                const long long p0 = (item / KG) * kOsTiles;
+                const long long p0 = oi.p0;
                 const long long nt = min(static_cast<long long>(kOsTiles), P - p0);
                 const unsigned char* Mb = static_cast<const unsigned char*>(d.Mw);
                 for (int i = threadIdx.x; i < E * 12; i += 256) {
@@ -1024,6 +1058,8 @@ InDesc make_in_desc(const Geom& g, const void* x, const void* x_end, void* V, co
     d.tb = b.tb; d.nbh = b.nbh; d.cb = b.cb; d.stride_bytes = b.stride;
     d.gx = static_cast<long long>(g.n) * b.nbh;
     d.gy = (g.c + b.cb - 1) / b.cb;
+    d.fd_gy = make_fastdiv(static_cast<uint32_t>(d.gy));
+    d.fd_nbh = make_fastdiv(static_cast<uint32_t>(b.nbh));
     d.blk_begin = 0;
     *smem = in_smem_total(b.buf);
     return d;
@@ -1042,6 +1078,9 @@ OutDesc make_out_desc(const Geom& g, MType mt, const void* Mw, void* out, const 
     d.gx = (g.P + kOsTiles - 1) / kOsTiles;
     d.gy = d.KG;
     d.blk_begin = 0;
+    d.fd_kg = make_fastdiv(static_cast<uint32_t>(d.KG));
+    d.fd_tw = make_fastdiv(static_cast<uint32_t>(g.tiles_w));
+    d.fd_th = make_fastdiv(static_cast<uint32_t>(g.tiles_h));
     // M larger than L2 streams through it: its lines are dropped as soon as
     // they are read (32 x 256 x 56^2 -> 256 F(4x3), 231 MB of fp32 M: output
     // transform 48.4 -> 42.1 us on one box); M that fits stays in L2 for this

@@ -82,6 +82,33 @@ cudaError_t launch_input_transform(Xform xf, OpType op, const Geom& g, const voi
 
 // Per-problem descriptors of the transform kernels (device-resident arrays of
 // them drive the grouped launches that run many problems at once).
+// Division by a runtime-invariant divisor d (1 <= d < 2^31) as a multiply
+// and a shift, for dividends below 2^31 (Granlund and Montgomery's method):
+// with l = ceil(log2 d), mul = ceil(2^(31+l) / d) < 2^32 and
+// n / d = (n * mul) >> (31 + l) exactly for every n < 2^31.
+struct FastDiv {
+    uint32_t d = 1, mul = 0, shift = 0;
+};
+inline FastDiv make_fastdiv(uint32_t d) {
+    FastDiv f;
+    f.d = d;
+    if (d > 1) {
+        uint32_t l = 0;
+        while ((1u << l) < d) ++l;
+        const uint32_t p = 31 + l;
+        f.mul = static_cast<uint32_t>(((1ull << p) + d - 1) / d);
+        f.shift = p - 32;
+    }
+    return f;
+}
+__host__ __device__ inline uint32_t fast_div(const FastDiv& f, uint32_t n) {
+#ifdef __CUDA_ARCH__
+    return f.d == 1 ? n : (__umulhi(n, f.mul) >> f.shift);
+#else
+    return f.d == 1 ? n : static_cast<uint32_t>((static_cast<uint64_t>(n) * f.mul) >> 32) >> f.shift;
+#endif
+}
+
 struct InDesc {
     const __half* x;
     const __half* x_end;
@@ -93,6 +120,7 @@ struct InDesc {
     long long gx;         // work items along (image, tile-row block)
     int gy;               // work items along channel blocks (cb <= 32)
     long long blk_begin;  // first work item of this problem in a grouped launch
+    FastDiv fd_gy, fd_nbh;   // item -> (image x tile-row block, channel block), -> (image, tile-row block)
 };
 
 struct OutDesc {
@@ -108,6 +136,7 @@ struct OutDesc {
     int discard_m;        // M is read once here: drop its L2 lines without write-back
     long long m_lo;       // 24-bit M: byte offset of the low plane from Mw
     long long m_pp;       // 24-bit M: rows of the low plane per granule (P rounded up to 8)
+    FastDiv fd_kg, fd_tw, fd_th;   // item -> (tile block, granule), tile -> (image, row, column)
 };
 
 // Descriptor of one problem's input transform and the dynamic shared memory
@@ -148,7 +177,8 @@ struct alignas(64) GemmDesc {
     int v_cg, v_pp, discard_v;
     int resb;            // single launches: U block resident in shared memory, contiguous item ranges per CTA
     long long tile_begin;
-    long long tiles;     // E * m_blocks * n_blocks
+    long long tiles;     // E * m_blocks * n_blocks (below 2^31)
+    FastDiv fd_mb, fd_nb;   // division by m_blocks, n_blocks
 };
 
 struct GemmPlan {
