@@ -210,7 +210,7 @@ __global__ void __launch_bounds__(256) nhwc_output_transform(const __grid_consta
     constexpr int A = TF::ALPHA, E = A * A;
     pdl_wait();     // M written, earlier readers of the output done
     pdl_trigger();
-    const long long p = static_cast<long long>(blockIdx.x) * d.tpc + threadIdx.x / d.tpt;
+    const long long p = static_cast<long long>(blockIdx.x) * d.tpc + fast_div(d.fd_tpt, threadIdx.x);
     if (p < d.P && threadIdx.x < d.tpt * d.tpc) nh_out_tile<TF, MT>(d, p);
     if (d.discard_m) {
         // every M row of the CTA's tiles has been read (rows are whole 128-byte
@@ -220,10 +220,13 @@ __global__ void __launch_bounds__(256) nhwc_output_transform(const __grid_consta
         const int tiles = static_cast<int>(min(static_cast<long long>(d.tpc), d.P - p_first));
         const int lpr = d.Kp * static_cast<int>(sizeof(MT)) / 128;   // lines per row
         const unsigned char* Mb = static_cast<const unsigned char*>(d.Mw);
-        for (int i = threadIdx.x; i < E * tiles * lpr; i += blockDim.x) {
-            const int l = i % lpr, rest = i / lpr;
-            const int tt = rest % tiles, e = rest / tiles;
-            discard_l2_line(Mb + ((static_cast<long long>(e) * d.P + p_first + tt) * d.Kp) * sizeof(MT) + l * 128);
+        // i = (e * tpc + tt) * lpr + l over whole CTAs' worth of tiles; the
+        // last CTA skips its missing ones
+        for (int i = threadIdx.x; i < E * d.tpc * lpr; i += blockDim.x) {
+            const uint32_t rest = fast_div(d.fd_lpr, i), e = fast_div(d.fd_tpc, rest);
+            const int l = static_cast<int>(i - rest * lpr), tt = static_cast<int>(rest - e * d.tpc);
+            if (tt < tiles)
+                discard_l2_line(Mb + ((static_cast<long long>(e) * d.P + p_first + tt) * d.Kp) * sizeof(MT) + l * 128);
         }
     }
 }
@@ -231,15 +234,18 @@ __global__ void __launch_bounds__(256) nhwc_output_transform(const __grid_consta
 template <class TF, class MT>
 __device__ __forceinline__ void nh_out_tile(const NhwcOutDesc& d, long long p) {
     constexpr int M = TF::M, A = TF::ALPHA, E = A * A;
-    const int tw = static_cast<int>(p % d.tiles_w);
-    const long long r = p / d.tiles_w;
-    const int th = static_cast<int>(r % d.tiles_h);
-    const long long n = r / d.tiles_h;
+    // p < P < 2^31 (the GEMM descriptor refuses more tiles)
+    const uint32_t pu = static_cast<uint32_t>(p);
+    const uint32_t r = fast_div(d.fd_tw, pu), nn = fast_div(d.fd_th, r);
+    const int tw = static_cast<int>(pu - r * static_cast<uint32_t>(d.tiles_w));
+    const int th = static_cast<int>(r - nn * static_cast<uint32_t>(d.tiles_h));
+    const long long n = nn;
     const int oh0 = th * M, ow0 = tw * M;
     const int vr = min(M, d.OH - oh0), vc = min(M, d.OW - ow0);
     const MT* Mw = static_cast<const MT*>(d.Mw);
     const long long estride = d.P * d.Kp;
-    for (int kk = threadIdx.x % d.tpt; 2 * kk < d.K; kk += d.tpt) {
+    const int kk0 = static_cast<int>(threadIdx.x - fast_div(d.fd_tpt, threadIdx.x) * static_cast<uint32_t>(d.tpt));
+    for (int kk = kk0; 2 * kk < d.K; kk += d.tpt) {
         const MT* src = Mw + p * d.Kp + 2 * kk;
         float2 m[E];
 #pragma unroll
@@ -356,6 +362,10 @@ NhwcOutDesc make_nhwc_out_desc(const Geom& g, const void* Mw, void* out) {
     d.P = g.P;
     d.tpt = std::min(256, (g.kp / 2 + 31) / 32 * 32);
     d.tpc = 256 / d.tpt;
+    d.fd_tpt = make_fastdiv(static_cast<uint32_t>(d.tpt));
+    d.fd_tw = make_fastdiv(static_cast<uint32_t>(g.tiles_w));
+    d.fd_th = make_fastdiv(static_cast<uint32_t>(g.tiles_h));
+    d.fd_tpc = make_fastdiv(static_cast<uint32_t>(d.tpc));
     return d;
 }
 
@@ -373,6 +383,7 @@ cudaError_t launch_nhwc_output_transform(Xform xf, MType mt, const NhwcOutDesc& 
     const char* keep_ws = std::getenv("WG_CONV2D_KEEP_WORKSPACE");
     d.discard_m = !(keep_ws && std::atoi(keep_ws) != 0) && (d.Kp * esize) % 128 == 0 &&
                   static_cast<long long>(A) * A * d.P * d.Kp * esize > l2_cache_bytes();
+    d.fd_lpr = make_fastdiv(static_cast<uint32_t>(std::max(1, d.Kp * esize / 128)));
     switch (xf) {
         case Xform::F2:
             return m_fp32 ? launch_pdl(nhwc_output_transform<F2, float>, grid, dim3(256), 0, s, d)

@@ -229,6 +229,7 @@ struct NhwcOutDesc {
     long long P;
     int tpt, tpc;         // threads per tile, tiles per CTA
     int discard_m;        // drop M's lines from L2 once read (set by the launcher)
+    FastDiv fd_tpt, fd_tw, fd_th, fd_tpc, fd_lpr;   // divisions by tpt, tiles_w, tiles_h, tpc, M lines per row
 };
 NhwcOutDesc make_nhwc_out_desc(const Geom& g, const void* Mw, void* out);
 cudaError_t launch_nhwc_output_transform(Xform xf, MType mt, const NhwcOutDesc& d, cudaStream_t stream);
