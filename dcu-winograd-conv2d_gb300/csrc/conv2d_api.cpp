@@ -208,13 +208,14 @@ int Plan::build(const problem_t* pr, const conv2d_options_t* opt_in) {
     // lose ~10x accuracy there); M in fp32 either way
     if (opt.io_bf16) op = m == 2 ? OpType::BF16 : OpType::F16;
     // M: 24-bit for F(4x3) with fp16 operands (fp16 M would add ~1e-2
-    // through A^T m A), fp32 where asked, for bf16 operands, for channels-last
-    // output (row-major M) and for F(2x3) with bf16 tensors, fp16 for F(2x3)
-    // otherwise
+    // through A^T m A; channels-last outputs too, from the same granule
+    // layout), fp32 where asked, for bf16 operands and for F(2x3) with bf16
+    // tensors, fp16 for F(2x3) otherwise.  Channels-last F(2x3) and fp32 M
+    // take the row-major M of the NHWC output transform.
     if (algo == CONV2D_ALGO_4X3_ROW)
         mt = MType::F16;   // no M
     else if (m == 4)
-        mt = (nhwc || opt.m_fp32 || op == OpType::BF16) ? MType::F32 : MType::F24;
+        mt = (opt.m_fp32 || op == OpType::BF16) ? MType::F32 : MType::F24;
     else
         mt = opt.io_bf16 ? MType::F32 : MType::F16;
     scaling = (m == 4) && (opt.tile_scaling || opt.io_bf16) && algo != CONV2D_ALGO_4X3_ROW;
@@ -295,14 +296,14 @@ int Plan::build(const problem_t* pr, const conv2d_options_t* opt_in) {
             if (ce != cudaSuccess) return cuda_fail(ce, "NHWC tensor map");
         }
         const int bn = opt.gemm_bn ? opt.gemm_bn : default_bn(g.k);
-        ce = plan_gemm(gemm_full, op, E, Pc, g.k, g.kp, g.cp, V, U, Mw, mt, bn, num_sms, nhwc);
+        ce = plan_gemm(gemm_full, op, E, Pc, g.k, g.kp, g.cp, V, U, Mw, mt, bn, num_sms, m_row());
         if (ce != cudaSuccess) return cuda_fail(ce, "GEMM plan (tensor maps)");
         n_chunks = (static_cast<int>(pr->n) + chunk_n - 1) / chunk_n;
         const int tail_n = static_cast<int>(pr->n) - (n_chunks - 1) * chunk_n;
         has_tail = tail_n != chunk_n;
         if (has_tail) {
             const long long Pt = static_cast<long long>(tail_n) * g.tiles_h * g.tiles_w;
-            ce = plan_gemm(gemm_tail, op, E, Pt, g.k, g.kp, g.cp, V, U, Mw, mt, bn, num_sms, nhwc);
+            ce = plan_gemm(gemm_tail, op, E, Pt, g.k, g.kp, g.cp, V, U, Mw, mt, bn, num_sms, m_row());
             if (ce != cudaSuccess) return cuda_fail(ce, "GEMM plan (tail)");
         }
         launches = n_chunks * (3 + (scaling ? 1 : 0));
@@ -356,7 +357,8 @@ int Plan::run_range(int n0, int nc, const GemmPlan* gp, cudaStream_t s) {
         ce = launch_gemm(*gp, err, s);
         if (ce != cudaSuccess) return cuda_fail(ce, "GEMM launch");
         mark(s);
-        ce = launch_nhwc_output_transform(xf, mt, make_nhwc_out_desc(gc, Mw, yout), s);
+        ce = mt == MType::F24 ? launch_output_transform_nhwc24(xf, gc, Mw, yout, err, s)
+                              : launch_nhwc_output_transform(xf, mt, make_nhwc_out_desc(gc, Mw, yout), s);
         if (ce != cudaSuccess) return cuda_fail(ce, "NHWC output transform launch");
         mark(s);
         return CONV2D_OK;
@@ -458,7 +460,7 @@ const GemmPlan* Plan::host_gemm_for(int nc) {
     const int E = g.alpha * g.alpha;
     GemmPlan& gp = host_gemm[n_host_plans];
     if (plan_gemm(gp, op, E, static_cast<long long>(nc) * g.tiles_h * g.tiles_w, g.k, g.kp, g.cp, V, U, Mw, mt,
-                  gemm_full.bn, num_sms, nhwc) != cudaSuccess)
+                  gemm_full.bn, num_sms, m_row()) != cudaSuccess)
         return nullptr;
     host_plan_n[n_host_plans++] = nc;
     return &gp;

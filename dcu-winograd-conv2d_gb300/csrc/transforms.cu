@@ -695,7 +695,9 @@ constexpr int kOs24Threads = 32 * 9;
 template <class TF> __host__ __device__ constexpr int os24_item_bytes() { return TF::ALPHA * TF::ALPHA * kOsTiles * (16 + 8); }
 template <class TF> __host__ __device__ constexpr int os24_smem_bytes() { return 128 + 2 * os24_item_bytes<TF>(); }
 
-template <class TF, bool YB>
+// YNHWC: the output is channels-last, y[N][OH][OW][K] (fp16, unscaled): a
+// thread writes its channel pair at each of the tile's pixels.
+template <class TF, bool YB, bool YNHWC = false>
 __device__ __forceinline__ void output_staged_body_m24(const OutDesc* descs, int ndesc, long long total, DevErr* err) {
     using YT = typename IO<YB>::T;
     constexpr int M = TF::M, A = TF::ALPHA, E = A * A;
@@ -786,17 +788,43 @@ __device__ __forceinline__ void output_staged_body_m24(const OutDesc* descs, int
                 }
                 float2 y2[M * M];
                 output_tile_transform2<TF>(m, y2);
+                if constexpr (YNHWC) {
+                    // channels kc, kc + 1 of each pixel: one 4-byte store where
+                    // both exist and the pair is 4-byte aligned (K even)
+                    const int kc = g * 8 + qd * 2;
+                    if (kc < K) {
+                        YT* o = out + ((n * OH + oh0) * static_cast<long long>(OW) + ow0) * K + kc;
+                        const bool pair = kc + 1 < K, even = (K & 1) == 0;
 #pragma unroll
-                for (int ch = 0; ch < 2; ++ch) {
-                    const int kc = g * 8 + qd * 2 + ch;
-                    if (kc >= K) break;
-                    float y[M * M];
+                        for (int i = 0; i < M; ++i) {
+                            if (i >= vr) break;
 #pragma unroll
-                    for (int i = 0; i < M * M; ++i) y[i] = ch == 0 ? y2[i].x : y2[i].y;
-                    YT* o = out + ((n * K + kc) * OH + oh0) * static_cast<long long>(OW) + ow0;
+                            for (int j = 0; j < M; ++j) {
+                                if (j >= vc) break;
+                                YT* q = o + (static_cast<long long>(i) * OW + j) * K;
+                                const float2 v = y2[i * M + j];
+                                if (pair && even) {
+                                    *reinterpret_cast<uint32_t*>(q) = pack2<YT>(v.x, v.y);
+                                } else {
+                                    q[0] = from_f32<YT>(v.x);
+                                    if (pair) q[1] = from_f32<YT>(v.y);
+                                }
+                            }
+                        }
+                    }
+                } else {
 #pragma unroll
-                    for (int i = 0; i < M; ++i)
-                        if (i < vr) store_row<M>(o + static_cast<long long>(i) * OW, &y[i * M], vc, inv);
+                    for (int ch = 0; ch < 2; ++ch) {
+                        const int kc = g * 8 + qd * 2 + ch;
+                        if (kc >= K) break;
+                        float y[M * M];
+#pragma unroll
+                        for (int i = 0; i < M * M; ++i) y[i] = ch == 0 ? y2[i].x : y2[i].y;
+                        YT* o = out + ((n * K + kc) * OH + oh0) * static_cast<long long>(OW) + ow0;
+#pragma unroll
+                        for (int i = 0; i < M; ++i)
+                            if (i < vr) store_row<M>(o + static_cast<long long>(i) * OW, &y[i * M], vc, inv);
+                    }
                 }
             }
             if (d.discard_m) {
@@ -827,10 +855,10 @@ __device__ __forceinline__ void output_staged_body_m24(const OutDesc* descs, int
     }
 }
 
-template <class TF, bool YB>
+template <class TF, bool YB, bool YNHWC = false>
 __global__ void __launch_bounds__(kOs24Threads, 2)
     output_transform_staged_m24(const __grid_constant__ OutDesc d, long long total, DevErr* err) {
-    output_staged_body_m24<TF, YB>(&d, 1, total, err);
+    output_staged_body_m24<TF, YB, YNHWC>(&d, 1, total, err);
 }
 
 template <class TF>
@@ -944,11 +972,11 @@ cudaError_t output_launch(const OutDesc& d, DevErr* err, cudaStream_t s) {
     return launch_pdl(kern, dim3(static_cast<unsigned>(grid)), dim3(kOsThreads), smem, s, d, total, err);
 }
 
-template <class TF, bool YB = false>
+template <class TF, bool YB = false, bool YNHWC = false>
 cudaError_t output_launch_m24(const OutDesc& d, DevErr* err, cudaStream_t s) {
     const long long total = (d.P + kOsTiles - 1) / kOsTiles * d.KG;
     if (total <= 0) return cudaSuccess;
-    auto kern = output_transform_staged_m24<TF, YB>;
+    auto kern = output_transform_staged_m24<TF, YB, YNHWC>;
     constexpr int smem = os24_smem_bytes<TF>();
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e != cudaSuccess) return e;
@@ -1187,6 +1215,17 @@ cudaError_t launch_output_transform(Xform xf, MType mt, const Geom& g, const voi
             return m_fp32 ? output_launch<F4, float>(d, err, stream) : output_launch<F4, __half>(d, err, stream);
         case Xform::F4Ref:
             return m_fp32 ? output_launch<F4Ref, float>(d, err, stream) : output_launch<F4Ref, __half>(d, err, stream);
+    }
+    return cudaErrorInvalidValue;
+}
+
+cudaError_t launch_output_transform_nhwc24(Xform xf, const Geom& g, const void* Mw, void* out, DevErr* err,
+                                          cudaStream_t stream) {
+    const OutDesc d = make_out_desc(g, MType::F24, Mw, out, nullptr);
+    switch (xf) {
+        case Xform::F2: return cudaErrorNotSupported;
+        case Xform::F4: return output_launch_m24<F4, false, true>(d, err, stream);
+        case Xform::F4Ref: return output_launch_m24<F4Ref, false, true>(d, err, stream);
     }
     return cudaErrorInvalidValue;
 }

@@ -150,6 +150,10 @@ cudaError_t launch_input_transform_grouped(Xform xf, OpType op, const InDesc* de
                                            int smem, bool scaled, DevErr* err, cudaStream_t stream);
 cudaError_t launch_output_transform_grouped(Xform xf, MType mt, const OutDesc* descs, int ndesc, long long blocks,
                                             DevErr* err, cudaStream_t stream);
+// out[N][OH][OW][K] (channels-last, fp16) from the 24-bit granule-layout M
+// of F(4x3): the arithmetic of launch_output_transform, other store order.
+cudaError_t launch_output_transform_nhwc24(Xform xf, const Geom& g, const void* Mw, void* out, DevErr* err,
+                                          cudaStream_t stream);
 
 // out[N][K][OH][OW] = A^T M A from M stored as `mt` (granule layouts above);
 // divides by scale[p] when scale is not null.

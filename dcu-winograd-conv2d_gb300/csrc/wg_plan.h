@@ -78,6 +78,9 @@ struct Plan {
 
     // one kernel per call, no Winograd-domain workspace
     bool single_kernel() const { return algo == CONV2D_ALGO_2X3_FUSED || algo == CONV2D_ALGO_4X3_ROW; }
+    // GEMM result row-major (M[E][P][Kp]) for the NHWC output transform of
+    // fp16 / fp32 M; 24-bit M keeps the granule layout in both layouts
+    bool m_row() const { return nhwc && mt != MType::F24; }
 
     ~Plan();
     int build(const problem_t* pr, const conv2d_options_t* opt);

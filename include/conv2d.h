@@ -127,7 +127,7 @@ typedef struct
                             non-fused F(2x3)/F(4x3), fp16 tensors, images up to ~250 columns */
     int m_fp32;          /* F(4x3) non-fused: 1 stores the GEMM result M in fp32; 0 (default) in 24 bits
                             (each fp32 accumulator rounded to its upper 24 bits: relative rounding
-                            2^-17, 3/4 of the fp32 bytes).  NHWC tensors always use fp32 M */
+                            2^-17, 3/4 of the fp32 bytes), for NCHW and NHWC tensors alike */
     int reserved[1];
 } conv2d_options_t;
 

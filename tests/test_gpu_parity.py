@@ -390,22 +390,23 @@ def test_bf16_end_to_end(wg, algo, shape):
 NHWC_SHAPES = [(2, 24, 16, 16, 32, 1), (1, 16, 13, 11, 27, 1), (3, 40, 9, 30, 36, 2), (2, 64, 28, 28, 64, 0)]
 
 
-@pytest.mark.parametrize("algo", [0, 1, 2])
+@pytest.mark.parametrize("algo,mfp32", [(0, 0), (0, 1), (1, 0), (2, 0)])
 @pytest.mark.parametrize("shape", NHWC_SHAPES)
-def test_nhwc_matches_nchw_bit_for_bit(wg, algo, shape):
+def test_nhwc_matches_nchw_bit_for_bit(wg, algo, mfp32, shape):
     """Channels-last input and output (filter KCRS): the same V, M and output
     arithmetic as the NCHW path, so the result is the NCHW result transposed,
-    bit for bit (the fused selection runs F(2x3) non-fused for NHWC).  NHWC
-    stores F(4x3)'s M in fp32, so the NCHW call is asked for fp32 M too."""
+    bit for bit (the fused selection runs F(2x3) non-fused for NHWC).  F(4x3)
+    with 24-bit M (granule layout, as NCHW) and with fp32 M (row-major, the
+    NHWC output transform's own layout)."""
     n, c, h, w, k, pad = shape
     x, wt = O.uniform_inputs(41 + algo, n, c, h, w, k)
-    y_nchw, op1 = run(wg, x, wt, pad, pad, opts_for(wg, 1 if algo == 2 else algo, m_fp32=1))
+    y_nchw, op1 = run(wg, x, wt, pad, pad, opts_for(wg, 1 if algo == 2 else algo, m_fp32=mfp32))
     xt = torch.from_numpy(np.ascontiguousarray(x.transpose(0, 2, 3, 1))).cuda()
     wtt = torch.from_numpy(wt).cuda()
     oh, ow = h + 2 * pad - 2, w + 2 * pad - 2
     y = torch.full((n, oh, ow, k), float("nan"), dtype=torch.float16, device="cuda")
     prob = wg.make_problem(xt.data_ptr(), wtt.data_ptr(), y.data_ptr(), n, c, h, w, k, pad, pad)
-    op = wg.Conv2d(prob, opts_for(wg, algo, layout_nhwc=1))
+    op = wg.Conv2d(prob, opts_for(wg, algo, layout_nhwc=1, m_fp32=mfp32))
     op(torch.cuda.current_stream().cuda_stream)
     torch.cuda.synchronize()
     assert op.check_device()[0] == wg.OK
