@@ -109,7 +109,7 @@ enum {
  * more than 3% faster; the choice is cached per shape (and in
  * WG_CONV2D_TUNE_FILE).  On GB300 the reference rule's fused F(2x3) pick is
  * several times slower than the alternatives for wide K (e.g. 392 against
- * 121 us on 32x256x56^2 -> 256).  algo = CONV2D_ALGO_REFERENCE, or
+ * 115 us on 32x256x56^2 -> 256).  algo = CONV2D_ALGO_REFERENCE, or
  * WG_CONV2D_ALGO=ref, applies the reference rule (src/conv2d.cpp:83-114)
  * exactly; conv2d_get_algo reports what was chosen. */
 typedef struct
