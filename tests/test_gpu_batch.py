@@ -63,3 +63,30 @@ def test_batch_grouped_equals_percall_and_oracle(wg, algo):
         tol = 3e-2 if (a == 0 and x.shape[1] < 16) else TOL[a]
         assert O.rel_errors(y.cpu().numpy(), r64)[0] <= tol, (i, a)
     b.destroy()
+
+
+@pytest.mark.parametrize("split", ["0", "1"])
+def test_batch_stream_orders_give_the_same_bits(wg, monkeypatch, split):
+    """The batch graph's units run as parallel branches on forked streams by
+    default; one chain after another on one stream (WG_CONV2D_BATCH_BRANCH=0)
+    and one chain per (transform, GEMM tile) (WG_CONV2D_BATCH_SPLIT_BN=1) are
+    the same kernels on the same data: every order gives the same bits."""
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    probs, keep, _ = _make(wg, SHAPES, 23)
+    s = torch.cuda.current_stream().cuda_stream
+    outs = []
+    for branch in ("1", "0"):
+        monkeypatch.setenv("WG_CONV2D_BATCH_BRANCH", branch)
+        monkeypatch.setenv("WG_CONV2D_BATCH_SPLIT_BN", split)
+        for _, _, y in keep:
+            y.zero_()
+        b = wg.Batch(probs, wg.default_options(algo=3))
+        b.run(s)
+        b.run(s)
+        torch.cuda.synchronize()
+        assert b.check_device()[0] == wg.OK
+        outs.append([y.clone() for _, _, y in keep])
+        b.destroy()
+    for i, (a, c) in enumerate(zip(*outs)):
+        assert torch.equal(a, c), i

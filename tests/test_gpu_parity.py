@@ -417,8 +417,10 @@ def test_nhwc_matches_nchw_bit_for_bit(wg, algo, mfp32, shape):
     op.destroy()
 
 
-def test_nhwc_host_buffers_in_chunks(wg):
-    """NHWC through the host-buffer entry point, cut into 3 image chunks."""
+@pytest.mark.parametrize("algo", [1, 0])
+def test_nhwc_host_buffers_in_chunks(wg, algo):
+    """NHWC through the host-buffer entry point, cut into 3 image chunks
+    (F(2x3) with row-major fp16 M, F(4x3) with 24-bit granule-layout M)."""
     n, c, h, w, k = 11, 64, 100, 100, 64
     x, wt = O.uniform_inputs(77, n, c, h, w, k)
     xh = np.ascontiguousarray(x.transpose(0, 2, 3, 1))
@@ -426,11 +428,11 @@ def test_nhwc_host_buffers_in_chunks(wg):
     wtt = torch.from_numpy(wt).cuda()
     y = torch.empty((n, h, w, k), dtype=torch.float16, device="cuda")
     prob = wg.make_problem(xt.data_ptr(), wtt.data_ptr(), y.data_ptr(), n, c, h, w, k)
-    op = wg.Conv2d(prob, opts_for(wg, 1, layout_nhwc=1))
+    op = wg.Conv2d(prob, opts_for(wg, algo, layout_nhwc=1))
     hin = torch.from_numpy(xh).pin_memory()
     hout = torch.empty((n, h, w, k), dtype=torch.float16).pin_memory()
     op.host(hin.data_ptr(), hout.data_ptr(), torch.cuda.current_stream().cuda_stream)
-    dev, _ = run(wg, x, wt, 1, 1, opts_for(wg, 1))
+    dev, _ = run(wg, x, wt, 1, 1, opts_for(wg, algo))
     assert np.array_equal(hout.numpy().transpose(0, 3, 1, 2).view(np.uint16), dev.view(np.uint16))
     op.destroy()
 
