@@ -166,7 +166,7 @@ __global__ void __launch_bounds__(256) tile_scale_kernel(const typename IO<XB>::
 constexpr int kInComputeWarps = 7;
 constexpr int kInThreads = 32 * (kInComputeWarps + 1);  // + one producer warp
 constexpr int kInMaxBufs = 3;   // staging buffers: 3 where two CTAs of them fit an SM, else 2
-constexpr int kInHeader = 96;   // 2 x kInMaxBufs mbarriers, an abort flag, 16 zero bytes
+constexpr int kInHeader = 96;   // 2 x kInMaxBufs mbarriers, an abort flag, 32 zero bytes at 64
 constexpr int kInSlack = 256;   // bytes before and after the two buffers: reads
                                 // of columns in the padding (masked to zero)
                                 // stay inside the CTA's shared memory
@@ -283,7 +283,16 @@ __device__ __forceinline__ void in_issue(const InDesc& d, long long local, unsig
 // Compute warp cw (of kInComputeWarps) transforms its share of the item:
 // lanes are (tile offset q, channel pair sub) with four pairs per granule
 // row; tiles q, q + Q, q + 2Q, ... of the item for every granule.
-template <class TF, class OutT, bool SCALED, bool XB, bool KEEP>
+//
+// WORDS (problems with pad 1, W a multiple of M and an 8-byte aligned input;
+// InDesc::words): a tile's row of ALPHA elements starts 2 bytes before a
+// word boundary, so it is read as ALPHA/2 + 1 aligned words (F(4x3): one
+// 32-bit, one 64-bit and one 32-bit load; F(2x3): three 32-bit loads)
+// instead of ALPHA 16-bit loads, and a byte permute takes each element's
+// half of the two channels' words.  Only the first column of the first tile
+// and the last column of the last tile of a row can fall outside the image
+// there; they are set to zero after the permute.
+template <class TF, class OutT, bool SCALED, bool XB, bool KEEP, bool WORDS>
 __device__ __forceinline__ void in_compute(const InDesc& d, long long local, const unsigned char* buf,
                                            const unsigned char* zero, int cw) {
     constexpr int M = TF::M, A = TF::ALPHA;
@@ -322,8 +331,14 @@ __device__ __forceinline__ void in_compute(const InDesc& d, long long local, con
             // column outside the image takes the zero upper half of the
             // zero-extended 16-bit loads through the byte-permute selector
             uint32_t sel[A];
+            bool lpad = false, rpad = false;
+            if constexpr (WORDS) {
+                lpad = tw == 0;
+                rpad = tw == tiles_w - 1;
+            } else {
 #pragma unroll
-            for (int j = 0; j < A; ++j) sel[j] = (x0 + j >= 0 && x0 + j < W) ? 0x5410u : 0x3232u;
+                for (int j = 0; j < A; ++j) sel[j] = (x0 + j >= 0 && x0 + j < W) ? 0x5410u : 0x3232u;
+            }
             float2 s2 = f2(1.f);
             if constexpr (SCALED) s2 = f2(d.scale ? d.scale[p0 + t] : 1.f);  // unscaled problems of a group
             // rows first: r[i][.] = d[i][.] B, then columns: V[.][j] = B^T r[.][j]
@@ -332,16 +347,48 @@ __device__ __forceinline__ void in_compute(const InDesc& d, long long local, con
             for (int i = 0; i < A; ++i) {
                 const int yr = y0 + i;
                 const bool rok = yr >= 0 && yr < rows;
-                const int ofs = yr * W * 2 + 2 * x0;
-                const uint16_t* r0 = reinterpret_cast<const uint16_t*>(rok && ok0 ? cb0 + ofs : zero);
-                const uint16_t* r1 = reinterpret_cast<const uint16_t*>(rok && ok1 ? cb1 + ofs : zero);
                 float2 dv[A];
+                if constexpr (WORDS) {
+                    // word k of a channel's row covers bytes [4k - 4, 4k) from the
+                    // tile's second element; element j is half (j + 1) & 1 of word (j + 1) / 2
+                    constexpr int NW = A / 2 + 1;
+                    const int ofs = yr * W * 2 + 2 * M * tw;
+                    const unsigned char* q0 = rok && ok0 ? cb0 + ofs : zero + 8;
+                    const unsigned char* q1 = rok && ok1 ? cb1 + ofs : zero + 8;
+                    uint32_t w0[NW], w1[NW];
+                    w0[0] = *reinterpret_cast<const uint32_t*>(q0 - 4);
+                    w1[0] = *reinterpret_cast<const uint32_t*>(q1 - 4);
+                    if constexpr (A == 6) {
+                        const uint2 a = *reinterpret_cast<const uint2*>(q0);
+                        const uint2 b = *reinterpret_cast<const uint2*>(q1);
+                        w0[1] = a.x; w0[2] = a.y;
+                        w1[1] = b.x; w1[2] = b.y;
+                    } else {
+                        w0[1] = *reinterpret_cast<const uint32_t*>(q0);
+                        w1[1] = *reinterpret_cast<const uint32_t*>(q1);
+                    }
+                    w0[NW - 1] = *reinterpret_cast<const uint32_t*>(q0 + 4 * (NW - 2));
+                    w1[NW - 1] = *reinterpret_cast<const uint32_t*>(q1 + 4 * (NW - 2));
 #pragma unroll
-                for (int j = 0; j < A; ++j) {
-                    const uint32_t h = __byte_perm(r0[j], r1[j], sel[j]);
-                    float2 v = IO<XB>::pair(h);
-                    if constexpr (SCALED) v = __fmul2_rn(v, s2);
-                    dv[j] = v;
+                    for (int j = 0; j < A; ++j) {
+                        uint32_t h = __byte_perm(w0[(j + 1) / 2], w1[(j + 1) / 2], ((j + 1) & 1) ? 0x7632u : 0x5410u);
+                        if (j == 0 && lpad) h = 0u;
+                        if (j == A - 1 && rpad) h = 0u;
+                        float2 v = IO<XB>::pair(h);
+                        if constexpr (SCALED) v = __fmul2_rn(v, s2);
+                        dv[j] = v;
+                    }
+                } else {
+                    const int ofs = yr * W * 2 + 2 * x0;
+                    const uint16_t* r0 = reinterpret_cast<const uint16_t*>(rok && ok0 ? cb0 + ofs : zero);
+                    const uint16_t* r1 = reinterpret_cast<const uint16_t*>(rok && ok1 ? cb1 + ofs : zero);
+#pragma unroll
+                    for (int j = 0; j < A; ++j) {
+                        const uint32_t h = __byte_perm(r0[j], r1[j], sel[j]);
+                        float2 v = IO<XB>::pair(h);
+                        if constexpr (SCALED) v = __fmul2_rn(v, s2);
+                        dv[j] = v;
+                    }
                 }
                 Bt2<TF>::run(dv, r[i]);
             }
@@ -390,7 +437,8 @@ __device__ __forceinline__ void input_body(const InDesc* descs, int ndesc, long 
     uint64_t* full = reinterpret_cast<uint64_t*>(smem_raw);
     uint64_t* empty = full + kInMaxBufs;
     volatile int* abort_flag = reinterpret_cast<volatile int*>(full + 2 * kInMaxBufs);
-    unsigned char* zero = smem_raw + 64;  // 16 zero bytes: the ALPHA elements of a padding row
+    unsigned char* zero = smem_raw + 64;  // 32 zero bytes: the ALPHA elements of a padding row
+                                          // (16-bit loads from zero, word loads around zero + 8)
     unsigned char* bufs = smem_raw + kInHeader + kInSlack;
     const int warp = threadIdx.x >> 5;
     if (threadIdx.x == 0) {
@@ -400,6 +448,7 @@ __device__ __forceinline__ void input_body(const InDesc* descs, int ndesc, long 
         }
         *abort_flag = 0;
         *reinterpret_cast<uint4*>(zero) = make_uint4(0u, 0u, 0u, 0u);
+        *reinterpret_cast<uint4*>(zero + 16) = make_uint4(0u, 0u, 0u, 0u);
         fence_barrier_init();
     }
     pdl_wait();     // input written, earlier readers of V done
@@ -419,7 +468,10 @@ __device__ __forceinline__ void input_body(const InDesc* descs, int ndesc, long 
             const int b = k % nbufs;
             if (!mbar_wait(&full[b], (k / nbufs) & 1, abort_flag, err, ERR_SITE_FULL)) break;
             const InDesc& d = in_desc_of(descs, ndesc, item);
-            in_compute<TF, OutT, SCALED, XB, KEEP>(d, item - d.blk_begin, bufs + b * buf_bytes, zero, warp);
+            if (d.words)
+                in_compute<TF, OutT, SCALED, XB, KEEP, true>(d, item - d.blk_begin, bufs + b * buf_bytes, zero, warp);
+            else
+                in_compute<TF, OutT, SCALED, XB, KEEP, false>(d, item - d.blk_begin, bufs + b * buf_bytes, zero, warp);
             __syncwarp();
             if ((threadIdx.x & 31) == 0) mbar_arrive(&empty[b]);
         }
@@ -1089,6 +1141,7 @@ InDesc make_in_desc(const Geom& g, const void* x, const void* x_end, void* V, co
     d.fd_gy = make_fastdiv(static_cast<uint32_t>(d.gy));
     d.fd_nbh = make_fastdiv(static_cast<uint32_t>(b.nbh));
     d.blk_begin = 0;
+    d.words = (g.m == 2 || g.m == 4) && g.pad_w == 1 && g.w % g.m == 0 && (reinterpret_cast<uintptr_t>(x) & 7) == 0;
     *smem = in_smem_total(b.buf);
     return d;
 }

@@ -121,6 +121,7 @@ struct InDesc {
     int gy;               // work items along channel blocks (cb <= 32)
     long long blk_begin;  // first work item of this problem in a grouped launch
     FastDiv fd_gy, fd_nbh;   // item -> (image x tile-row block, channel block), -> (image, tile-row block)
+    int words;               // rows read as aligned words (pad 1, W % M == 0, x 8-byte aligned)
 };
 
 struct OutDesc {
