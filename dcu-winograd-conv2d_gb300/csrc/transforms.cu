@@ -521,16 +521,16 @@ template <> struct MG<float> {
 // One output row of a tile (M values, `valid` of them inside the image) in
 // the caller's element type YT (fp16 or bf16).
 template <int M, class YT>
-__device__ __forceinline__ void store_row(YT* dst, const float* y, int valid, float inv) {
+__device__ __forceinline__ void store_row(YT* dst, const float* y, int valid) {
     const uintptr_t a = reinterpret_cast<uintptr_t>(dst);
     if (M == 2 && valid == 2 && (a & 3) == 0) {
-        *reinterpret_cast<uint32_t*>(dst) = pack2<YT>(y[0] * inv, y[1] * inv);
+        *reinterpret_cast<uint32_t*>(dst) = pack2<YT>(y[0], y[1]);
     } else if (M == 4 && valid == 4 && (a & 7) == 0) {
-        *reinterpret_cast<uint2*>(dst) = make_uint2(pack2<YT>(y[0] * inv, y[1] * inv), pack2<YT>(y[2] * inv, y[3] * inv));
+        *reinterpret_cast<uint2*>(dst) = make_uint2(pack2<YT>(y[0], y[1]), pack2<YT>(y[2], y[3]));
     } else {
 #pragma unroll
         for (int j = 0; j < M; ++j)
-            if (j < valid) dst[j] = from_f32<YT>(y[j] * inv);
+            if (j < valid) dst[j] = from_f32<YT>(y[j]);
     }
 }
 
@@ -650,7 +650,6 @@ __device__ __forceinline__ void output_staged_body(const OutDesc* descs, int nde
                 const long long n = ot.n;
                 const int oh0 = th * M, ow0 = tw * M;
                 const int vr = min(M, OH - oh0), vc = min(M, OW - ow0);
-                const float inv = d.scale ? 1.f / d.scale[p] : 1.f;  // exact: scale is a power of two
                 const unsigned char* src = bufs + b * kItemBytes + t * 16 + hh * 8;
                 float m[E][PH];
 #pragma unroll
@@ -663,10 +662,15 @@ __device__ __forceinline__ void output_staged_body(const OutDesc* descs, int nde
 #pragma unroll
                     for (int e = 0; e < E; ++e) mm[e] = m[e][ch];
                     output_tile_transform<TF>(mm, y);
+                    if (d.scale) {
+                        const float inv = 1.f / d.scale[p];  // exact: scale is a power of two
+#pragma unroll
+                        for (int i = 0; i < M * M; ++i) y[i] *= inv;
+                    }
                     YT* o = out + ((n * K + kc) * OH + oh0) * static_cast<long long>(OW) + ow0;
 #pragma unroll
                     for (int i = 0; i < M; ++i)
-                        if (i < vr) store_row<M>(o + static_cast<long long>(i) * OW, &y[i * M], vc, inv);
+                        if (i < vr) store_row<M>(o + static_cast<long long>(i) * OW, &y[i * M], vc);
                 }
             }
             if (d.discard_m) {
@@ -824,7 +828,6 @@ __device__ __forceinline__ void output_staged_body_m24(const OutDesc* descs, int
                 const long long n = ot.n;
                 const int oh0 = th * M, ow0 = tw * M;
                 const int vr = min(M, OH - oh0), vc = min(M, OW - ow0);
-                const float inv = d.scale ? 1.f / d.scale[p] : 1.f;  // exact: scale is a power of two
                 const unsigned char* hsrc = bufs + b * kItemBytes + t * 16 + qd * 4;
                 const unsigned char* lsrc = bufs + b * kItemBytes + kLoBase + t * 8 + qd * 2;
                 // value bits = high 16 | low 8 << 8: one byte permute per
@@ -865,6 +868,11 @@ __device__ __forceinline__ void output_staged_body_m24(const OutDesc* descs, int
                         }
                     }
                 } else {
+                    if (d.scale) {
+                        const float inv = 1.f / d.scale[p];  // exact: scale is a power of two
+#pragma unroll
+                        for (int i = 0; i < M * M; ++i) y2[i] = __fmul2_rn(y2[i], f2(inv));
+                    }
 #pragma unroll
                     for (int ch = 0; ch < 2; ++ch) {
                         const int kc = g * 8 + qd * 2 + ch;
@@ -875,7 +883,7 @@ __device__ __forceinline__ void output_staged_body_m24(const OutDesc* descs, int
                         YT* o = out + ((n * K + kc) * OH + oh0) * static_cast<long long>(OW) + ow0;
 #pragma unroll
                         for (int i = 0; i < M; ++i)
-                            if (i < vr) store_row<M>(o + static_cast<long long>(i) * OW, &y[i * M], vc, inv);
+                            if (i < vr) store_row<M>(o + static_cast<long long>(i) * OW, &y[i * M], vc);
                     }
                 }
             }
@@ -954,9 +962,14 @@ int in_ctas_per_sm(int smem) { return std::max(1, std::min(2, kSmemPerSm / (smem
 // per output row (halo re-reads).
 InBlocking choose_in_blocking(const Geom& g) {
     const int M = g.m, A = g.alpha;
+    // a channel's staged rows take whole 16-byte blocks, padded so that
+    // channels two apart start 8 or 24 banks apart: the four channel pairs
+    // that a warp reads at once then fall in different banks
     auto stride_for = [&](int tb) {
         const int rows = std::min(g.h, tb * M + A - M);
-        return (rows * g.w * 2 + 16 + 15) / 16 * 16;
+        int st = (rows * g.w * 2 + 16 + 15) / 16 * 16;
+        while ((st / 4) % 16 != 4 && (st / 4) % 16 != 12) st += 16;
+        return st;
     };
     InBlocking best{1, g.tiles_h, 8, stride_for(1), 8 * stride_for(1)};
     double best_cost = 1e300;

@@ -123,13 +123,16 @@ def read_m(wg, ptr, E, P, kp, mtype):
     return Mw.transpose(0, 2, 1, 3).reshape(E, P, kp).astype(np.float64)
 
 
+@pytest.mark.parametrize("h,w", [(11, 13), (9, 16)])
 @pytest.mark.parametrize("algo,variant,mfp32", [(1, "F2", 0), (0, "F4", 0), (0, "F4", 1), (0, "F4Ref", 0)])
-def test_transform_kernels_elementwise(wg, monkeypatch, algo, variant, mfp32):
+def test_transform_kernels_elementwise(wg, monkeypatch, algo, variant, mfp32, h, w):
     """U, V and M read back from the workspace, each against its restatement
     (the GEMM otherwise drops V from L2 once it is read, leaving its memory
-    undefined).  F(4x3) stores M in 24 bits by default, in fp32 on request."""
+    undefined).  F(4x3) stores M in 24 bits by default, in fp32 on request.
+    W = 16 takes the input transform's aligned-word reads, W = 13 its 16-bit
+    reads."""
     monkeypatch.setenv("WG_CONV2D_KEEP_WORKSPACE", "1")
-    n, c, h, w, k = 2, 20, 11, 13, 24
+    n, c, k = 2, 20, 24
     x, wt = O.uniform_inputs(31, n, c, h, w, k)
     opts = opts_for(wg, algo, f4_points=1 if variant == "F4Ref" else 0, m_fp32=mfp32)
     y, op = run(wg, x, wt, 1, 1, opts)
