@@ -98,11 +98,14 @@ __device__ __forceinline__ void nh_compute(const NhwcInDesc& d, long long local,
     const long long p0 = ((n - n_base) * d.tiles_h + th0) * tiles_w;  // tiles of this launch's images
     OutT* __restrict__ V = static_cast<OutT*>(d.V);
     const int tasks = ntiles * G * 4;
+    // G is 1-4 and rest below 2^14: rest / 3 by multiply-shift (exact below 2^17)
+    const uint32_t g_shift = static_cast<uint32_t>(G >> 1);
     for (int task = cw * 32 + (threadIdx.x & 31); task < tasks; task += kNhComputeWarps * 32) {
         const int sub = task & 3;
-        const int rest = task >> 2;
-        const int g = rest % G, t = rest / G;
-        const int tr = t / tiles_w, tw = t - tr * tiles_w;
+        const uint32_t rest = static_cast<uint32_t>(task >> 2);
+        const int t = static_cast<int>(G == 3 ? (rest * 43691u) >> 17 : rest >> g_shift);
+        const int g = static_cast<int>(rest) - t * G;
+        const int tr = static_cast<int>(fast_div(d.fd_tw, static_cast<uint32_t>(t))), tw = t - tr * tiles_w;
         // pixel (tr*M + i, tw*M + j) of the box, channels g*8 + sub*2 + {0,1}
         const unsigned char* src = buf + (static_cast<size_t>(tr * M) * bw + tw * M) * cb * 2 + (g * 8 + sub * 2) * 2;
         float2 r[A][A];
@@ -288,6 +291,7 @@ cudaError_t make_nhwc_in_desc(NhwcInDesc& d, const Geom& g, const void* x, void*
     d.V = V;
     d.C = g.c; d.H = g.h; d.W = g.w; d.pad_h = g.pad_h; d.pad_w = g.pad_w;
     d.tiles_h = g.tiles_h; d.tiles_w = g.tiles_w;
+    d.fd_tw = make_fastdiv(static_cast<uint32_t>(g.tiles_w));
     d.Pp = round_rows(g.P);
     d.CG = g.cp / 8;
     d.bw = g.tiles_w * M + A - M;

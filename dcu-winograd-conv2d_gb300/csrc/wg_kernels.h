@@ -218,6 +218,7 @@ struct alignas(64) NhwcInDesc {
     int CG, tb, nbh, cb, bw, rows;
     long long gx;         // work items along (image, tile-row block)
     int gy;               // work items along channel blocks
+    FastDiv fd_tw;        // tile of an item -> (tile row, tile column)
 };
 // cudaErrorNotSupported when C is not a multiple of 8 (TMA strides), the
 // padded row width exceeds one TMA box (256) or two boxes do not fit in
