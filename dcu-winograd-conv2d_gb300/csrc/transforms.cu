@@ -6,7 +6,9 @@
 //   U       U[E][Cp/8][Kp][8]        operand type (fp16 or bf16)
 //   V       V[E][Cp/8][Pp][8]        operand type, P = tiles in the batch,
 //                                    Pp = P rounded up to 8
-//   M       M[E][Kp/8][P][8]  fp16   (F(2x3)),  M[E][Kp/4][P][4]  fp32  (F(4x3))
+//   M       M[E][Kp/8][P][8]  fp16   (F(2x3)),  M[E][Kp/4][P][4]  fp32  (F(4x3) on
+//           request), 24-bit planes H[Kp/8][NB][E][64][8] and L[Kp/8][NB][E][64][8]
+//           (F(4x3) default; NB = ceil(P/64) blocks of 64 tiles)
 //   output  y[N][K][OH][OW]          fp16
 // Cp, Kp are C, K rounded up to 8.  The contraction index is split into
 // 16-byte granules of 8 channels; within an element e, granule g holds one
@@ -542,6 +544,7 @@ __device__ __forceinline__ void store_row(YT* dst, const float* y, int valid) {
 // reads 256 contiguous bytes of shared memory per element, and the NCHW row
 // writes of a warp are contiguous across tiles.
 constexpr int kOsTiles = 64;
+static_assert(kOsTiles == kM24Tiles, "a 24-bit M block is one output-transform work item");
 constexpr int kOsThreads = 32 * 5;
 
 template <class TF> constexpr int os_smem_bytes() { return 128 + 2 * TF::ALPHA * TF::ALPHA * kOsTiles * 16; }
@@ -740,11 +743,13 @@ __device__ __forceinline__ void output_tile_transform2(const float2 (&m)[TF::ALP
     for (int i = 0; i < M; ++i) At2<TF>::run(&t[i * A], 1, &y[i * M], 1);  // (A^T m) A
 }
 
-// 24-bit M (high plane H[e][KG][P][8] of 16-bit words, low plane
-// L[e][KG][Pp][8] of bytes): a work item is 64 tiles x one granule of 8
-// channels; warp 8 stages the item's E high runs (up to 1 KB) and E low runs
-// (up to 512 B) into one half of a double buffer while warps 0-7 transform the
-// previous item: thread = (tile, channel pair), so a warp reads 128
+// 24-bit M (high plane H[KG][NB][E][64][8] of 16-bit words, low plane
+// L[KG][NB][E][64][8] of bytes, NB blocks of 64 tiles): a work item is one
+// block of 64 tiles x one granule of 8 channels, whose E high runs (1 KB
+// each) and E low runs (512 B each) are contiguous: warp 8 stages them with
+// two bulk copies into one half of a double buffer while warps 0-7 transform
+// the previous item (2E copies of the single runs took 36.9 against 28.7 us
+// on N32 C256 56x56 K256): thread = (tile, channel pair), so a warp reads 128
 // contiguous bytes of the high run and 64 of the low run per element and
 // rebuilds each value as high << 16 | low << 8.
 constexpr int kOs24Threads = 32 * 9;
@@ -780,7 +785,8 @@ __device__ __forceinline__ void output_staged_body_m24(const OutDesc* descs, int
         int k = 0;
         for (long long gitem = blockIdx.x; gitem < total; gitem += gridDim.x, ++k) {
             const int b = k & 1;
-            if (!mbar_wait(&empty[b], ((k >> 1) & 1) ^ 1u, abort_flag, err, ERR_SITE_EMPTY)) break;
+            const uint32_t ph = (k >> 1) & 1;
+            if (!mbar_wait(&empty[b], ph ^ 1u, abort_flag, err, ERR_SITE_EMPTY)) break;
             const OutDesc& d = out_desc_of(descs, ndesc, gitem);
             const long long item = gitem - d.blk_begin;
             const long long P = d.P;
@@ -789,30 +795,25 @@ __device__ __forceinline__ void output_staged_body_m24(const OutDesc* descs, int
             const OutItem oi = out_item(d, item);
             const long long p0 = oi.p0;
             const int g = oi.g;
-            const long long nt = min(static_cast<long long>(kOsTiles), P - p0);
-            const uint32_t hbytes = static_cast<uint32_t>(nt) * 16u;
-            // the low plane's rows are padded to a multiple of 8 tiles: an
-            // even tile count keeps the copy a multiple of 16 bytes
-            const uint32_t lbytes = static_cast<uint32_t>((nt + 1) & ~1LL) * 8u;
-            uint32_t mine = 0;
-            for (int e = lane; e < E; e += 32) mine += hbytes + lbytes;
+            // the item's E runs are one contiguous range in each plane (the
+            // last block's rows past P are padding, copied and not read)
+            const long long run = (static_cast<long long>(g) * d.m_nb + p0 / kOsTiles) * E;
+            const uint32_t mine = lane == 0 ? E * kOsTiles * 16u : lane == 1 ? E * kOsTiles * 8u : 0u;
             if (mine) fence_proxy_async_smem();  // earlier reads of this buffer before the async writes
             mbar_arrive_expect_tx(&full[b], mine);
             const uint64_t drop = l2_evict_first();   // M is read once
-            for (int e = lane; e < E; e += 32) {
-                const long long gi = static_cast<long long>(e) * KG + g;
-                bulk_g2s_hint(bufs + b * kItemBytes + e * (kOsTiles * 16), Mb + (gi * P + p0) * 16, hbytes, &full[b],
-                              drop);
-                bulk_g2s_hint(bufs + b * kItemBytes + kLoBase + e * (kOsTiles * 8), Mb + d.m_lo + (gi * d.m_pp + p0) * 8,
-                              lbytes, &full[b], drop);
-            }
+            if (lane == 0)
+                bulk_g2s_hint(bufs + b * kItemBytes, Mb + run * (kOsTiles * 16), mine, &full[b], drop);
+            else if (lane == 1)
+                bulk_g2s_hint(bufs + b * kItemBytes + kLoBase, Mb + d.m_lo + run * (kOsTiles * 8), mine, &full[b], drop);
         }
     } else {
         const int t = threadIdx.x >> 2, qd = threadIdx.x & 3;
         int k = 0;
         for (long long gitem = blockIdx.x; gitem < total; gitem += gridDim.x, ++k) {
             const int b = k & 1;
-            if (!mbar_wait(&full[b], (k >> 1) & 1, abort_flag, err, ERR_SITE_FULL)) break;
+            const uint32_t ph = (k >> 1) & 1;
+            if (!mbar_wait(&full[b], ph, abort_flag, err, ERR_SITE_FULL)) break;
             const OutDesc& d = out_desc_of(descs, ndesc, gitem);
             const long long item = gitem - d.blk_begin;
             const long long P = d.P;
@@ -873,36 +874,48 @@ __device__ __forceinline__ void output_staged_body_m24(const OutDesc* descs, int
 #pragma unroll
                         for (int i = 0; i < M * M; ++i) y2[i] = __fmul2_rn(y2[i], f2(inv));
                     }
+                    // a whole tile of a whole granule with 8-byte aligned rows
+                    // (OW a multiple of 4, y 8-byte aligned): M row stores per
+                    // channel without per-row checks
+                    const bool whole = M == 4 && vr == M && vc == M && g * 8 + 8 <= K && (OW & 3) == 0 &&
+                                       (reinterpret_cast<uintptr_t>(out) & 7) == 0;
+                    if (whole) {
 #pragma unroll
-                    for (int ch = 0; ch < 2; ++ch) {
-                        const int kc = g * 8 + qd * 2 + ch;
-                        if (kc >= K) break;
-                        float y[M * M];
+                        for (int ch = 0; ch < 2; ++ch) {
+                            YT* o = out + ((n * K + g * 8 + qd * 2 + ch) * OH + oh0) * static_cast<long long>(OW) + ow0;
 #pragma unroll
-                        for (int i = 0; i < M * M; ++i) y[i] = ch == 0 ? y2[i].x : y2[i].y;
-                        YT* o = out + ((n * K + kc) * OH + oh0) * static_cast<long long>(OW) + ow0;
+                            for (int i = 0; i < M; ++i) {
+                                const float2* r = &y2[i * M];
+                                *reinterpret_cast<uint2*>(o + static_cast<long long>(i) * OW) =
+                                    ch == 0 ? make_uint2(pack2<YT>(r[0].x, r[1].x), pack2<YT>(r[2].x, r[3].x))
+                                            : make_uint2(pack2<YT>(r[0].y, r[1].y), pack2<YT>(r[2].y, r[3].y));
+                            }
+                        }
+                    } else {
 #pragma unroll
-                        for (int i = 0; i < M; ++i)
-                            if (i < vr) store_row<M>(o + static_cast<long long>(i) * OW, &y[i * M], vc);
+                        for (int ch = 0; ch < 2; ++ch) {
+                            const int kc = g * 8 + qd * 2 + ch;
+                            if (kc >= K) break;
+                            float y[M * M];
+#pragma unroll
+                            for (int i = 0; i < M * M; ++i) y[i] = ch == 0 ? y2[i].x : y2[i].y;
+                            YT* o = out + ((n * K + kc) * OH + oh0) * static_cast<long long>(OW) + ow0;
+#pragma unroll
+                            for (int i = 0; i < M; ++i)
+                                if (i < vr) store_row<M>(o + static_cast<long long>(i) * OW, &y[i * M], vc);
+                        }
                     }
                 }
             }
             if (d.discard_m) {
-                // the item's runs are in shared memory and nothing reads them
-                // again: drop the 128-byte lines that lie wholly inside them
-                const long long p0 = oi.p0;
-                const long long nt = min(static_cast<long long>(kOsTiles), P - p0);
-                const unsigned char* Mb = static_cast<const unsigned char*>(d.Mw);
-                for (int i = threadIdx.x; i < E * 12; i += 256) {
-                    const int e = i / 12, l = i % 12;
-                    const long long gi = static_cast<long long>(e) * KG + g;
-                    const bool hi = l < 8;
-                    const long long s0 = hi ? (gi * P + p0) * 16 : d.m_lo + (gi * d.m_pp + p0) * 8;
-                    const long long nbytes = hi ? nt * 16 : nt * 8;
-                    const long long first = (s0 + 127) & ~127LL, end = (s0 + nbytes) & ~127LL;
-                    const int li = hi ? l : l - 8;
-                    if (first + (li + 1) * 128LL <= end) discard_l2_line(Mb + first + li * 128LL);
-                }
+                // the item's ranges (E KB of the high plane, E/2 KB of the low
+                // one, 128-byte aligned) are in shared memory and nothing reads
+                // them again: drop their L2 lines
+                const long long run = (static_cast<long long>(g) * d.m_nb + oi.p0 / kOsTiles) * E;
+                const unsigned char* hb = static_cast<const unsigned char*>(d.Mw) + run * (kOsTiles * 16);
+                const unsigned char* lb = static_cast<const unsigned char*>(d.Mw) + d.m_lo + run * (kOsTiles * 8);
+                for (int i = threadIdx.x; i < E * 12; i += 256)
+                    discard_l2_line(i < E * 8 ? hb + i * 128 : lb + (i - E * 8) * 128);
             }
             __syncwarp();
             if (lane == 0) mbar_arrive(&empty[b]);
@@ -1168,7 +1181,7 @@ OutDesc make_out_desc(const Geom& g, MType mt, const void* Mw, void* out, const 
     d.P = g.P;
     d.KG = mt == MType::F32 ? g.kp / 4 : g.kp / 8;
     d.m_lo = m24_lo_offset(static_cast<long long>(g.alpha) * g.alpha, g.P, g.kp);
-    d.m_pp = round_rows(g.P);
+    d.m_nb = m24_blocks(g.P);
     d.gx = (g.P + kOsTiles - 1) / kOsTiles;
     d.gy = d.KG;
     d.blk_begin = 0;
@@ -1182,7 +1195,7 @@ OutDesc make_out_desc(const Geom& g, MType mt, const void* Mw, void* out, const 
     // 22.5 -> 23.8 us).  WG_CONV2D_KEEP_WORKSPACE=1 keeps M readable after the
     // call.
     const char* keep_ws = std::getenv("WG_CONV2D_KEEP_WORKSPACE");
-    d.discard_m = !(keep_ws && std::atoi(keep_ws) != 0) &&
+    d.discard_m = !(keep_ws && std::atoi(keep_ws) != 0) && (reinterpret_cast<uintptr_t>(Mw) & 127) == 0 &&
                   m_bytes(mt, static_cast<long long>(g.alpha) * g.alpha, g.P, g.kp) > l2_cache_bytes();
     return d;
 }

@@ -29,11 +29,11 @@ enum class OpType : int { F16 = 0, BF16 = 1 };
 //   F32  M[e][Kp/4][P][4] fp32 (granule layout), or M[e][P][Kp] row-major for
 //        the channels-last output path;
 //   F24  each fp32 value rounded to nearest at 24 bits and split in two
-//        planes: its upper 16 bits in H[e][Kp/8][P][8] (16-byte granules of 8
-//        channels, the fp16 layout) and its next 8 bits in
-//        L[e][Kp/8][Pp][8] (8-byte granules, Pp = P rounded up to 8), L
-//        right after H.  Relative rounding 2^-17 (fp16 M: 2^-12) for 3/4 of
-//        the fp32 bytes; the F(4x3) default.
+//        planes: its upper 16 bits in H[Kp/8][NB][E][64][8] (16-byte granules
+//        of 8 channels, blocks of 64 tiles, NB = ceil(P/64)) and its next 8
+//        bits in L[Kp/8][NB][E][64][8] (8-byte granules), L right after H.
+//        Relative rounding 2^-17 (fp16 M: 2^-12) for 3/4 of the fp32 bytes;
+//        the F(4x3) default.
 enum class MType : int { F16 = 0, F32 = 1, F24 = 2 };
 
 inline const char* mtype_name(MType t) { return t == MType::F16 ? "fp16" : t == MType::F32 ? "fp32" : "24-bit"; }
@@ -56,14 +56,21 @@ Geom make_geom(int n, int c, int h, int w, int k, int pad_h, int pad_w, int m);
 // 128-byte rows of 8 tiles).
 inline long long round_rows(long long P) { return (P + 7) / 8 * 8; }
 
+// 24-bit M is stored in blocks of kM24Tiles tiles (the output transform's
+// work item): H[Kp/8][NB][E][kM24Tiles][8] of 16-bit words, then
+// L[Kp/8][NB][E][kM24Tiles][8] of bytes, NB = ceil(P / kM24Tiles), so the E
+// runs of one (granule, tile block) are one contiguous range in each plane.
+constexpr int kM24Tiles = 64;
+inline long long m24_blocks(long long P) { return (P + kM24Tiles - 1) / kM24Tiles; }
+
 // Bytes of M for E elements, P tiles and Kp (a multiple of 8) channels.
 inline long long m_bytes(MType t, long long E, long long P, long long Kp) {
     if (t == MType::F16) return E * P * Kp * 2;
     if (t == MType::F32) return E * P * Kp * 4;
-    return E * P * Kp * 2 + E * round_rows(P) * Kp;
+    return E * m24_blocks(P) * kM24Tiles * Kp * 3;
 }
 // Byte offset of the low plane of 24-bit M.
-inline long long m24_lo_offset(long long E, long long P, long long Kp) { return E * P * Kp * 2; }
+inline long long m24_lo_offset(long long E, long long P, long long Kp) { return E * m24_blocks(P) * kM24Tiles * Kp * 2; }
 
 // U[e][Cp/8][Kp][8] = G g G^T, from KCRS fp16 weights; fp32 arithmetic, result
 // in the operand type; zero for c >= C or k >= K.
@@ -136,7 +143,7 @@ struct OutDesc {
     long long blk_begin;
     int discard_m;        // M is read once here: drop its L2 lines without write-back
     long long m_lo;       // 24-bit M: byte offset of the low plane from Mw
-    long long m_pp;       // 24-bit M: rows of the low plane per granule (P rounded up to 8)
+    long long m_nb;       // 24-bit M: tile blocks per granule
     FastDiv fd_kg, fd_tw, fd_th;   // item -> (tile block, granule), tile -> (image, row, column)
 };
 
@@ -173,7 +180,7 @@ struct alignas(64) GemmDesc {
     int m_row;           // 1: M[e][P][Kp] (rows of output channels, NHWC output path)
     int kp;
     long long m_lo;      // 24-bit M: byte offset of the low plane from Mw
-    int m_pp;            // 24-bit M: rows of the low plane per granule
+    int m_nb;            // 24-bit M: tile blocks per granule
     int keep_m;          // M fits in L2: store it with the evict_last priority
     // V[E][v_cg][v_pp][8] is read by this GEMM only (one block of output
     // channels): its lines are discarded from L2 once a tile is done, so the

@@ -107,18 +107,24 @@ def _dev_array(wg, ptr, count, dtype):
 
 def read_m(wg, ptr, E, P, kp, mtype):
     """M read back from the workspace as float64 [E][P][Kp]: fp16
-    M[E][Kp/8][P][8], fp32 M[E][Kp/4][P][4], or 24-bit M (upper 16 bits of
-    each rounded fp32 value in H[E][Kp/8][P][8], the next 8 bits in
-    L[E][Kp/8][Pp][8] right after H)."""
+    M[E][Kp/8][P][8], fp32 M[E][Kp/4][P][4], or 24-bit M in blocks of 64
+    tiles (upper 16 bits of each rounded fp32 value in
+    H[Kp/8][NB][E][64][8], the next 8 bits in L[Kp/8][NB][E][64][8] right
+    after H, NB = ceil(P / 64))."""
     if mtype == "fp16":
         Mw = _dev_array(wg, ptr, E * P * kp, np.float16).reshape(E, kp // 8, P, 8)
     elif mtype == "fp32":
         Mw = _dev_array(wg, ptr, E * P * kp, np.float32).reshape(E, kp // 4, P, 4)
     else:
-        Pp = (P + 7) // 8 * 8
-        raw = _dev_array(wg, ptr, 2 * E * P * kp + E * Pp * kp, np.uint8)
-        hi = raw[:2 * E * P * kp].view(np.uint16).reshape(E, kp // 8, P, 8).astype(np.uint32)
-        lo = raw[2 * E * P * kp:].reshape(E, kp // 8, Pp, 8)[:, :, :P].astype(np.uint32)
+        nb = (P + 63) // 64
+        raw = _dev_array(wg, ptr, 3 * E * nb * 64 * kp, np.uint8)
+
+        def plane(a):
+            a = a.reshape(kp // 8, nb, E, 64, 8).transpose(2, 0, 1, 3, 4)
+            return a.reshape(E, kp // 8, nb * 64, 8)[:, :, :P].astype(np.uint32)
+
+        hi = plane(raw[:2 * E * nb * 64 * kp].view(np.uint16))
+        lo = plane(raw[2 * E * nb * 64 * kp:])
         Mw = ((hi << 16) | (lo << 8)).view(np.float32)
     return Mw.transpose(0, 2, 1, 3).reshape(E, P, kp).astype(np.float64)
 
