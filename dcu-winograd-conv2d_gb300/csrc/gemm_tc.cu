@@ -97,8 +97,8 @@ __device__ __forceinline__ void store32<float>(float* Mw, const uint32_t (&r)[32
 }
 
 // 24-bit M: tag type of the split-plane storage (upper 16 bits of each
-// rounded fp32 value in H[Kp/8][NB][E][64][8], next 8 bits in
-// L[Kp/8][NB][E][64][8]: blocks of 64 tiles, NB = ceil(P/64)).
+// rounded fp32 value in H[NB][Kp/8][E][64][8], next 8 bits in
+// L[NB][Kp/8][E][64][8]: blocks of 64 tiles, NB = ceil(P/64)).
 struct M24 {};
 
 // 24-bit M: 32 accumulator columns (four granules of 8 channels) of tile row
@@ -109,10 +109,9 @@ struct M24 {};
 // store per granule); a warp's 32 rows lie in one 64-tile block, so its
 // stores cover 512 and 256 contiguous bytes.
 __device__ __forceinline__ void store32_m24(unsigned char* Mb, const uint32_t (&r)[32], long long p, int k0,
-                                            int kg_count, int e, int E, long long m_nb, long long m_lo, uint64_t pol) {
+                                            int kg_count, int e, int E, long long m_lo, uint64_t pol) {
     const int g0 = k0 / 8;
-    const long long gstep = m_nb * E * 64;   // rows from one granule's blocks to the next
-    const long long row0 = ((static_cast<long long>(g0) * m_nb + (p >> 6)) * E + e) * 64 + (p & 63);
+    const long long row0 = (((p >> 6) * kg_count + g0) * E + e) * 64 + (p & 63);
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
         if (g0 + j >= kg_count) break;
@@ -124,7 +123,7 @@ __device__ __forceinline__ void store32_m24(unsigned char* Mb, const uint32_t (&
         const uint32_t l01 = __byte_perm(v[0], v[1], 0x5151), l23 = __byte_perm(v[2], v[3], 0x5151);
         const uint32_t l45 = __byte_perm(v[4], v[5], 0x5151), l67 = __byte_perm(v[6], v[7], 0x5151);
         const uint2 lo = make_uint2(__byte_perm(l01, l23, 0x5410), __byte_perm(l45, l67, 0x5410));
-        const long long row = row0 + j * gstep;
+        const long long row = row0 + j * E * 64;
         st_hint_v4(Mb + row * 16, hi, pol);
         st_hint_v2(Mb + m_lo + row * 8, lo, pol);
     }
@@ -374,7 +373,7 @@ __device__ __forceinline__ void gemm_body(const GemmDesc* __restrict__ descs, in
             const long long P = d.P;
             const int kg_count = d.kg_count;
             const int m_row = d.m_row, kp = d.kp;
-            const long long m_lo = d.m_lo, m_nb = d.m_nb;
+            const long long m_lo = d.m_lo;
             if (!mbar_wait(&tfull[acc], acc_phase, abort_flag, err, ERR_SITE_TMEM_FULL)) break;
             tc_fence_after();
             const long long p = static_cast<long long>(it.mb) * kBM + row;
@@ -414,7 +413,7 @@ __device__ __forceinline__ void gemm_body(const GemmDesc* __restrict__ descs, in
                 } else if (p < P) {
                     if constexpr (std::is_same<MT, M24>::value)
                         store32_m24(static_cast<unsigned char*>(d.Mw), r[ch & 1], p, it.nb * BN + col0 + ch * 32,
-                                    kg_count, it.e, d.E, m_nb, m_lo, m_pol);
+                                    kg_count, it.e, d.E, m_lo, m_pol);
                     else
                         store32<MT>(Mw, r[ch & 1], P, p, it.nb * BN + col0 + ch * 32, kg_count, it.e, m_pol);
                 }
@@ -563,7 +562,6 @@ cudaError_t make_gemm_desc(GemmDesc& d, OpType op, int E, long long P, int K, in
     d.P = static_cast<int>(P);
     d.kg_count = mt == MType::F32 ? Kp / 4 : Kp / 8;
     d.m_lo = m24_lo_offset(E, P, Kp);
-    d.m_nb = static_cast<int>(m24_blocks(P));
     d.m_row = m_row ? 1 : 0;
     d.kp = Kp;
     d.keep_m = 0;   // plan_gemm decides for single launches; grouped ones stream M

@@ -7,7 +7,7 @@
 //   V       V[E][Cp/8][Pp][8]        operand type, P = tiles in the batch,
 //                                    Pp = P rounded up to 8
 //   M       M[E][Kp/8][P][8]  fp16   (F(2x3)),  M[E][Kp/4][P][4]  fp32  (F(4x3) on
-//           request), 24-bit planes H[Kp/8][NB][E][64][8] and L[Kp/8][NB][E][64][8]
+//           request), 24-bit planes H[NB][Kp/8][E][64][8] and L[NB][Kp/8][E][64][8]
 //           (F(4x3) default; NB = ceil(P/64) blocks of 64 tiles)
 //   output  y[N][K][OH][OW]          fp16
 // Cp, Kp are C, K rounded up to 8.  The contraction index is split into
@@ -743,8 +743,8 @@ __device__ __forceinline__ void output_tile_transform2(const float2 (&m)[TF::ALP
     for (int i = 0; i < M; ++i) At2<TF>::run(&t[i * A], 1, &y[i * M], 1);  // (A^T m) A
 }
 
-// 24-bit M (high plane H[KG][NB][E][64][8] of 16-bit words, low plane
-// L[KG][NB][E][64][8] of bytes, NB blocks of 64 tiles): a work item is one
+// 24-bit M (high plane H[NB][KG][E][64][8] of 16-bit words, low plane
+// L[NB][KG][E][64][8] of bytes, NB blocks of 64 tiles): a work item is one
 // block of 64 tiles x one granule of 8 channels, whose E high runs (1 KB
 // each) and E low runs (512 B each) are contiguous: warp 8 stages them with
 // two bulk copies into one half of a double buffer while warps 0-7 transform
@@ -797,7 +797,7 @@ __device__ __forceinline__ void output_staged_body_m24(const OutDesc* descs, int
             const int g = oi.g;
             // the item's E runs are one contiguous range in each plane (the
             // last block's rows past P are padding, copied and not read)
-            const long long run = (static_cast<long long>(g) * d.m_nb + p0 / kOsTiles) * E;
+            const long long run = (p0 / kOsTiles * KG + g) * E;
             const uint32_t mine = lane == 0 ? E * kOsTiles * 16u : lane == 1 ? E * kOsTiles * 8u : 0u;
             if (mine) fence_proxy_async_smem();  // earlier reads of this buffer before the async writes
             mbar_arrive_expect_tx(&full[b], mine);
@@ -911,7 +911,7 @@ __device__ __forceinline__ void output_staged_body_m24(const OutDesc* descs, int
                 // the item's ranges (E KB of the high plane, E/2 KB of the low
                 // one, 128-byte aligned) are in shared memory and nothing reads
                 // them again: drop their L2 lines
-                const long long run = (static_cast<long long>(g) * d.m_nb + oi.p0 / kOsTiles) * E;
+                const long long run = (static_cast<long long>(oi.p0) / kOsTiles * KG + g) * E;
                 const unsigned char* hb = static_cast<const unsigned char*>(d.Mw) + run * (kOsTiles * 16);
                 const unsigned char* lb = static_cast<const unsigned char*>(d.Mw) + d.m_lo + run * (kOsTiles * 8);
                 for (int i = threadIdx.x; i < E * 12; i += 256)
@@ -1181,7 +1181,6 @@ OutDesc make_out_desc(const Geom& g, MType mt, const void* Mw, void* out, const 
     d.P = g.P;
     d.KG = mt == MType::F32 ? g.kp / 4 : g.kp / 8;
     d.m_lo = m24_lo_offset(static_cast<long long>(g.alpha) * g.alpha, g.P, g.kp);
-    d.m_nb = m24_blocks(g.P);
     d.gx = (g.P + kOsTiles - 1) / kOsTiles;
     d.gy = d.KG;
     d.blk_begin = 0;

@@ -29,9 +29,9 @@ enum class OpType : int { F16 = 0, BF16 = 1 };
 //   F32  M[e][Kp/4][P][4] fp32 (granule layout), or M[e][P][Kp] row-major for
 //        the channels-last output path;
 //   F24  each fp32 value rounded to nearest at 24 bits and split in two
-//        planes: its upper 16 bits in H[Kp/8][NB][E][64][8] (16-byte granules
+//        planes: its upper 16 bits in H[NB][Kp/8][E][64][8] (16-byte granules
 //        of 8 channels, blocks of 64 tiles, NB = ceil(P/64)) and its next 8
-//        bits in L[Kp/8][NB][E][64][8] (8-byte granules), L right after H.
+//        bits in L[NB][Kp/8][E][64][8] (8-byte granules), L right after H.
 //        Relative rounding 2^-17 (fp16 M: 2^-12) for 3/4 of the fp32 bytes;
 //        the F(4x3) default.
 enum class MType : int { F16 = 0, F32 = 1, F24 = 2 };
@@ -57,9 +57,10 @@ Geom make_geom(int n, int c, int h, int w, int k, int pad_h, int pad_w, int m);
 inline long long round_rows(long long P) { return (P + 7) / 8 * 8; }
 
 // 24-bit M is stored in blocks of kM24Tiles tiles (the output transform's
-// work item): H[Kp/8][NB][E][kM24Tiles][8] of 16-bit words, then
-// L[Kp/8][NB][E][kM24Tiles][8] of bytes, NB = ceil(P / kM24Tiles), so the E
-// runs of one (granule, tile block) are one contiguous range in each plane.
+// work item): H[NB][Kp/8][E][kM24Tiles][8] of 16-bit words, then
+// L[NB][Kp/8][E][kM24Tiles][8] of bytes, NB = ceil(P / kM24Tiles), so the E
+// runs of one (tile block, granule) are one contiguous range in each plane
+// and the granules of one tile block lie together.
 constexpr int kM24Tiles = 64;
 inline long long m24_blocks(long long P) { return (P + kM24Tiles - 1) / kM24Tiles; }
 
@@ -143,7 +144,6 @@ struct OutDesc {
     long long blk_begin;
     int discard_m;        // M is read once here: drop its L2 lines without write-back
     long long m_lo;       // 24-bit M: byte offset of the low plane from Mw
-    long long m_nb;       // 24-bit M: tile blocks per granule
     FastDiv fd_kg, fd_tw, fd_th;   // item -> (tile block, granule), tile -> (image, row, column)
 };
 
@@ -180,7 +180,6 @@ struct alignas(64) GemmDesc {
     int m_row;           // 1: M[e][P][Kp] (rows of output channels, NHWC output path)
     int kp;
     long long m_lo;      // 24-bit M: byte offset of the low plane from Mw
-    int m_nb;            // 24-bit M: tile blocks per granule
     int keep_m;          // M fits in L2: store it with the evict_last priority
     // V[E][v_cg][v_pp][8] is read by this GEMM only (one block of output
     // channels): its lines are discarded from L2 once a tile is done, so the

@@ -109,7 +109,7 @@ def read_m(wg, ptr, E, P, kp, mtype):
     """M read back from the workspace as float64 [E][P][Kp]: fp16
     M[E][Kp/8][P][8], fp32 M[E][Kp/4][P][4], or 24-bit M in blocks of 64
     tiles (upper 16 bits of each rounded fp32 value in
-    H[Kp/8][NB][E][64][8], the next 8 bits in L[Kp/8][NB][E][64][8] right
+    H[NB][Kp/8][E][64][8], the next 8 bits in L[NB][Kp/8][E][64][8] right
     after H, NB = ceil(P / 64))."""
     if mtype == "fp16":
         Mw = _dev_array(wg, ptr, E * P * kp, np.float16).reshape(E, kp // 8, P, 8)
@@ -120,7 +120,7 @@ def read_m(wg, ptr, E, P, kp, mtype):
         raw = _dev_array(wg, ptr, 3 * E * nb * 64 * kp, np.uint8)
 
         def plane(a):
-            a = a.reshape(kp // 8, nb, E, 64, 8).transpose(2, 0, 1, 3, 4)
+            a = a.reshape(nb, kp // 8, E, 64, 8).transpose(2, 1, 0, 3, 4)
             return a.reshape(E, kp // 8, nb * 64, 8)[:, :, :P].astype(np.uint32)
 
         hi = plane(raw[:2 * E * nb * 64 * kp].view(np.uint16))
