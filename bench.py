@@ -325,7 +325,7 @@ def algorithmic_work(name, geo, m_bytes_per_value=None):
       row4x3            x + U1 (2*18*C*K) + y;       FLOPs 2*18*RT*C*K over
                         RT = N*OH*ceil(OW/4) row tiles
     M is counted at `m_bytes_per_value` bytes per value (3 for the 24-bit
-    F(4x3) default, 4 for fp32, 2 for fp16).
+    F(4x3) default, stored in blocks of 64 tiles; 4 for fp32, 2 for fp16).
     Returns (algorithmic bytes, design bytes, FLOPs, formula)."""
     n, c, h, w, k, m = geo
     oh, ow = h, w  # pad 1
@@ -333,7 +333,8 @@ def algorithmic_work(name, geo, m_bytes_per_value=None):
     E = (m + 2) ** 2
     mb = m_bytes_per_value or (3.0 if m == 4 else 2.0)
     x_b, y_b = 2.0 * n * c * h * w, 2.0 * n * k * oh * ow
-    v_b, u_b, m_b = 2.0 * E * tiles * c, 2.0 * E * c * k, mb * E * tiles * k
+    m_tiles = math.ceil(tiles / 64) * 64 if mb == 3.0 else tiles
+    v_b, u_b, m_b = 2.0 * E * tiles * c, 2.0 * E * c * k, mb * E * m_tiles * k
     if name == "gemm_tcgen05":
         return v_b + u_b, v_b + u_b + m_b, 2.0 * E * tiles * c * k, f"V + U (design adds M {m_b / 1e6:.1f} MB)"
     if name == "fused2x3":
@@ -578,7 +579,7 @@ def our_arm(args):
     dom_ms = tot[dominant] / launches_of_dom
     m = 4 if algo in (wg.ALGO_4X3, wg.ALGO_4X3_ROW) else 2
     pk, pk_kind = peaks()
-    mbv = 2.0 if m == 2 else (4.0 if (args.m_fp32 or args.nhwc) else 3.0)
+    mbv = 2.0 if m == 2 else (4.0 if args.m_fp32 else 3.0)
     roof = roofline_for(dominant, wg, (n, c, h, w, k, m), dom_ms, pk, pk_kind, mbv)
     traffic = committed_traffic(dominant, args.workload)
     roof["traffic"] = traffic
@@ -710,7 +711,7 @@ def our_arm(args):
                    "input": f"{xdist}, filter {wdist}",
                    "l2": f"{nsets} rotating input/output sets ({nsets * (in_bytes + out_bytes) / 2**20:.0f} MiB) > L2",
                    "layout": "NHWC" if args.nhwc else "NCHW",
-                   "m_storage": "fp32" if (args.m_fp32 or args.nhwc) else "24-bit (F(4x3)) / fp16 (F(2x3))",
+                   "m_storage": "fp32" if args.m_fp32 else "24-bit (F(4x3)) / fp16 (F(2x3))",
                    "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
         "latency_us": {"p50": lat[len(lat) // 2] * 1e3, "p99": lat[min(len(lat) - 1, int(0.99 * len(lat)))] * 1e3},
         "kernel_ms": kernel_ms,
