@@ -545,21 +545,28 @@ def our_arm(args):
     sampler = ClockSampler(local)
     sampler.start()
     load_phase(lambda i: ops[i % nsets](sptr), device)
-    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     if dist:
         dist.barrier()
     torch.cuda.synchronize(device)
+    # the timed steps are queued back to back with events only at the two
+    # ends: an event between two calls would keep the next call's first kernel
+    # from being scheduled behind the previous call's last one
     t_start = torch.cuda.Event(enable_timing=True)
     t_end = torch.cuda.Event(enable_timing=True)
     t_start.record(stream)
     for i in range(args.steps):
-        evs[i][0].record(stream)
         ops[i % nsets](sptr)
-        evs[i][1].record(stream)
     t_end.record(stream)
     torch.cuda.synchronize(device)
     if dist:
         dist.barrier()
+    # per-call latency (p50 / p99): the same calls again, each between events
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    for i in range(args.steps):
+        evs[i][0].record(stream)
+        ops[i % nsets](sptr)
+        evs[i][1].record(stream)
+    torch.cuda.synchronize(device)
     clocks = with_window(sampler.stop())
     per_step = [a.elapsed_time(b) for a, b in evs]
     total_ms, value = replica_throughput(t_start.elapsed_time(t_end), flops, args.steps, world, dist, device)
