@@ -129,14 +129,15 @@ def read_m(wg, ptr, E, P, kp, mtype):
     return Mw.transpose(0, 2, 1, 3).reshape(E, P, kp).astype(np.float64)
 
 
-@pytest.mark.parametrize("h,w", [(11, 13), (9, 16)])
+@pytest.mark.parametrize("h,w", [(11, 13), (9, 16), (24, 24)])
 @pytest.mark.parametrize("algo,variant,mfp32", [(1, "F2", 0), (0, "F4", 0), (0, "F4", 1), (0, "F4Ref", 0)])
 def test_transform_kernels_elementwise(wg, monkeypatch, algo, variant, mfp32, h, w):
     """U, V and M read back from the workspace, each against its restatement
     (the GEMM otherwise drops V from L2 once it is read, leaving its memory
     undefined).  F(4x3) stores M in 24 bits by default, in fp32 on request.
-    W = 16 takes the input transform's aligned-word reads, W = 13 its 16-bit
-    reads."""
+    W = 16 and 24 take the input transform's aligned-word reads, W = 13 its
+    16-bit reads; 24 x 24 gives F(4x3) 72 tiles, two 64-tile blocks of 24-bit
+    M with a partial last one."""
     monkeypatch.setenv("WG_CONV2D_KEEP_WORKSPACE", "1")
     n, c, k = 2, 20, 24
     x, wt = O.uniform_inputs(31, n, c, h, w, k)
