@@ -235,7 +235,24 @@ __device__ __forceinline__ void gemm_body(const GemmDesc* __restrict__ descs, in
         *abort_flag = 0;
         fence_barrier_init();
     }
-    pdl_wait();     // V and U written, earlier readers of M done
+    // The first resident U block is read before the wait: U comes from the
+    // filter transform, which completed before the kernel ahead of this one
+    // (the input transform) passed its own wait and released this grid, so
+    // only V depends on the kernel ahead; the copy overlaps that kernel's tail.
+    int first_key = -1;
+    if constexpr (RESB) {
+        if (threadIdx.x == 0 && t_lo < t_hi) {   // the producer thread (warp 0, lane 0)
+            int pi0 = 0;
+            const Item it0 = locate_item<RESB>(descs, ndesc, t_lo, pi0);
+            const GemmDesc& d0 = descs[pi0];
+            tma_prefetch_desc(&d0.tmB);
+            mbar_arrive_expect_tx(bfull, static_cast<uint32_t>(d0.k_blocks) * Cfg::kTileB);
+            for (int kb = 0; kb < d0.k_blocks; ++kb)
+                tma_load_4d(sB + kb * Cfg::kTileB, &d0.tmB, bfull, 0, it0.nb * (BN / 8), kb * 8, it0.e);
+            first_key = it0.e * d0.n_blocks + it0.nb;
+        }
+    }
+    pdl_wait();     // V written, earlier readers of M done
     pdl_trigger();
     if (warp == 1) tmem_alloc(tmem_slot, Cfg::kTmemCols);
     tc_fence_before();
@@ -249,7 +266,7 @@ __device__ __forceinline__ void gemm_body(const GemmDesc* __restrict__ descs, in
             int stage = 0;
             uint32_t phase = 0;
             int pi = 0, prefetched = -1;
-            int bkey = -1;          // (element, channel block) of the resident U
+            int bkey = first_key;   // (element, channel block) of the resident U
             uint32_t bphase = 0;
             for (long long t = t_lo; t < t_hi; t += t_step) {
                 const Item it = locate_item<RESB>(descs, ndesc, t, pi);
