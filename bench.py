@@ -717,6 +717,8 @@ def our_arm(args):
                    "algo": wg.ALGO_NAMES[algo], "selection": args.algo, "accumulate": "fp32",
                    "input": f"{xdist}, filter {wdist}",
                    "l2": f"{nsets} rotating input/output sets ({nsets * (in_bytes + out_bytes) / 2**20:.0f} MiB) > L2",
+                   "timing": "K calls back to back, CUDA events at the two ends; latency_us from a second pass "
+                             "with events around each call",
                    "layout": "NHWC" if args.nhwc else "NCHW",
                    "m_storage": "fp32" if args.m_fp32 else "24-bit (F(4x3)) / fp16 (F(2x3))",
                    "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
