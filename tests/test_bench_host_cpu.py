@@ -117,3 +117,23 @@ def test_f2x3_report_records_a_failing_path_instead_of_raising():
     assert set(out) == {"non_fused", "fused"}
     assert out["non_fused"]["error"] == "_Err: cannot plan algorithm 1"
     assert out["fused"]["error"] == "_Err: cannot plan algorithm 2"
+
+
+def test_algorithmic_and_design_bytes():
+    """The roofline counts V + U for the GEMM and y for the output transform
+    (M excluded); the design bytes add M, 24-bit M padded to blocks of 64
+    tiles (N32 C512 28x28 K512: 1568 tiles -> 1600), fp32 and fp16 M not."""
+    b = load_bench()
+    E = 36
+    # N32 C256 56x56 K256, F(4x3): 6272 tiles, a multiple of 64
+    alg, design, flops, _ = b.algorithmic_work("gemm_tcgen05", (32, 256, 56, 56, 256, 4))
+    v, u, m = 2.0 * E * 6272 * 256, 2.0 * E * 256 * 256, 3.0 * E * 6272 * 256
+    assert alg == pytest.approx(v + u) and design == pytest.approx(v + u + m)
+    assert flops == pytest.approx(2.0 * E * 6272 * 256 * 256)
+    # N32 C512 28x28 K512: 1568 tiles, 24-bit M over 1600
+    alg, design, _, _ = b.algorithmic_work("output_transform", (32, 512, 28, 28, 512, 4))
+    y = 2.0 * 32 * 512 * 28 * 28
+    assert alg == pytest.approx(y) and design == pytest.approx(y + 3.0 * E * 1600 * 512)
+    # fp32 M is not padded
+    _, design, _, _ = b.algorithmic_work("output_transform", (32, 512, 28, 28, 512, 4), 4.0)
+    assert design == pytest.approx(y + 4.0 * E * 1568 * 512)
